@@ -1,0 +1,11 @@
+"""GB300-native AFAR per-stage residual + SSP-RK3 update (2-D compressible Euler, unstructured FV).
+
+The compute path is libafar.so (csrc/: sm_103a CUDA kernels + C++ host precompute) behind the C ABI
+in include/afar.h; this package is its Python host mirror (ctypes) plus the synthetic mesh
+generators used by the tests and the benchmark.
+"""
+from . import mesh  # noqa: F401
+from ._ffi import AfarError, lib  # noqa: F401
+from .solver import CaseConfig, CudaSolver, HostFields, gauss_quadrature, precompute  # noqa: F401
+
+__all__ = ["mesh", "lib", "AfarError", "CaseConfig", "CudaSolver", "HostFields", "precompute", "gauss_quadrature"]

@@ -1,0 +1,839 @@
+// AFAR stage kernels for sm_103a: reconstruct, BVD switch, adaptive flux, fused residual gather +
+// SSP-RK3 update + boundary ghosts, plus the setup kernels that build the device operators.
+//
+// Device layout (one mesh):
+//   per cell      W[Nc+Nb] (ghosts after the cells), U/U0[Nc], grad[2Nc], lim[Nc], si[Nc+Nb]
+//   per slot      slot-major "[slot][ldc]" arrays, slot i of every cell contiguous so that a warp
+//                 of consecutive cells reads one coalesced row per slot:
+//                   sten[maxS]            global stencil cell ids
+//                   cf[maxM]              signed face ids (+f+1 owner side, -(f+1) neighbour side)
+//                   lsm[maxM]             least-squares gradient rows (M1, M2)
+//                   sg[maxM], sr[maxM]    face offset from the cell centre; (delta r, fraction)
+//                   wts[maxM*(maxS+1)]    O3 weights of the cell's side of each face
+//   per face      on[Nf], fd[Nf] (face offsets from owner and neighbour), fs[Nf+Nb] (Sf, |Sf|),
+//                 dtg[Nf] (CFL geometry), fv[2Nf] face values, flux[Nf+Nb]
+// Every kernel here is one thread per cell or per face; every output element has one writer, so
+// the stage is deterministic (no atomics except the min of the time step, which is exact).
+#pragma once
+
+#include "afar_policy.cuh"
+
+namespace afar {
+
+struct StepCtl {
+  unsigned long long dt_bits;  // running min of the CFL time step (bits of a non-negative double)
+  double t;                    // simulated time
+  double t_end;                // > 0: clip the last step to land on t_end
+  double dt_fixed;             // > 0: fixed step, else CFL step
+  double cfl;
+  double last_dt;
+  long long steps;
+};
+
+// The step of the current RK step: fixed or CFL, clipped to t_end; <= 0 means "no step".
+__device__ __forceinline__ double step_dt(const StepCtl* c) {
+  double dt = c->dt_fixed > 0.0 ? c->dt_fixed : __longlong_as_double((long long)c->dt_bits);
+  if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
+  return dt;
+}
+
+template <class P>
+struct StageArgs {
+  using S = typename P::S;
+  using G = typename P::G;
+  int Nc, Nf, Nb, ldc, maxS, maxM;
+  // operators (read-only)
+  const V2<double>* cellC;    // Nc+Nb cell centres, ghosts = boundary face centres
+  const int2* on;             // Nf (owner, neighbour)
+  const V4<G>* fd;            // Nf (xf-x_own, yf-y_own, xf-x_nei, yf-y_nei)
+  const V4<G>* fs;            // Nf+Nb (Sfx, Sfy, magSf, 0)
+  const V2<double>* dtg;      // Nf (delta r, fraction) of the CFL estimate
+  const V2<double>* bn;       // Nb unit normal of each boundary face
+  const uint8_t* btype;       // Nb cudaEulerBCs label
+  const double* vol;          // Nc
+  const uint8_t* nS;          // Nc stencil size
+  const uint8_t* nM;          // Nc faces per cell (compact stencil size)
+  const int* sten;            // [maxS][ldc]
+  const int* cf;              // [maxM][ldc]
+  const V2<S>* lsm;           // [maxM][ldc]
+  const V2<G>* sg;            // [maxM][ldc]
+  const V2<S>* sr;            // [maxM][ldc]
+  const S* wts;               // [maxM*(maxS+1)][ldc]
+  // state and stage intermediates
+  V4<typename P::W>* W;       // Nc+Nb
+  V4<double>* U;              // Nc
+  V4<double>* U0;             // Nc
+  V4<G>* grad;                // 2Nc
+  V4<S>* lim;                 // Nc
+  int8_t* si;                 // 2(Nc+Nb): [2c] troubled-cell flag, [2c+1] final switch type
+  V4<G>* fv;                  // 2Nf
+  V4<typename P::F>* flux;    // Nf+Nb
+  StepCtl* ctl;
+  V4<double>* res_dbg;        // optional residual dump (parity hook)
+  double R, Cv;
+};
+
+// limiterProcess (reference cudaLimiter.h:35-50)
+template <class S, class G>
+__device__ __forceinline__ void limiter_process(S& limiter, S& phif, const S phic, const S phiMax, const S phiMin,
+                                                const G gx, const G gy, const G dx, const G dy) {
+  phif = phic;
+  phif += gx * dx + gy * dy;
+  const S d2 = phif - phic;
+  const S d1 = (phif < phic) * (phiMin - phic) + (phif >= phic) * (phiMax - phic);
+  S yy = fmn(S(2), S(0.5) * d1 / (d2 + (d2 >= S(0)) * AFAR_LIT(S, 1e-10) - (d2 < S(0)) * AFAR_LIT(S, 1e-10)));
+  const bool valid = (fab(d2) >= AFAR_LIT(S, 1e-5));
+  yy = valid * yy + (1 - valid) * S(1);
+  limiter = fmn(limiter, yy);
+}
+
+// reconstruct (reference cudaLimiter.h:53-316): LS gradient, stencil min/max, raw limiter,
+// O3 RBF face values of this cell's side of each internal face, troubled-cell flag.
+template <class P>
+__global__ void __launch_bounds__(128) k_reconstruct(StageArgs<P> a) {
+  using S = typename P::S;
+  using G = typename P::G;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V4<S>* sv = reinterpret_cast<V4<S>*>(smem_raw);  // [maxS][blockDim] staged stencil values
+  const int t = threadIdx.x, B = blockDim.x;
+  const int c = blockIdx.x * B + t;
+  if (c >= a.Nc) return;
+  const int ldc = a.ldc;
+  const int nS = a.nS[c], nM = a.nM[c];
+  const V4<typename P::W> wc = a.W[c];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  for (int i = 0; i < nS; ++i) {
+    const V4<typename P::W> wj = a.W[a.sten[i * ldc + c]];
+    sv[i * B + t] = V4<S>{(S)wj.x, (S)wj.y, (S)wj.z, (S)wj.w};
+  }
+
+  G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
+  for (int i = 0; i < nM; ++i) {  // reference :148-169
+    const V2<S> m = a.lsm[i * ldc + c];
+    const S M1 = m.x, M2 = m.y;
+    const V4<S> v = sv[i * B + t];
+    S dphi = v.x - pc;
+    gPx += M1 * dphi;
+    gPy += M2 * dphi;
+    dphi = v.y - uxc;
+    gUxx += M1 * dphi;
+    gUyx += M2 * dphi;
+    dphi = v.z - uyc;
+    gUxy += M1 * dphi;
+    gUyy += M2 * dphi;
+    dphi = v.w - tc;
+    gTx += M1 * dphi;
+    gTy += M2 * dphi;
+  }
+  a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
+  a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
+
+  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
+  for (int i = 0; i < nM; ++i) {  // reference :190-205
+    const V4<S> v = sv[i * B + t];
+    pMax = fmx(v.x, pMax);
+    pMin = fmn(v.x, pMin);
+    uxMax = fmx(v.y, uxMax);
+    uxMin = fmn(v.y, uxMin);
+    uyMax = fmx(v.z, uyMax);
+    uyMin = fmn(v.z, uyMin);
+    tMax = fmx(v.w, tMax);
+    tMin = fmn(v.w, tMin);
+  }
+
+  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
+  V4<S> L;
+  int8_t flag0;
+  if (fab(tMax - tMin) < VSMALL) {  // reference :208-233
+    L = V4<S>{S(1), S(1), S(1), S(1)};
+    for (int fi = 0; fi < nM; ++fi) {
+      int f = a.cf[fi * ldc + c];
+      const bool isNei = (f < 0);
+      f = abs(f) - 1;
+      if (f >= a.Nf) continue;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      V4<G> o;
+      o.x = (G)(pc) + gPx * dx + gPy * dy;
+      o.y = (G)(uxc) + gUxx * dx + gUyx * dy;
+      o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
+      o.w = (G)(tc) + gTx * dx + gTy * dy;
+      a.fv[2 * f + isNei] = o;
+    }
+    flag0 = 0;
+  } else {  // reference :235-314
+    S lp = S(2), lux = S(2), luy = S(2), lt = S(2);
+    S smooth = S(0);
+    bool notTrouble = true;
+    for (int fi = 0; fi < nM; ++fi) {
+      int f = a.cf[fi * ldc + c];
+      const bool isNei = (f < 0);
+      f = abs(f) - 1;
+      if (f >= a.Nf) continue;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      const V2<S> rf = a.sr[fi * ldc + c];
+      const S deltaR = rf.x, fraction = rf.y;
+      const S* w = a.wts + (size_t)(fi * (a.maxS + 1)) * ldc + c;
+      S wk = w[0];
+      G pf = wk * pc;
+      G uxf = wk * uxc;
+      G uyf = wk * uyc;
+      G tf = wk * tc;
+      for (int ci = 0; ci < nS; ++ci) {
+        wk = w[(size_t)(ci + 1) * ldc];
+        const V4<S> v = sv[ci * B + t];
+        pf += wk * v.x;
+        uxf += wk * v.y;
+        uyf += wk * v.z;
+        tf += wk * v.w;
+      }
+      const S pnb = sv[fi * B + t].x;
+      S phif;
+      V4<G> o;
+      limiter_process(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
+      o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
+      notTrouble = phif > S(0);
+      smooth = fmx(smooth, fab((S(1) - fraction) * pc + fraction * pnb - phif) / deltaR + (pf <= S(0)) * AFAR_LIT(S, 1e20) +
+                               (phif <= S(0)) * AFAR_LIT(S, 1e20));
+      limiter_process(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
+      o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
+      limiter_process(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
+      o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
+      limiter_process(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
+      o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
+      notTrouble = phif > S(0);
+      a.fv[2 * f + isNei] = o;
+    }
+    L.x = fmx(lp, S(0)) * notTrouble;
+    L.y = fmx(lux, S(0)) * notTrouble;
+    L.z = fmx(luy, S(0)) * notTrouble;
+    L.w = fmx(lt, S(0)) * notTrouble;
+    smooth = smooth / (S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
+    flag0 = (smooth > S(1));
+  }
+  a.lim[c] = L;
+  a.si[2 * c] = flag0;
+}
+
+// Limiter maps (reference cudaLimiter.h:14-32)
+template <class S>
+__device__ __forceinline__ S to_bj(const S y) {
+  return fmn(S(2) * y, S(1));
+}
+template <class S>
+__device__ __forceinline__ S to_venkat(const S y) {
+  return fmn((y * y + y + AFAR_LIT(S, 1e-10)) / (y * y + S(0.5) + S(0.5) * y + AFAR_LIT(S, 1e-10)), S(1));
+}
+
+// BVDindicator (reference cudaLimiter.h:319-464): stencil flag counts, BVD test on T, final
+// switch type, limiter transform.
+template <class P>
+__global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
+  using S = typename P::S;
+  using G = typename P::G;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int ldc = a.ldc;
+  const int nS = a.nS[c], nM = a.nM[c];
+  int8_t shockType = a.si[2 * c];
+  int8_t shockTypeExt = shockType;
+  for (int ci = 0; ci < nM; ++ci) {
+    shockType += a.si[2 * a.sten[ci * ldc + c]];
+    shockTypeExt = shockType;
+  }
+  for (int ci = nM; ci < nS; ++ci) shockTypeExt += a.si[2 * a.sten[ci * ldc + c]];
+
+  const S tc = (S)a.W[c].w;
+  const V4<G> g1 = a.grad[2 * c + 1];
+  const G gTx = g1.z, gTy = g1.w;
+  V4<S> L = a.lim[c];
+  int bvdType = 0, bfaces = 0;
+  for (int fi = 0; fi < nM; ++fi) {
+    int f = a.cf[fi * ldc + c];
+    const bool isNei = (f < 0);
+    f = abs(f) - 1;
+    if (f >= a.Nf) {
+      bfaces += 1;
+      if (bfaces >= 2) {  // corner cell: low order
+        bvdType = 1;
+        break;
+      }
+      continue;
+    }
+    const V2<G> d = a.sg[fi * ldc + c];
+    const G tfOwn = a.fv[2 * f].w;
+    const G tfNei = a.fv[2 * f + 1].w;
+    const G tfCur = pick<P>(isNei, !isNei, tfNei, tfOwn);
+    const G tfOther = pick<P>(!isNei, isNei, tfNei, tfOwn);
+    const G lim = to_bj(L.w);
+    const G tfTVD = tc + lim * (gTx * d.x + gTy * d.y);
+    const int typeval = fab(tfTVD - tfOther) < AFAR_LIT(S, 0.5) * fab(tfCur - tfOther);
+    const int notFlat = fab(tfCur - tfOther) > AFAR_LIT(S, 1e-10);
+    const int limited = (lim < AFAR_LIT(S, 0.9)) + (shockTypeExt > 0);
+    bvdType = max(bvdType, notFlat * limited * typeval);
+  }
+  const int finalType = (shockType > 0) * (shockTypeExt > 1) * (-2) + (bvdType > 0);
+  a.si[2 * c + 1] = (int8_t)finalType;
+  const bool isShock = finalType < 0;
+  L.x = pick<P>(isShock, !isShock, to_venkat(L.x), to_bj(L.x));
+  L.y = pick<P>(isShock, !isShock, to_venkat(L.y), to_bj(L.y));
+  L.z = pick<P>(isShock, !isShock, to_venkat(L.z), to_bj(L.z));
+  L.w = pick<P>(isShock, !isShock, to_venkat(L.w), to_bj(L.w));
+  a.lim[c] = L;
+}
+
+// minimizeDeltaValue (reference cudaRiemannSolver.h:7-14)
+template <class D, class G>
+__device__ __forceinline__ D min_delta(const G l, const G r, const G lT, const G rT) {
+  D d = fab(r - l);
+  d = fmn((G)(d), fab(r - lT));
+  d = fmn((G)(d), fab(rT - l));
+  d = fmn((G)(d), fab(rT - lT));
+  d = (r >= l) * d - (r < l) * d;
+  return d;
+}
+
+// KFVSFlux (reference cudaRiemannSolver.h:16-68): adds (kinetic flux - central) so the face
+// carries the kinetic flux-vector-splitting flux.
+template <class D, class RC, class G>
+__device__ __forceinline__ void kfvs_flux(G& rhoFlux, G& rhoUxFlux, G& rhoUyFlux, G& rhoEFlux, const D& rhoL,
+                                          const D& rhoR, const D& pL, const D& pR, const D& uxL, const D& uxR,
+                                          const D& uyL, const D& uyR, const D& tL, const D& tR, const RC& R,
+                                          const RC& Cv, const D magSf, const D Sfx, const D Sfy) {
+  const D nfx = Sfx / magSf;
+  const D nfy = Sfy / magSf;
+  const D uLl = uxL * nfx + uyL * nfy;
+  const D vLl = uyL * nfx - uxL * nfy;
+  const D uRl = uxR * nfx + uyR * nfy;
+  const D vRl = uyR * nfx - uxR * nfy;
+  const D lamL = D(0.5) * rhoL / pL;
+  const D lamR = D(0.5) * rhoR / pR;
+  // the reference writes pi as the float literal 3.141593f; the FP64 policy uses pi itself
+  const D PI = std::is_same<D, float>::value ? (D)3.141593f : (D)3.14159265358979323846;
+  const D m0p = D(0.5) * erfc_(-sqr_(lamL) * uLl);
+  const D m1p = uLl * m0p + D(0.5) * exp_(-lamL * uLl * uLl) / (sqr_(PI * lamL));
+  const D m2p = uLl * m1p + D(0.5) * m0p / lamL;
+  const D m3p = uLl * m2p + m1p / lamL;
+  const D m0n = D(0.5) * erfc_(sqr_(lamR) * uRl);
+  const D m1n = uRl * m0n - D(0.5) * exp_(-lamR * uRl * uRl) / (sqr_(PI * lamR));
+  const D m2n = uRl * m1n + D(0.5) * m0n / lamR;
+  const D m3n = uRl * m2n + m1n / lamR;
+  const D& mvL = vLl;
+  const D& mvR = vRl;
+  const D K = D(2) * Cv / R - D(2);
+  const D trho = rhoL * m1p + rhoR * m1n;
+  const D trhoUx = rhoL * m2p + rhoR * m2n;
+  const D trhoUy = rhoL * m1p * mvL + rhoR * m1n * mvR;
+  const D trhoE = D(0.5) * rhoL * (m3p + m1p * (vLl * mvL + D(0.5) / lamL) + m1p * K * D(0.5) / lamL) +
+                  D(0.5) * rhoR * (m3n + m1n * (vRl * mvR + D(0.5) / lamR) + m1n * K * D(0.5) / lamR);
+  rhoUxFlux += trhoUx * Sfx - trhoUy * Sfy - D(0.5) * ((D)(rhoFlux)*uxL + pL * Sfx) - D(0.5) * ((D)(rhoFlux)*uxR + pR * Sfx);
+  rhoUyFlux += trhoUx * Sfy + trhoUy * Sfx - D(0.5) * ((D)(rhoFlux)*uyL + pL * Sfy) - D(0.5) * ((D)(rhoFlux)*uyR + pR * Sfy);
+  rhoEFlux += trhoE * magSf - D(0.5) * (D)(rhoFlux) * (Cv * tL + D(0.5) * (uxL * uxL + uyL * uyL) + pL / rhoL) -
+              D(0.5) * (D)(rhoFlux) * (Cv * tR + D(0.5) * (uxR * uxR + uyR * uyR) + pR / rhoR);
+  rhoFlux += trho * magSf - D(0.5) * rhoL * (uxL * Sfx + uyL * Sfy) - D(0.5) * rhoR * (uxR * Sfx + uyR * Sfy);
+}
+
+// RoeFlux (reference cudaRiemannSolver.h:71-136): Roe dissipation with a Harten-type entropy fix.
+template <class D, class RC, class G>
+__device__ __forceinline__ void roe_flux(G& rhoFlux, G& rhoUxFlux, G& rhoUyFlux, G& rhoEFlux, const D& rhoL,
+                                         const D& rhoR, const D& pL, const D& pR, const D& uxL, const D& uxR,
+                                         const D& uyL, const D& uyR, const D& tL, const D& tR, const D& deltaP,
+                                         const D& deltaRho, const RC& R, const RC& Cv, const D magSf, const D Sfx,
+                                         const D Sfy) {
+  const D gamma = (Cv + R) / Cv;
+  const D nfx = Sfx / magSf;
+  const D nfy = Sfy / magSf;
+  const D cvL = uxL * nfx + uyL * nfy;
+  const D cvR = uxR * nfx + uyR * nfy;
+  const D hL = Cv * tL + D(0.5) * (uxL * uxL + uyL * uyL) + pL / rhoL;
+  const D hR = Cv * tR + D(0.5) * (uxR * uxR + uyR * uyR) + pR / rhoR;
+  const D tiny = AFAR_LIT(D, 1e-20);
+  const D rhoT = sqr_(fmx(rhoL * rhoR, tiny));
+  const D wL = sqr_(fmx(rhoL, tiny)) / (sqr_(fmx(rhoL, tiny)) + sqr_(fmx(rhoR, tiny)));
+  const D wR = D(1) - wL;
+  const D uxT = uxL * wL + uxR * wR;
+  const D uyT = uyL * wL + uyR * wR;
+  const D hT = hL * wL + hR * wR;
+  const D q2 = uxT * uxT + uyT * uyT;
+  const D cT = sqr_(fmx((gamma - D(1)) * (hT - D(0.5) * q2), tiny));
+  const D cvT = uxT * nfx + uyT * nfy;
+  const D dUx = uxR - uxL;
+  const D dUy = uyR - uyL;
+  const D dCv = dUx * nfx + dUy * nfy;
+  const D r1 = (deltaP - rhoT * cT * dCv) / (D(2) * cT * cT);
+  const D r2 = deltaRho - deltaP / (cT * cT);
+  const D r3 = (deltaP + rhoT * cT * dCv) / (D(2) * cT * cT);
+  const D& UL = cvL;
+  const D& UR = cvR;
+  const D cL = sqr_(fmx((gamma - D(1)) * (hL - D(0.5) * (uxL * uxL + uyL * uyL)), tiny));
+  const D cR = sqr_(fmx((gamma - D(1)) * (hR - D(0.5) * (uxR * uxR + uyR * uyR)), tiny));
+  const D eps0 = AFAR_LIT(D, 1e-30);
+  D eps = D(2) * fmx(D(0), (UR - cR) - (UL - cL));
+  D l1 = fab(cvT - cT);
+  l1 = (l1 >= eps) * l1 + (l1 < eps) * ((l1 * l1 + eps * eps) / (D(2) * eps + eps0));
+  eps = D(2) * fmx(D(0), UR - UL);
+  D l2 = fab(cvT);
+  l2 = (l2 >= eps) * l2 + (l2 < eps) * ((l2 * l2 + eps * eps) / (D(2) * eps + eps0));
+  eps = D(2) * fmx(D(0), (UR + cR) - (UL + cL));
+  D l3 = fab(cvT + cT);
+  l3 = (l3 >= eps) * l3 + (l3 < eps) * ((l3 * l3 + eps * eps) / (D(2) * eps + eps0));
+  rhoFlux -= D(0.5) * (l1 * r1 + l2 * r2 + l3 * r3) * magSf;
+  rhoUxFlux -= D(0.5) * (l1 * r1 * (uxT - cT * nfx) + l2 * (r2 * uxT + rhoT * (dUx - dCv * nfx)) + l3 * r3 * (uxT + cT * nfx)) * magSf;
+  rhoUyFlux -= D(0.5) * (l1 * r1 * (uyT - cT * nfy) + l2 * (r2 * uyT + rhoT * (dUy - dCv * nfy)) + l3 * r3 * (uyT + cT * nfy)) * magSf;
+  rhoEFlux -= D(0.5) *
+              (l1 * r1 * (hT - cT * cvT) + l2 * (r2 * D(0.5) * q2 + rhoT * (uxT * dUx + uyT * dUy - cvT * dCv)) +
+               l3 * r3 * (hT + cT * cvT)) *
+              magSf;
+}
+
+// Out-of-line dissipation with the reference's parameter passing (outputs by reference, float
+// states by const reference) behind a device function-pointer table like the reference's
+// calcFlux[] (cudaRiemannSolver.h:139-152); used by the ref policy's k_flux_ref_layout.
+__device__ __noinline__ void roe_ref(double& rhoFlux, double& rhoUxFlux, double& rhoUyFlux, double& rhoEFlux,
+                                     const float& rhoL, const float& rhoR, const float& pL, const float& pR,
+                                     const float& uxL, const float& uxR, const float& uyL, const float& uyR,
+                                     const float& tL, const float& tR, const float& deltaP, const float& deltaRho,
+                                     const double& R, const double& Cv, const float magSf, const float Sfx,
+                                     const float Sfy) {
+  roe_flux<float, double, double>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoL, rhoR, pL, pR, uxL, uxR, uyL, uyR, tL,
+                                  tR, deltaP, deltaRho, R, Cv, magSf, Sfx, Sfy);
+}
+__device__ __noinline__ void kfvs_ref(double& rhoFlux, double& rhoUxFlux, double& rhoUyFlux, double& rhoEFlux,
+                                      const float& rhoL, const float& rhoR, const float& pL, const float& pR,
+                                      const float& uxL, const float& uxR, const float& uyL, const float& uyR,
+                                      const float& tL, const float& tR, const float& deltaP, const float& deltaRho,
+                                      const double& R, const double& Cv, const float magSf, const float Sfx,
+                                      const float Sfy) {
+  (void)deltaP;
+  (void)deltaRho;
+  kfvs_flux<float, double, double>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoL, rhoR, pL, pR, uxL, uxR, uyL, uyR, tL,
+                                   tR, R, Cv, magSf, Sfx, Sfy);
+}
+__device__ void (*ref_flux_table[])(double&, double&, double&, double&, const float&, const float&, const float&,
+                                    const float&, const float&, const float&, const float&, const float&,
+                                    const float&, const float&, const float&, const float&, const double&,
+                                    const double&, const float, const float, const float) = {roe_ref, kfvs_ref};
+
+// Reference-layout structs (basicDataStructure.h:10-65) for the ref-policy flux kernel below.
+struct RCell { double x, y; };
+struct RFace { double x, y, magSf, Sfx, Sfy; };
+struct RField { double p, Ux, Uy, T; };
+struct RGrad { double gradPx, gradPy, gradUxx, gradUxy, gradUyx, gradUyy, gradTx, gradTy; };
+struct RLim { float pLimiter, UxLimiter, UyLimiter, TLimiter; };
+struct RFlux { double rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux; };
+
+// The ref-policy face flux on the reference's array-of-structs layout, one statement per
+// statement of evaluateFlux (cudaRiemannSolver.h:171-251) in the same order: nvcc's multiply-add
+// fusion depends on how the surrounding code is arranged, and matching the arrangement is what
+// keeps the ref policy's flux bit-identical to the reference kernel's.
+__global__ void __launch_bounds__(128) k_flux_ref_layout(RFlux* __restrict__ Flux, const RField* __restrict__ FD,
+                                                         const RGrad* __restrict__ gradFD,
+                                                         const RLim* __restrict__ limiter,
+                                                         const RField* __restrict__ faceFD,
+                                                         const int8_t* __restrict__ shockIndicator,
+                                                         const RCell* __restrict__ CELL,
+                                                         const RFace* __restrict__ FACE,
+                                                         const int* __restrict__ neighbour, const int facesNum,
+                                                         const int cellsNum, const int totalBoundaryFacesNum,
+                                                         const double R, const double Cv) {
+  const int f = threadIdx.x + blockIdx.x * blockDim.x;
+  if (f < facesNum) {
+    const int own = neighbour[2 * f];
+    const int nei = neighbour[2 * f + 1];
+    const double dxL = FACE[f].x - CELL[own].x;
+    const double dyL = FACE[f].y - CELL[own].y;
+    const double dxR = FACE[f].x - CELL[nei].x;
+    const double dyR = FACE[f].y - CELL[nei].y;
+    const bool tvdL = shockIndicator[2 * own + 1] != 0;
+    const bool tvdR = shockIndicator[2 * nei + 1] != 0;
+    const bool isShock = shockIndicator[2 * own + 1] < 0 || shockIndicator[2 * nei + 1] < 0;
+    const double magSf = FACE[f].magSf;
+    const double Sfx = FACE[f].Sfx;
+    const double Sfy = FACE[f].Sfy;
+    double rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux;
+    float pLf, uxLf, uyLf, tLf, rhoLf, pRf, uxRf, uyRf, tRf, rhoRf, dP, dRho;
+    {
+      const double pLT = FD[own].p + limiter[own].pLimiter * (gradFD[own].gradPx * dxL + gradFD[own].gradPy * dyL);
+      const double uxLT = FD[own].Ux + limiter[own].UxLimiter * (gradFD[own].gradUxx * dxL + gradFD[own].gradUyx * dyL);
+      const double uyLT = FD[own].Uy + limiter[own].UyLimiter * (gradFD[own].gradUxy * dxL + gradFD[own].gradUyy * dyL);
+      const double tLT = FD[own].T + limiter[own].TLimiter * (gradFD[own].gradTx * dxL + gradFD[own].gradTy * dyL);
+      const double rhoLT = pLT / (R * tLT);
+      const double pRT = FD[nei].p + limiter[nei].pLimiter * (gradFD[nei].gradPx * dxR + gradFD[nei].gradPy * dyR);
+      const double uxRT = FD[nei].Ux + limiter[nei].UxLimiter * (gradFD[nei].gradUxx * dxR + gradFD[nei].gradUyx * dyR);
+      const double uyRT = FD[nei].Uy + limiter[nei].UyLimiter * (gradFD[nei].gradUxy * dxR + gradFD[nei].gradUyy * dyR);
+      const double tRT = FD[nei].T + limiter[nei].TLimiter * (gradFD[nei].gradTx * dxR + gradFD[nei].gradTy * dyR);
+      const double rhoRT = pRT / (R * tRT);
+      const double pL = (1 - tvdL) * faceFD[2 * f].p + tvdL * pLT;
+      const double uxL = (1 - tvdL) * faceFD[2 * f].Ux + tvdL * uxLT;
+      const double uyL = (1 - tvdL) * faceFD[2 * f].Uy + tvdL * uyLT;
+      const double tL = (1 - tvdL) * faceFD[2 * f].T + tvdL * tLT;
+      const double rhoL = pL / (R * tL);
+      const double pR = (1 - tvdR) * faceFD[2 * f + 1].p + tvdR * pRT;
+      const double uxR = (1 - tvdR) * faceFD[2 * f + 1].Ux + tvdR * uxRT;
+      const double uyR = (1 - tvdR) * faceFD[2 * f + 1].Uy + tvdR * uyRT;
+      const double tR = (1 - tvdR) * faceFD[2 * f + 1].T + tvdR * tRT;
+      const double rhoR = pR / (R * tR);
+      dP = min_delta<float, double>(pL, pR, pLT, pRT);
+      dRho = min_delta<float, double>(rhoL, rhoR, rhoLT, rhoRT);
+      rhoFlux = 0.5 * rhoL * (uxL * Sfx + uyL * Sfy) + 0.5 * rhoR * (uxR * Sfx + uyR * Sfy);
+      rhoUxFlux = 0.5 * (rhoFlux * uxL + pL * Sfx) + 0.5 * (rhoFlux * uxR + pR * Sfx);
+      rhoUyFlux = 0.5 * (rhoFlux * uyL + pL * Sfy) + 0.5 * (rhoFlux * uyR + pR * Sfy);
+      rhoEFlux = 0.5 * rhoFlux * (Cv * tL + 0.5 * (uxL * uxL + uyL * uyL) + pL / rhoL) +
+                 0.5 * rhoFlux * (Cv * tR + 0.5 * (uxR * uxR + uyR * uyR) + pR / rhoR);
+      pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
+      pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
+    }
+    ref_flux_table[isShock](rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf,
+                            tLf, tRf, dP, dRho, R, Cv, magSf, Sfx, Sfy);
+    Flux[f].rhoFlux = rhoFlux;
+    Flux[f].rhoUxFlux = rhoUxFlux;
+    Flux[f].rhoUyFlux = rhoUyFlux;
+    Flux[f].rhoEFlux = rhoEFlux;
+  }
+  if (f < totalBoundaryFacesNum) {
+    const double Sfx = FACE[facesNum + f].Sfx;
+    const double Sfy = FACE[facesNum + f].Sfy;
+    const double bp = FD[cellsNum + f].p;
+    const double bUx = FD[cellsNum + f].Ux;
+    const double bUy = FD[cellsNum + f].Uy;
+    const double bT = FD[cellsNum + f].T;
+    const double rho = bp / (R * bT);
+    const double rf = rho * (bUx * Sfx + bUy * Sfy);
+    Flux[facesNum + f].rhoFlux = rf;
+    Flux[facesNum + f].rhoUxFlux = rf * bUx + bp * Sfx;
+    Flux[facesNum + f].rhoUyFlux = rf * bUy + bp * Sfy;
+    Flux[facesNum + f].rhoEFlux = rf * (Cv * bT + 0.5 * (bUx * bUx + bUy * bUy) + bp / rho);
+  }
+}
+
+// evaluateFlux (reference cudaRiemannSolver.h:155-271): one thread per internal face, then one per
+// boundary face (ids Nf..Nf+Nb-1; the reference's grid covers boundary faces b < 128*ceil(Nf/128)
+// only, which holds on every mesh with Nf >= Nb).  DT: also reduce the CFL step of the reference's
+// setDeltaT (cudaFieldOperation.h:124-180) from the state at the start of the step.
+template <class P, bool DT>
+__global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
+  using S = typename P::S;
+  using G = typename P::G;
+  using D = typename P::D;
+  using RC = typename P::RC;
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtf = 1e5;
+  if (id < a.Nf) {
+    const int2 on = a.on[id];
+    const int own = on.x, nei = on.y;
+    const V4<G> fd = a.fd[id];
+    const G dxL = fd.x, dyL = fd.y, dxR = fd.z, dyR = fd.w;
+    const int8_t sL = a.si[2 * own + 1], sR = a.si[2 * nei + 1];
+    const bool tvdL = sL != 0, tvdR = sR != 0;
+    const bool isShock = sL < 0 || sR < 0;
+    const V4<G> fs = a.fs[id];
+    const G Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
+    const G R = (G)a.R, Cv = (G)a.Cv;
+    const V4<typename P::W> Wo = a.W[own], Wn = a.W[nei];
+    const V4<G> go0 = a.grad[2 * own], go1 = a.grad[2 * own + 1];
+    const V4<G> gn0 = a.grad[2 * nei], gn1 = a.grad[2 * nei + 1];
+    const V4<S> lo = a.lim[own], ln = a.lim[nei];
+    const V4<G> fo = a.fv[2 * id], fn = a.fv[2 * id + 1];
+    G rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux;
+    D pLf, uxLf, uyLf, tLf, rhoLf, pRf, uxRf, uyRf, tRf, rhoRf, dP, dRho;
+    {
+      const G pLT = (G)Wo.x + lo.x * (go0.x * dxL + go0.y * dyL);
+      const G uxLT = (G)Wo.y + lo.y * (go0.z * dxL + go1.x * dyL);
+      const G uyLT = (G)Wo.z + lo.z * (go0.w * dxL + go1.y * dyL);
+      const G tLT = (G)Wo.w + lo.w * (go1.z * dxL + go1.w * dyL);
+      const G rhoLT = pLT / (R * tLT);
+      const G pRT = (G)Wn.x + ln.x * (gn0.x * dxR + gn0.y * dyR);
+      const G uxRT = (G)Wn.y + ln.y * (gn0.z * dxR + gn1.x * dyR);
+      const G uyRT = (G)Wn.z + ln.z * (gn0.w * dxR + gn1.y * dyR);
+      const G tRT = (G)Wn.w + ln.w * (gn1.z * dxR + gn1.w * dyR);
+      const G rhoRT = pRT / (R * tRT);
+      const G pL = pick<P>(!tvdL, tvdL, fo.x, pLT);
+      const G uxL = pick<P>(!tvdL, tvdL, fo.y, uxLT);
+      const G uyL = pick<P>(!tvdL, tvdL, fo.z, uyLT);
+      const G tL = pick<P>(!tvdL, tvdL, fo.w, tLT);
+      const G rhoL = pL / (R * tL);
+      const G pR = pick<P>(!tvdR, tvdR, fn.x, pRT);
+      const G uxR = pick<P>(!tvdR, tvdR, fn.y, uxRT);
+      const G uyR = pick<P>(!tvdR, tvdR, fn.z, uyRT);
+      const G tR = pick<P>(!tvdR, tvdR, fn.w, tRT);
+      const G rhoR = pR / (R * tR);
+      dP = min_delta<D, G>(pL, pR, pLT, pRT);
+      dRho = min_delta<D, G>(rhoL, rhoR, rhoLT, rhoRT);
+      const G h = G(0.5);
+      rhoFlux = h * rhoL * (uxL * Sfx + uyL * Sfy) + h * rhoR * (uxR * Sfx + uyR * Sfy);
+      rhoUxFlux = h * (rhoFlux * uxL + pL * Sfx) + h * (rhoFlux * uxR + pR * Sfx);
+      rhoUyFlux = h * (rhoFlux * uyL + pL * Sfy) + h * (rhoFlux * uyR + pR * Sfy);
+      rhoEFlux = h * rhoFlux * (Cv * tL + h * (uxL * uxL + uyL * uyL) + pL / rhoL) +
+                 h * rhoFlux * (Cv * tR + h * (uxR * uxR + uyR * uyR) + pR / rhoR);
+      pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
+      pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
+    }
+    const RC Rr = (RC)a.R, Cvr = (RC)a.Cv;
+    if (isShock)
+      kfvs_flux<D, RC, G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
+                          tRf, Rr, Cvr, (D)magSf, (D)Sfx, (D)Sfy);
+    else
+      roe_flux<D, RC, G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
+                         tRf, dP, dRho, Rr, Cvr, (D)magSf, (D)Sfx, (D)Sfy);
+    a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)rhoUxFlux, (typename P::F)rhoUyFlux,
+                                   (typename P::F)rhoEFlux};
+    if (DT) {
+      const StepCtl* ctl = a.ctl;
+      if (!(ctl->dt_fixed > 0.0)) {  // setDeltaT, cudaFieldOperation.h:140-157
+        const V2<double> g = a.dtg[id];
+        const double deltaR = g.x, fraction = g.y;
+        const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
+        const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
+        dtf = CFL * deltaR * msf /
+              ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
+               fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
+               sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
+      }
+    }
+  } else if (id < a.Nf + a.Nb) {  // boundary faces, reference :254-270
+    const int b = id - a.Nf;
+    const V4<typename P::W> wb = a.W[a.Nc + b];
+    const V4<G> fs = a.fs[id];
+    const G Sfx = fs.x, Sfy = fs.y;
+    const G R = (G)a.R, Cv = (G)a.Cv;
+    const G bp = wb.x, bUx = wb.y, bUy = wb.z, bT = wb.w;
+    const G rho = bp / (R * bT);
+    const G rhoFlux = rho * (bUx * Sfx + bUy * Sfy);
+    a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)(rhoFlux * bUx + bp * Sfx),
+                                   (typename P::F)(rhoFlux * bUy + bp * Sfy),
+                                   (typename P::F)(rhoFlux * (Cv * bT + G(0.5) * (bUx * bUx + bUy * bUy) + bp / rho))};
+  }
+  if (DT) {
+    // block min (warp shuffles) then one atomicMin per block on the bit pattern; non-negative
+    // doubles order like their bit patterns, and NaN patterns sort above +inf.
+    unsigned long long v = (unsigned long long)__double_as_longlong(dtf);
+    if (!(dtf >= 0.0)) v = 0x7FF0000000000000ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+      v = u < v ? u : v;
+    }
+    __shared__ unsigned long long wmin[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmin[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long m = wmin[0];
+      for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = wmin[k] < m ? wmin[k] : m;
+      atomicMin(&a.ctl->dt_bits, m);
+    }
+  }
+}
+
+// Ghost state of boundary face b from its owner's state (reference cudaEulerBCs.h:45-95 and
+// BCs/2D/<label>.h:4-10).
+__device__ __forceinline__ V4<double> boundary_value(const int type, const V4<double> w, const V2<double> n) {
+  switch (type) {
+    case 0:  // constantTemperatureWallBoundary
+      return V4<double>{w.x, 0.0, 0.0, 1.0};
+    case 1:  // adiabaticWallBoundary
+      return V4<double>{w.x, 0.0, 0.0, w.w};
+    case 2:  // symmetryBoundary
+      return V4<double>{w.x, w.y - (w.y * n.x + w.z * n.y) * n.x, w.z - (w.y * n.x + w.z * n.y) * n.y, w.w};
+    case 3:  // fixedValueBoundary
+      return V4<double>{1.0, 3.0, 0.0, 1.0};
+    case 4:  // outletBoundary
+      return w;
+    case 5:  // fixedValue2Boundary
+      return V4<double>{30.05945, 4.07795, 0.0, 5.97677};
+    default:
+      return w;
+  }
+}
+
+// evaluateResidual + updateFieldData + updateBoundaryFieldData (+ storeConservedFieldData on the
+// last stage), reference cudaFieldOperation.h:183-268, cudaEulerBCs.h:64-95: signed gather of the
+// face fluxes in the cell's face order (no atomics), SSP-RK3 combine, conserved -> primitive, and
+// the ghost state of this cell's boundary faces from the new state.
+template <class P>
+__global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double beta1, const double beta2,
+                                                const double beta3, const int last_stage) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const double deltaT = step_dt(a.ctl);
+  if (!(deltaT > 0.0)) return;  // past t_end: the step is a no-op
+  const int ldc = a.ldc;
+  const int nM = a.nM[c];
+  double Rrho = 0.0, RrhoUx = 0.0, RrhoUy = 0.0, RrhoE = 0.0;
+  for (int fi = 0; fi < nM; ++fi) {
+    int f = a.cf[fi * ldc + c];
+    const int direction = (f > 0) - (f < 0);
+    f = abs(f) - 1;
+    const V4<typename P::F> fl = a.flux[f];
+    Rrho += direction * (double)fl.x;
+    RrhoUx += direction * (double)fl.y;
+    RrhoUy += direction * (double)fl.z;
+    RrhoE += direction * (double)fl.w;
+  }
+  if (a.res_dbg) a.res_dbg[c] = V4<double>{Rrho, RrhoUx, RrhoUy, RrhoE};
+  const double V = a.vol[c];
+  const V4<double> o = a.U0[c];
+  const V4<double> u = a.U[c];
+  const double rho = beta1 * o.x + beta2 * u.x + beta3 * deltaT * (-Rrho / V);
+  const double rhoUx = beta1 * o.y + beta2 * u.y + beta3 * deltaT * (-RrhoUx / V);
+  const double rhoUy = beta1 * o.z + beta2 * u.z + beta3 * deltaT * (-RrhoUy / V);
+  const double rhoE = beta1 * o.w + beta2 * u.w + beta3 * deltaT * (-RrhoE / V);
+  const V4<double> un{rho, rhoUx, rhoUy, rhoE};
+  a.U[c] = un;
+  if (last_stage) a.U0[c] = un;
+  const double R = a.R;
+  const double gamma = a.R / a.Cv + 1.0;
+  const double p = (gamma - 1.0) * (rhoE - 0.5 * (rhoUx * rhoUx + rhoUy * rhoUy) / rho);
+  using WT = typename P::W;
+  const V4<WT> wn{(WT)p, (WT)(rhoUx / rho), (WT)(rhoUy / rho), (WT)(p / (R * rho))};
+  a.W[c] = wn;
+  for (int fi = 0; fi < nM; ++fi) {
+    const int f = abs(a.cf[fi * ldc + c]) - 1;
+    if (f < a.Nf) continue;
+    const int b = f - a.Nf;
+    const V4<double> g =
+        boundary_value(a.btype[b], V4<double>{(double)wn.x, (double)wn.y, (double)wn.z, (double)wn.w}, a.bn[b]);
+    a.W[a.Nc + b] = V4<WT>{(WT)g.x, (WT)g.y, (WT)g.z, (WT)g.w};
+  }
+}
+
+// Closes a step: advance time, record the step, re-arm the CFL minimum for the next step.
+__global__ void k_finish_step(StepCtl* ctl) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double dt = step_dt(ctl);
+    if (dt > 0.0) {
+      ctl->t += dt;
+      ctl->steps += 1;
+      ctl->last_dt = dt;
+    }
+    ctl->dt_bits = (unsigned long long)__double_as_longlong(1e5);
+  }
+}
+
+// The CFL step alone (adjustTimeStep of the drop-in API): min over internal faces into *bits.
+// With ctl != nullptr (the step graph) it reduces into ctl->dt_bits with ctl->cfl, and does nothing
+// when the step size is fixed.
+template <class P>
+__global__ void __launch_bounds__(256) k_delta_t(StageArgs<P> a, double CFL, unsigned long long* bits,
+                                                 const StepCtl* ctl) {
+  if (ctl) {
+    if (ctl->dt_fixed > 0.0) return;
+    CFL = ctl->cfl;
+  }
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  double dtf = 1e5;
+  if (id < a.Nf) {
+    const int2 on = a.on[id];
+    const V4<typename P::W> Wo = a.W[on.x], Wn = a.W[on.y];
+    const V4<typename P::G> fs = a.fs[id];
+    const double sfx = (double)fs.x, sfy = (double)fs.y, msf = (double)fs.z;
+    const V2<double> g = a.dtg[id];
+    const double deltaR = g.x, fraction = g.y, Rd = a.R, Cvd = a.Cv;
+    dtf = CFL * deltaR * msf /
+          ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
+           fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
+           sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
+  }
+  unsigned long long v = (unsigned long long)__double_as_longlong(dtf);
+  if (!(dtf >= 0.0)) v = 0x7FF0000000000000ull;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = u < v ? u : v;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMin(bits, v);
+}
+
+// ---------------------------------------------------------------------------------- setup kernels
+
+// calcLeastSquareMatrix (reference cudaFieldOperation.h:91-120) into the slot-major matrix, in
+// FP64 math, stored in the policy's operator type.
+template <class P>
+__global__ void k_setup_lsm(StageArgs<P> a, V2<typename P::S>* lsm, float* lsm_ref_layout, int maxM_ref) {
+  using S = typename P::S;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int m = a.nM[c];
+  double Sxx = 0.0, Sxy = 0.0, Syy = 0.0;
+  const double x0 = a.cellC[c].x, y0 = a.cellC[c].y;
+  for (int i = 0; i < m; ++i) {
+    const int j = a.sten[i * a.ldc + c];
+    const double xj = a.cellC[j].x, yj = a.cellC[j].y;
+    Sxx += (xj - x0) * (xj - x0);
+    Sxy += (xj - x0) * (yj - y0);
+    Syy += (yj - y0) * (yj - y0);
+  }
+  for (int i = 0; i < m; ++i) {
+    const int j = a.sten[i * a.ldc + c];
+    const double xj = a.cellC[j].x, yj = a.cellC[j].y;
+    const S m1 = (Syy * (xj - x0) - Sxy * (yj - y0)) / (Sxx * Syy - Sxy * Sxy);
+    const S m2 = (-Sxy * (xj - x0) + Sxx * (yj - y0)) / (Sxx * Syy - Sxy * Sxy);
+    lsm[i * a.ldc + c] = V2<S>{m1, m2};
+    if (lsm_ref_layout) {
+      lsm_ref_layout[2 * (size_t)maxM_ref * c + 2 * i] = (float)m1;
+      lsm_ref_layout[2 * (size_t)maxM_ref * c + 2 * i + 1] = (float)m2;
+    }
+  }
+}
+
+// Geometry constants of each (cell, face slot): the face offset from the cell centre and the
+// (delta r, fraction) pair reconstruct uses, with the reference's expressions
+// (cudaLimiter.h:258-262), so the values are bit-identical to what its kernel computes per stage.
+template <class P>
+__global__ void k_setup_slot_geom(StageArgs<P> a, const V4<double>* faceXY) {
+  using S = typename P::S;
+  using G = typename P::G;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int m = a.nM[c];
+  const double x0 = a.cellC[c].x, y0 = a.cellC[c].y;
+  V2<G>* sg = const_cast<V2<G>*>(a.sg);
+  V2<S>* sr = const_cast<V2<S>*>(a.sr);
+  for (int fi = 0; fi < m; ++fi) {
+    const int f = abs(a.cf[fi * a.ldc + c]) - 1;
+    const double dx = faceXY[f].x - x0;
+    const double dy = faceXY[f].y - y0;
+    sg[fi * a.ldc + c] = V2<G>{(G)dx, (G)dy};
+    S dR = S(1), fr = S(0);
+    if (f < a.Nf) {
+      const int nb = a.sten[fi * a.ldc + c];
+      const float deltaR = hypot(a.cellC[nb].x - x0, a.cellC[nb].y - y0);
+      const float fraction = sqrt(dx * dx + dy * dy) / deltaR;
+      if (P::id == PolicyFP64::id) {
+        const double dRd = hypot(a.cellC[nb].x - x0, a.cellC[nb].y - y0);
+        dR = (S)dRd;
+        fr = (S)(sqrt(dx * dx + dy * dy) / dRd);
+      } else {
+        dR = (S)deltaR;
+        fr = (S)fraction;
+      }
+    }
+    sr[fi * a.ldc + c] = V2<S>{dR, fr};
+  }
+}
+
+// Per-face constants: offsets of the face centre from owner and neighbour (evaluateFlux :178-182),
+// the CFL geometry (setDeltaT :145-146), face vectors, boundary unit normals (symmetryBoundary.h).
+template <class P>
+__global__ void k_setup_face_geom(StageArgs<P> a, const V4<double>* faceXY, const V4<double>* faceS) {
+  using G = typename P::G;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= a.Nf + a.Nb) return;
+  const V4<double> xy = faceXY[f];  // x, y
+  const V4<double> s = faceS[f];    // Sfx, Sfy, magSf
+  const_cast<V4<G>*>(a.fs)[f] = V4<G>{(G)s.x, (G)s.y, (G)s.z, G(0)};
+  if (f < a.Nf) {
+    const int2 on = a.on[f];
+    const V2<double> co = a.cellC[on.x], cn = a.cellC[on.y];
+    const_cast<V4<G>*>(a.fd)[f] = V4<G>{(G)(xy.x - co.x), (G)(xy.y - co.y), (G)(xy.x - cn.x), (G)(xy.y - cn.y)};
+    const double deltaR = hypot(cn.x - co.x, cn.y - co.y);
+    const double fraction = hypot(xy.x - co.x, xy.y - co.y) / deltaR;
+    const_cast<V2<double>*>(a.dtg)[f] = V2<double>{deltaR, fraction};
+  } else {
+    const int b = f - a.Nf;
+    const_cast<V2<double>*>(a.bn)[b] = V2<double>{s.x / s.z, s.y / s.z};
+  }
+}
+
+}  // namespace afar

@@ -1,0 +1,910 @@
+// libafar host<->device boundary: the drop-in replacement of the reference's GPUevolve.{h,cu}
+// (setDeviceFieldData x2, adjustTimeStep, GPUevolve, copyFieldDataDeviceToHost, freeFieldData),
+// plus graph-captured multi-step runs and per-stage parity hooks.
+//
+// The caller hands over the reference's host arrays (include/afar.h afar_fieldPointer); the
+// library re-lays them out on the device (slot-major per-cell lists, per-face geometry constants,
+// policy-typed intermediates; see afar_kernels.cuh) and owns all device memory.
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <algorithm>
+#include <vector>
+
+#include "afar_internal.h"
+#include "afar_kernels.cuh"
+
+using namespace afar;
+
+#define AFAR_CUDA(call)                                                                      \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess) {                                                                 \
+      set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return AFAR_ERR_CUDA;                                                                  \
+    }                                                                                        \
+  } while (0)
+
+namespace {
+
+constexpr int kCellBlock = 128;
+constexpr int kFaceBlock = 256;
+// GPUevolve.cu:223-225: the reference's truncated SSP-RK3 coefficients
+constexpr double kBeta1[3] = {1.0, 0.75, 0.333333};
+constexpr double kBeta2[3] = {0.0, 0.25, 0.666667};
+constexpr double kBeta3[3] = {1.0, 0.25, 0.666667};
+
+struct FaceRaw {
+  double x, y, magSf, Sfx, Sfy;
+};
+
+// setup kernels that only move the reference arrays into the device layout
+__global__ void k_setup_lists(int Nc, int ldc, int maxS, int maxM, int maxLB, const uint8_t* nS, const uint8_t* nM,
+                              const uint16_t* localStencil, const int* extendStencil, const int* cellFaces, int* sten,
+                              int* cf) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= Nc) return;
+  const int blk = c / AFAR_BLOCKDIM;
+  for (int i = 0; i < nS[c]; ++i) {
+    const int loc = localStencil[(size_t)maxS * c + i];
+    sten[(size_t)i * ldc + c] =
+        loc < AFAR_BLOCKDIM ? blk * AFAR_BLOCKDIM + loc : extendStencil[(size_t)(maxLB - AFAR_BLOCKDIM) * blk + (loc - AFAR_BLOCKDIM)];
+  }
+  for (int i = 0; i < nM[c]; ++i) cf[(size_t)i * ldc + c] = cellFaces[(size_t)maxM * c + i];
+}
+
+__global__ void k_split_faces(int n, const FaceRaw* raw, V4<double>* xy, V4<double>* s) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= n) return;
+  const FaceRaw r = raw[f];
+  xy[f] = V4<double>{r.x, r.y, 0.0, 0.0};
+  s[f] = V4<double>{r.Sfx, r.Sfy, r.magSf, 0.0};
+}
+
+template <class T, class Src>
+__global__ void k_setup_wts(int Nc, int Nf, int ldc, int maxS, const uint8_t* nS, const uint8_t* nM, const int* cf,
+                            const Src* rbf, T* wts) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= Nc) return;
+  const size_t nmax = (size_t)maxS + 1;
+  for (int fi = 0; fi < nM[c]; ++fi) {
+    int f = cf[(size_t)fi * ldc + c];
+    const int side = f < 0;
+    f = abs(f) - 1;
+    if (f >= Nf) continue;
+    const Src* src = rbf + 2 * nmax * f + side * nmax;
+    T* dst = wts + (size_t)fi * nmax * ldc + c;
+    for (int j = 0; j <= nS[c]; ++j) dst[(size_t)j * ldc] = (T)src[j];
+  }
+}
+
+__global__ void k_set_ctl(StepCtl* ctl, double dt_fixed, double cfl, double t_end) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    ctl->dt_fixed = dt_fixed;
+    ctl->cfl = cfl;
+    ctl->t_end = t_end;
+  }
+}
+
+__global__ void k_init_ctl(StepCtl* ctl) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    ctl->dt_bits = (unsigned long long)__double_as_longlong(1e5);
+    ctl->t = 0.0;
+    ctl->t_end = 0.0;
+    ctl->dt_fixed = 0.0;
+    ctl->cfl = 0.5;
+    ctl->last_dt = 0.0;
+    ctl->steps = 0;
+  }
+}
+
+template <class A, class B>
+__global__ void k_convert4(int n, const V4<A>* in, V4<B>* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = V4<B>{(B)in[i].x, (B)in[i].y, (B)in[i].z, (B)in[i].w};
+}
+
+inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+
+}  // namespace
+
+struct afar_solver {
+  int policy = AFAR_POLICY_REF;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // sizes
+  int Nc = 0, Nf = 0, Nb = 0, patches = 0, maxS = 0, maxM = 0, maxLB = 0, maxCLB = 0, ldc = 0;
+  bool have_fields = false, have_stencil = false;
+  double R = 0.0, Cv = 0.0;  // of the captured graph
+  // policy-independent device arrays
+  V2<double>* cellC = nullptr;
+  FaceRaw* faceRaw = nullptr;
+  double* vol = nullptr;
+  int2* on = nullptr;
+  int* bnei = nullptr;
+  uint8_t* btype = nullptr;
+  uint8_t* nS = nullptr;
+  uint8_t* nM = nullptr;
+  int* sten = nullptr;
+  int* cf = nullptr;
+  V4<double>* U = nullptr;
+  V4<double>* U0 = nullptr;
+  int8_t* si = nullptr;
+  V2<double>* dtg = nullptr;
+  V2<double>* bn = nullptr;
+  V4<double>* res_dbg = nullptr;
+  StepCtl* ctl = nullptr;
+  unsigned long long* dt_bits = nullptr;
+  // policy-typed device arrays (element size depends on the policy)
+  void* W = nullptr;
+  void* fd = nullptr;
+  void* fs = nullptr;
+  void* lsm = nullptr;
+  void* sg = nullptr;
+  void* sr = nullptr;
+  void* wts = nullptr;
+  void* grad = nullptr;
+  void* lim = nullptr;
+  void* fv = nullptr;
+  void* flux = nullptr;
+  std::vector<double> rbf64;  // optional FP64 weights awaiting the stencil upload
+  cudaGraphExec_t graph = nullptr;
+  size_t bytes = 0;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+afar_status dalloc(afar_solver* s, void** p, size_t bytes) {
+  *p = nullptr;
+  if (bytes == 0) bytes = 16;
+  AFAR_CUDA(cudaMalloc(p, bytes));
+  s->allocs.push_back(*p);
+  s->bytes += bytes;
+  return AFAR_OK;
+}
+template <class T>
+afar_status dalloc_t(afar_solver* s, T** p, size_t n) {
+  return dalloc(s, reinterpret_cast<void**>(p), n * sizeof(T));
+}
+
+template <class P>
+StageArgs<P> make_args(afar_solver* s) {
+  StageArgs<P> a;
+  using S = typename P::S;
+  using G = typename P::G;
+  a.Nc = s->Nc;
+  a.Nf = s->Nf;
+  a.Nb = s->Nb;
+  a.ldc = s->ldc;
+  a.maxS = s->maxS;
+  a.maxM = s->maxM;
+  a.cellC = s->cellC;
+  a.on = s->on;
+  a.fd = static_cast<const V4<G>*>(s->fd);
+  a.fs = static_cast<const V4<G>*>(s->fs);
+  a.dtg = s->dtg;
+  a.bn = s->bn;
+  a.btype = s->btype;
+  a.vol = s->vol;
+  a.nS = s->nS;
+  a.nM = s->nM;
+  a.sten = s->sten;
+  a.cf = s->cf;
+  a.lsm = static_cast<const V2<S>*>(s->lsm);
+  a.sg = static_cast<const V2<G>*>(s->sg);
+  a.sr = static_cast<const V2<S>*>(s->sr);
+  a.wts = static_cast<const S*>(s->wts);
+  a.W = static_cast<V4<typename P::W>*>(s->W);
+  a.U = s->U;
+  a.U0 = s->U0;
+  a.grad = static_cast<V4<G>*>(s->grad);
+  a.lim = static_cast<V4<S>*>(s->lim);
+  a.si = s->si;
+  a.fv = static_cast<V4<G>*>(s->fv);
+  a.flux = static_cast<V4<typename P::F>*>(s->flux);
+  a.ctl = s->ctl;
+  a.res_dbg = nullptr;
+  a.R = s->R;
+  a.Cv = s->Cv;
+  return a;
+}
+
+template <class P>
+size_t recon_smem(const afar_solver* s) {
+  return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
+}
+
+// Enqueues one RK stage.  dt_stage: fuse the CFL reduction into the flux kernel.
+// The face flux of one stage.  The ref policy runs the reference-layout kernel (its fused
+// multiply-adds then fall where the reference's do) and, on the first stage, the CFL step as a
+// kernel of its own like the reference's setDeltaT; the other policies fuse the CFL reduction
+// into the flux kernel.
+template <class P>
+void enqueue_flux(afar_solver* s, const StageArgs<P>& a, bool dt_stage) {
+  if constexpr (P::id == PolicyRef::id) {
+    if (dt_stage && s->Nf > 0)
+      k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
+    const int gr = grid_for(std::max(s->Nf, s->Nb), 128);
+    k_flux_ref_layout<<<gr, 128, 0, s->stream>>>(
+        reinterpret_cast<RFlux*>(s->flux), reinterpret_cast<const RField*>(s->W), reinterpret_cast<const RGrad*>(s->grad),
+        reinterpret_cast<const RLim*>(s->lim), reinterpret_cast<const RField*>(s->fv), s->si,
+        reinterpret_cast<const RCell*>(s->cellC), reinterpret_cast<const RFace*>(s->faceRaw),
+        reinterpret_cast<const int*>(s->on), s->Nf, s->Nc, s->Nb, a.R, a.Cv);
+  } else {
+    const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
+    if (dt_stage)
+      k_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(a);
+    else
+      k_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(a);
+  }
+}
+
+template <class P>
+void enqueue_stage(afar_solver* s, const StageArgs<P>& a, int k, bool dt_stage) {
+  const int gc = grid_for(s->Nc, kCellBlock);
+  k_reconstruct<P><<<gc, kCellBlock, recon_smem<P>(s), s->stream>>>(a);
+  k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
+  enqueue_flux<P>(s, a, dt_stage);
+  k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+}
+
+template <class P>
+void enqueue_step(afar_solver* s) {
+  const StageArgs<P> a = make_args<P>(s);
+  for (int k = 0; k < 3; ++k) enqueue_stage<P>(s, a, k, k == 0);
+  k_finish_step<<<1, 32, 0, s->stream>>>(s->ctl);
+}
+
+template <class P>
+afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
+  using S = typename P::S;
+  using G = typename P::G;
+  const int Nc = s->Nc, Nf = s->Nf, Nb = s->Nb, ldc = s->ldc;
+  afar_status st;
+  if ((st = dalloc(s, &s->fd, sizeof(V4<G>) * (size_t)Nf))) return st;
+  if ((st = dalloc(s, &s->fs, sizeof(V4<G>) * (size_t)(Nf + Nb)))) return st;
+  if ((st = dalloc(s, &s->lsm, sizeof(V2<S>) * (size_t)s->maxM * ldc))) return st;
+  if ((st = dalloc(s, &s->sg, sizeof(V2<G>) * (size_t)s->maxM * ldc))) return st;
+  if ((st = dalloc(s, &s->sr, sizeof(V2<S>) * (size_t)s->maxM * ldc))) return st;
+  if ((st = dalloc(s, &s->wts, sizeof(S) * (size_t)s->maxM * (s->maxS + 1) * ldc))) return st;
+  AFAR_CUDA(cudaMemsetAsync(s->wts, 0, sizeof(S) * (size_t)s->maxM * (s->maxS + 1) * ldc, s->stream));
+  AFAR_CUDA(cudaMemsetAsync(s->lsm, 0, sizeof(V2<S>) * (size_t)s->maxM * ldc, s->stream));
+
+  // O3 weights: float reference layout (or the FP64 copy) -> slot-major
+  const size_t nrbf = 2 * (size_t)(s->maxS + 1) * Nf;
+  const int gc = grid_for(Nc, kCellBlock);
+  if (std::is_same<S, double>::value && s->rbf64.size() == nrbf) {
+    double* tmp = nullptr;
+    AFAR_CUDA(cudaMalloc(&tmp, sizeof(double) * (nrbf ? nrbf : 1)));
+    AFAR_CUDA(cudaMemcpyAsync(tmp, s->rbf64.data(), sizeof(double) * nrbf, cudaMemcpyHostToDevice, s->stream));
+    k_setup_wts<S, double><<<gc, kCellBlock, 0, s->stream>>>(Nc, Nf, ldc, s->maxS, s->nS, s->nM, s->cf, tmp,
+                                                             static_cast<S*>(s->wts));
+    AFAR_CUDA(cudaStreamSynchronize(s->stream));
+    AFAR_CUDA(cudaFree(tmp));
+  } else {
+    float* tmp = nullptr;
+    AFAR_CUDA(cudaMalloc(&tmp, sizeof(float) * (nrbf ? nrbf : 1)));
+    AFAR_CUDA(cudaMemcpyAsync(tmp, h->RBFbasis, sizeof(float) * nrbf, cudaMemcpyHostToDevice, s->stream));
+    k_setup_wts<S, float><<<gc, kCellBlock, 0, s->stream>>>(Nc, Nf, ldc, s->maxS, s->nS, s->nM, s->cf, tmp,
+                                                            static_cast<S*>(s->wts));
+    AFAR_CUDA(cudaStreamSynchronize(s->stream));
+    AFAR_CUDA(cudaFree(tmp));
+  }
+  s->rbf64.clear();
+  s->rbf64.shrink_to_fit();
+
+  V4<double>* fxy = nullptr;
+  V4<double>* fsr = nullptr;
+  AFAR_CUDA(cudaMalloc(&fxy, sizeof(V4<double>) * (size_t)(Nf + Nb + 1)));
+  AFAR_CUDA(cudaMalloc(&fsr, sizeof(V4<double>) * (size_t)(Nf + Nb + 1)));
+  const int gF = grid_for((long long)Nf + Nb, kFaceBlock);
+  k_split_faces<<<gF, kFaceBlock, 0, s->stream>>>(Nf + Nb, s->faceRaw, fxy, fsr);
+  StageArgs<P> a = make_args<P>(s);
+  k_setup_lsm<P><<<gc, kCellBlock, 0, s->stream>>>(a, static_cast<V2<S>*>(s->lsm), nullptr, 0);
+  k_setup_slot_geom<P><<<gc, kCellBlock, 0, s->stream>>>(a, fxy);
+  k_setup_face_geom<P><<<gF, kFaceBlock, 0, s->stream>>>(a, fxy, fsr);
+  AFAR_CUDA(cudaGetLastError());
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaFree(fxy));
+  AFAR_CUDA(cudaFree(fsr));
+  const size_t smem = recon_smem<P>(s);
+  AFAR_CUDA(cudaFuncSetAttribute(k_reconstruct<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  return AFAR_OK;
+}
+
+afar_status capture_graph(afar_solver* s) {
+  if (s->graph) {
+    AFAR_CUDA(cudaGraphExecDestroy(s->graph));
+    s->graph = nullptr;
+  }
+  cudaGraph_t g = nullptr;
+  AFAR_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  switch (s->policy) {
+    case AFAR_POLICY_REF: enqueue_step<PolicyRef>(s); break;
+    case AFAR_POLICY_FP64: enqueue_step<PolicyFP64>(s); break;
+    default: enqueue_step<PolicyMixed>(s); break;
+  }
+  AFAR_CUDA(cudaStreamEndCapture(s->stream, &g));
+  const cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    set_error("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
+    s->graph = nullptr;
+    return AFAR_ERR_CUDA;
+  }
+  return AFAR_OK;
+}
+
+afar_status check_ready(afar_solver* s) {
+  if (!s) {
+    set_error("null solver");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if (!s->have_fields || !s->have_stencil) {
+    set_error("call afar_setDeviceFieldData and afar_setDeviceFieldDataStencil first");
+    return AFAR_ERR_STATE;
+  }
+  AFAR_CUDA(cudaSetDevice(s->device));
+  return AFAR_OK;
+}
+
+size_t w_size(int policy) { return policy == AFAR_POLICY_MIXED ? sizeof(V4<float>) : sizeof(V4<double>); }
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+extern "C" afar_status afar_solver_create(afar_solver** out, int policy, int device) {
+  if (!out || policy < AFAR_POLICY_REF || policy > AFAR_POLICY_MIXED) {
+    set_error("afar_solver_create: null output or unknown policy %d", policy);
+    return AFAR_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  int n = 0;
+  AFAR_CUDA(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) {
+    set_error("afar_solver_create: device %d not present (%d devices)", device, n);
+    return AFAR_ERR_ARGUMENT;
+  }
+  AFAR_CUDA(cudaSetDevice(device));
+  afar_solver* s = new afar_solver();
+  s->policy = policy;
+  s->device = device;
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    delete s;
+    return AFAR_ERR_CUDA;
+  }
+  *out = s;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldPointer* h, int cellsNum, int facesNum,
+                                               int totalBoundaryFacesNum) {
+  if (!s || !h || !h->CELL || !h->FACE || !h->cellVolume || !h->FD || !h->cFD || cellsNum <= 0 || facesNum < 0 ||
+      totalBoundaryFacesNum < 0) {
+    set_error("afar_setDeviceFieldData: null array or bad size");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if (s->have_fields) {
+    set_error("afar_setDeviceFieldData: already called on this solver");
+    return AFAR_ERR_STATE;
+  }
+  AFAR_CUDA(cudaSetDevice(s->device));
+  s->Nc = cellsNum;
+  s->Nf = facesNum;
+  s->Nb = totalBoundaryFacesNum;
+  s->ldc = (cellsNum + 31) / 32 * 32;
+  const size_t Nc = cellsNum, Nf = facesNum, Nb = totalBoundaryFacesNum;
+  afar_status st;
+  if ((st = dalloc_t(s, &s->cellC, Nc + Nb))) return st;
+  if ((st = dalloc_t(s, &s->faceRaw, Nf + Nb))) return st;
+  if ((st = dalloc_t(s, &s->vol, Nc))) return st;
+  if ((st = dalloc_t(s, &s->U, Nc))) return st;
+  if ((st = dalloc_t(s, &s->U0, Nc))) return st;
+  if ((st = dalloc_t(s, &s->si, 2 * (Nc + Nb)))) return st;
+  if ((st = dalloc_t(s, &s->ctl, 1))) return st;
+  if ((st = dalloc_t(s, &s->dt_bits, 1))) return st;
+  if ((st = dalloc(s, &s->W, w_size(s->policy) * (Nc + Nb)))) return st;
+  AFAR_CUDA(cudaMemcpyAsync(s->cellC, h->CELL, sizeof(V2<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaMemcpyAsync(s->faceRaw, h->FACE, sizeof(FaceRaw) * (Nf + Nb), cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaMemcpyAsync(s->vol, h->cellVolume, sizeof(double) * Nc, cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaMemcpyAsync(s->U, h->cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaMemcpyAsync(s->U0, h->cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaMemsetAsync(s->si, 0, 2 * (Nc + Nb), s->stream));
+  if (s->policy == AFAR_POLICY_MIXED) {
+    V4<double>* tmp = nullptr;
+    AFAR_CUDA(cudaMalloc(&tmp, sizeof(V4<double>) * (Nc + Nb)));
+    AFAR_CUDA(cudaMemcpyAsync(tmp, h->FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
+    k_convert4<double, float><<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>((int)(Nc + Nb), tmp,
+                                                                            static_cast<V4<float>*>(s->W));
+    AFAR_CUDA(cudaStreamSynchronize(s->stream));
+    AFAR_CUDA(cudaFree(tmp));
+  } else {
+    AFAR_CUDA(cudaMemcpyAsync(s->W, h->FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
+  }
+  k_init_ctl<<<1, 32, 0, s->stream>>>(s->ctl);
+  // intermediates
+  const size_t g = s->policy == AFAR_POLICY_MIXED ? sizeof(V4<float>) : sizeof(V4<double>);
+  const size_t l = s->policy == AFAR_POLICY_FP64 ? sizeof(V4<double>) : sizeof(V4<float>);
+  if ((st = dalloc(s, &s->grad, g * 2 * Nc))) return st;
+  if ((st = dalloc(s, &s->lim, l * Nc))) return st;
+  if ((st = dalloc(s, &s->fv, g * 2 * Nf))) return st;
+  if ((st = dalloc(s, &s->flux, g * (Nf + Nb)))) return st;
+  if ((st = dalloc_t(s, &s->dtg, Nf))) return st;
+  if ((st = dalloc_t(s, &s->bn, Nb))) return st;
+  AFAR_CUDA(cudaMemsetAsync(s->fv, 0, g * 2 * Nf, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  s->have_fields = true;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_set_rbf_basis64(afar_solver* s, const double* rbf, size_t count) {
+  if (!s || (!rbf && count)) {
+    set_error("afar_set_rbf_basis64: null argument");
+    return AFAR_ERR_ARGUMENT;
+  }
+  s->rbf64.assign(rbf, rbf + count);
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar_fieldPointer* h, int cellsNum,
+                                                      int facesNum, int patchesNum, int totalBoundaryFacesNum,
+                                                      int maxStencilSize, int maxCompactStencilSize,
+                                                      int maxLocalBlockStencilSize,
+                                                      int maxCompactLocalBlockStencilSize) {
+  if (!s || !h) {
+    set_error("afar_setDeviceFieldDataStencil: null argument");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if (!s->have_fields) {
+    set_error("afar_setDeviceFieldDataStencil: call afar_setDeviceFieldData first");
+    return AFAR_ERR_STATE;
+  }
+  if (s->have_stencil) {
+    set_error("afar_setDeviceFieldDataStencil: already called on this solver");
+    return AFAR_ERR_STATE;
+  }
+  if (cellsNum != s->Nc || facesNum != s->Nf || totalBoundaryFacesNum != s->Nb) {
+    set_error("afar_setDeviceFieldDataStencil: sizes differ from afar_setDeviceFieldData");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if (maxStencilSize < 1 || maxStencilSize > AFAR_MAX_VALID_STENCIL_SIZE || maxCompactStencilSize < 1 ||
+      maxCompactStencilSize > maxStencilSize || maxLocalBlockStencilSize < AFAR_BLOCKDIM ||
+      maxCompactLocalBlockStencilSize < AFAR_BLOCKDIM || patchesNum < 0) {
+    set_error("afar_setDeviceFieldDataStencil: stencil sizes out of range (maxS %d, maxM %d, maxLB %d)",
+              maxStencilSize, maxCompactStencilSize, maxLocalBlockStencilSize);
+    return AFAR_ERR_LIMIT;
+  }
+  if (!h->neighbour && facesNum > 0) return (set_error("neighbour is null"), AFAR_ERR_ARGUMENT);
+  if (!h->stencilSize || !h->compactStencilSize || !h->localStencil || !h->cellFaces || !h->RBFbasis ||
+      (totalBoundaryFacesNum > 0 && (!h->boundaryFaceNeiLabel || !h->boundaryFacesType)) ||
+      (maxLocalBlockStencilSize > AFAR_BLOCKDIM && !h->extendStencil)) {
+    set_error("afar_setDeviceFieldDataStencil: null stencil array");
+    return AFAR_ERR_ARGUMENT;
+  }
+  AFAR_CUDA(cudaSetDevice(s->device));
+  const int Nc = s->Nc, Nf = s->Nf, Nb = s->Nb;
+  // host-side validation of everything a kernel indexes with
+  for (int c = 0; c < Nc; ++c) {
+    if (h->stencilSize[c] > maxStencilSize || h->compactStencilSize[c] > maxCompactStencilSize ||
+        h->compactStencilSize[c] > h->stencilSize[c]) {
+      set_error("cell %d: stencil sizes %d/%d exceed the declared maxima", c, h->stencilSize[c], h->compactStencilSize[c]);
+      return AFAR_ERR_ARGUMENT;
+    }
+    for (int i = 0; i < h->compactStencilSize[c]; ++i) {
+      const int fid = h->cellFaces[(size_t)maxCompactStencilSize * c + i];
+      const int f = (fid < 0 ? -fid : fid) - 1;
+      if (fid == 0 || f >= Nf + Nb || (f >= Nf && fid < 0)) {
+        set_error("cell %d: cellFaces entry %d out of range", c, fid);
+        return AFAR_ERR_ARGUMENT;
+      }
+    }
+    const int blk = c / AFAR_BLOCKDIM;
+    for (int i = 0; i < h->stencilSize[c]; ++i) {
+      const int loc = h->localStencil[(size_t)maxStencilSize * c + i];
+      if (loc >= maxLocalBlockStencilSize) {
+        set_error("cell %d: localStencil entry %d out of range", c, loc);
+        return AFAR_ERR_ARGUMENT;
+      }
+      const int g = loc < AFAR_BLOCKDIM ? blk * AFAR_BLOCKDIM + loc
+                                        : h->extendStencil[(size_t)(maxLocalBlockStencilSize - AFAR_BLOCKDIM) * blk + (loc - AFAR_BLOCKDIM)];
+      if (g < 0 || g >= Nc + Nb || (loc < AFAR_BLOCKDIM && g >= Nc)) {
+        set_error("cell %d: stencil member %d out of range", c, g);
+        return AFAR_ERR_ARGUMENT;
+      }
+    }
+  }
+  for (int f = 0; f < Nf; ++f) {
+    const int o = h->neighbour[2 * f], n = h->neighbour[2 * f + 1];
+    if (o < 0 || o >= Nc || n < 0 || n >= Nc) {
+      set_error("face %d: owner/neighbour (%d, %d) out of range", f, o, n);
+      return AFAR_ERR_ARGUMENT;
+    }
+  }
+  for (int b = 0; b < Nb; ++b) {
+    if (h->boundaryFaceNeiLabel[b] < 0 || h->boundaryFaceNeiLabel[b] >= Nc) {
+      set_error("boundary face %d: owner out of range", b);
+      return AFAR_ERR_ARGUMENT;
+    }
+    if (h->boundaryFacesType[b] > 5) {
+      set_error("boundary face %d: unknown cudaEulerBCs label %d (0-5)", b, h->boundaryFacesType[b]);
+      return AFAR_ERR_ARGUMENT;
+    }
+  }
+  s->patches = patchesNum;
+  s->maxS = maxStencilSize;
+  s->maxM = maxCompactStencilSize;
+  s->maxLB = maxLocalBlockStencilSize;
+  s->maxCLB = maxCompactLocalBlockStencilSize;
+  const size_t ldc = s->ldc;
+  afar_status st;
+  if ((st = dalloc_t(s, &s->on, (size_t)Nf))) return st;
+  if ((st = dalloc_t(s, &s->bnei, (size_t)Nb))) return st;
+  if ((st = dalloc_t(s, &s->btype, (size_t)Nb))) return st;
+  if ((st = dalloc_t(s, &s->nS, (size_t)Nc))) return st;
+  if ((st = dalloc_t(s, &s->nM, (size_t)Nc))) return st;
+  if ((st = dalloc_t(s, &s->sten, (size_t)s->maxS * ldc))) return st;
+  if ((st = dalloc_t(s, &s->cf, (size_t)s->maxM * ldc))) return st;
+  AFAR_CUDA(cudaMemsetAsync(s->sten, 0, sizeof(int) * s->maxS * ldc, s->stream));
+  AFAR_CUDA(cudaMemsetAsync(s->cf, 0, sizeof(int) * s->maxM * ldc, s->stream));
+  if (Nf) AFAR_CUDA(cudaMemcpyAsync(s->on, h->neighbour, sizeof(int2) * Nf, cudaMemcpyHostToDevice, s->stream));
+  if (Nb) {
+    AFAR_CUDA(cudaMemcpyAsync(s->bnei, h->boundaryFaceNeiLabel, sizeof(int) * Nb, cudaMemcpyHostToDevice, s->stream));
+    AFAR_CUDA(cudaMemcpyAsync(s->btype, h->boundaryFacesType, Nb, cudaMemcpyHostToDevice, s->stream));
+  }
+  AFAR_CUDA(cudaMemcpyAsync(s->nS, h->stencilSize, Nc, cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaMemcpyAsync(s->nM, h->compactStencilSize, Nc, cudaMemcpyHostToDevice, s->stream));
+  {
+    uint16_t* dls = nullptr;
+    int* dext = nullptr;
+    int* dcf = nullptr;
+    const size_t nblk = (Nc + AFAR_BLOCKDIM - 1) / AFAR_BLOCKDIM;
+    const size_t next = (size_t)(s->maxLB - AFAR_BLOCKDIM) * nblk;
+    AFAR_CUDA(cudaMalloc(&dls, sizeof(uint16_t) * (size_t)s->maxS * Nc));
+    AFAR_CUDA(cudaMalloc(&dext, sizeof(int) * (next ? next : 1)));
+    AFAR_CUDA(cudaMalloc(&dcf, sizeof(int) * (size_t)s->maxM * Nc));
+    AFAR_CUDA(cudaMemcpyAsync(dls, h->localStencil, sizeof(uint16_t) * (size_t)s->maxS * Nc, cudaMemcpyHostToDevice, s->stream));
+    if (next) AFAR_CUDA(cudaMemcpyAsync(dext, h->extendStencil, sizeof(int) * next, cudaMemcpyHostToDevice, s->stream));
+    AFAR_CUDA(cudaMemcpyAsync(dcf, h->cellFaces, sizeof(int) * (size_t)s->maxM * Nc, cudaMemcpyHostToDevice, s->stream));
+    k_setup_lists<<<grid_for(Nc, kCellBlock), kCellBlock, 0, s->stream>>>(Nc, s->ldc, s->maxS, s->maxM, s->maxLB, s->nS,
+                                                                           s->nM, dls, dext, dcf, s->sten, s->cf);
+    AFAR_CUDA(cudaGetLastError());
+    AFAR_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(dls);
+    cudaFree(dext);
+    cudaFree(dcf);
+  }
+  switch (s->policy) {
+    case AFAR_POLICY_REF: st = setup_operators<PolicyRef>(s, h); break;
+    case AFAR_POLICY_FP64: st = setup_operators<PolicyFP64>(s, h); break;
+    default: st = setup_operators<PolicyMixed>(s, h); break;
+  }
+  if (st) return st;
+  if ((st = dalloc_t(s, &s->res_dbg, (size_t)Nc))) return st;
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  s->have_stencil = true;
+  return AFAR_OK;
+}
+
+static afar_status ensure_graph(afar_solver* s, double R, double Cv) {
+  if (!s->graph || s->R != R || s->Cv != Cv) {
+    if (!s->have_stencil) {  // capture needs the operators; keep the constants for later
+      s->R = R;
+      s->Cv = Cv;
+      return AFAR_OK;
+    }
+    s->R = R;
+    s->Cv = Cv;
+    return capture_graph(s);
+  }
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_adjustTimeStep(afar_solver* s, int facesNum, double R, double Cv, double CFL, double* dt) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!dt || facesNum != s->Nf || !(R > 0.0) || !(Cv > 0.0) || !(CFL > 0.0)) {
+    set_error("afar_adjustTimeStep: bad argument");
+    return AFAR_ERR_ARGUMENT;
+  }
+  const unsigned long long init = 0x40F86A0000000000ull;  // bits of 1e5
+  AFAR_CUDA(cudaMemcpyAsync(s->dt_bits, &init, sizeof(init), cudaMemcpyHostToDevice, s->stream));
+  const int gf = grid_for(s->Nf, kFaceBlock);
+  if (s->Nf > 0) {
+    switch (s->policy) {
+      case AFAR_POLICY_REF: {
+        StageArgs<PolicyRef> a = make_args<PolicyRef>(s);
+        a.R = R;
+        a.Cv = Cv;
+        k_delta_t<PolicyRef><<<gf, kFaceBlock, 0, s->stream>>>(a, CFL, s->dt_bits, nullptr);
+        break;
+      }
+      case AFAR_POLICY_FP64: {
+        StageArgs<PolicyFP64> a = make_args<PolicyFP64>(s);
+        a.R = R;
+        a.Cv = Cv;
+        k_delta_t<PolicyFP64><<<gf, kFaceBlock, 0, s->stream>>>(a, CFL, s->dt_bits, nullptr);
+        break;
+      }
+      default: {
+        StageArgs<PolicyMixed> a = make_args<PolicyMixed>(s);
+        a.R = R;
+        a.Cv = Cv;
+        k_delta_t<PolicyMixed><<<gf, kFaceBlock, 0, s->stream>>>(a, CFL, s->dt_bits, nullptr);
+        break;
+      }
+    }
+  }
+  unsigned long long bits = 0;
+  AFAR_CUDA(cudaMemcpyAsync(&bits, s->dt_bits, sizeof(bits), cudaMemcpyDeviceToHost, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  double v;
+  std::memcpy(&v, &bits, sizeof(v));
+  *dt = v;
+  return AFAR_OK;
+}
+
+static afar_status run_impl(afar_solver* s, int nSteps, double dt, double CFL, double tEnd, bool wait) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (nSteps < 0 || (!(dt > 0.0) && !(CFL > 0.0))) {
+    set_error("afar_run: nSteps must be >= 0 and either deltaT > 0 or CFL > 0");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
+  if ((st = ensure_graph(s, s->R, s->Cv))) return st;
+  k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, tEnd);
+  for (int i = 0; i < nSteps; ++i) AFAR_CUDA(cudaGraphLaunch(s->graph, s->stream));
+  if (wait) AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_GPUevolve(afar_solver* s, double R, double Cv, double deltaT, int cellsNum, int facesNum,
+                                      int totalBoundaryFacesNum, int maxStencilSize, int maxCompactStencilSize,
+                                      int maxLocalBlockStencilSize, int maxCompactLocalBlockStencilSize) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (cellsNum != s->Nc || facesNum != s->Nf || totalBoundaryFacesNum != s->Nb || maxStencilSize != s->maxS ||
+      maxCompactStencilSize != s->maxM) {
+    set_error("afar_GPUevolve: sizes differ from the uploaded fields");
+    return AFAR_ERR_ARGUMENT;
+  }
+  (void)maxLocalBlockStencilSize;
+  (void)maxCompactLocalBlockStencilSize;
+  if (!(deltaT > 0.0) || !(R > 0.0) || !(Cv > 0.0)) {
+    set_error("afar_GPUevolve: deltaT, R and Cv must be positive");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if ((st = ensure_graph(s, R, Cv))) return st;
+  return run_impl(s, 1, deltaT, 1.0, 0.0, true);
+}
+
+extern "C" afar_status afar_set_gas(afar_solver* s, double R, double Cv) {
+  if (!s || !(R > 0.0) || !(Cv > 0.0)) {
+    set_error("afar_set_gas: bad argument");
+    return AFAR_ERR_ARGUMENT;
+  }
+  return ensure_graph(s, R, Cv);
+}
+
+extern "C" afar_status afar_run(afar_solver* s, int nSteps, double deltaT, double CFL, double tEnd) {
+  return run_impl(s, nSteps, deltaT, CFL, tEnd, true);
+}
+
+extern "C" afar_status afar_run_async(afar_solver* s, int nSteps, double deltaT, double CFL, double tEnd) {
+  return run_impl(s, nSteps, deltaT, CFL, tEnd, false);
+}
+
+extern "C" afar_status afar_synchronize(afar_solver* s) {
+  if (!s) return (set_error("null solver"), AFAR_ERR_ARGUMENT);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_get_stream(afar_solver* s, void** stream) {
+  if (!s || !stream) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  *stream = (void*)s->stream;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_get_time(afar_solver* s, double* t, double* lastDt, long long* steps) {
+  if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  StepCtl c;
+  AFAR_CUDA(cudaMemcpyAsync(&c, s->ctl, sizeof(c), cudaMemcpyDeviceToHost, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  if (t) *t = c.t;
+  if (lastDt) *lastDt = c.last_dt;
+  if (steps) *steps = c.steps;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_set_time(afar_solver* s, double t) {
+  if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  AFAR_CUDA(cudaMemcpyAsync(&s->ctl->t, &t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_stage_debug(afar_solver* s, int stage, double deltaT, afar_fieldPointer* out) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (stage < 0 || stage > 2 || !(deltaT > 0.0) || !out) {
+    set_error("afar_stage_debug: stage must be 0..2, deltaT > 0, out non-null");
+    return AFAR_ERR_ARGUMENT;
+  }
+  if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
+  k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, deltaT, 1.0, 0.0);
+  const size_t Nc = s->Nc, Nf = s->Nf, Nb = s->Nb;
+  const int gc = grid_for(s->Nc, kCellBlock);
+  const bool mixed = s->policy == AFAR_POLICY_MIXED;
+  const bool f64 = s->policy == AFAR_POLICY_FP64;
+  auto run = [&](auto tag) {
+    using P = decltype(tag);
+    StageArgs<P> a = make_args<P>(s);
+    a.res_dbg = s->res_dbg;
+    k_reconstruct<P><<<gc, kCellBlock, recon_smem<P>(s), s->stream>>>(a);
+    k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
+    enqueue_flux<P>(s, a, false);
+    k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[stage], kBeta2[stage], kBeta3[stage], stage == 2);
+  };
+  switch (s->policy) {
+    case AFAR_POLICY_REF: run(PolicyRef{}); break;
+    case AFAR_POLICY_FP64: run(PolicyFP64{}); break;
+    default: run(PolicyMixed{}); break;
+  }
+  AFAR_CUDA(cudaGetLastError());
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  // copy out in the reference layout
+  auto get4 = [&](void* dst, const void* src, size_t n, bool is_float) -> afar_status {
+    if (!is_float) {
+      AFAR_CUDA(cudaMemcpy(dst, src, n * sizeof(V4<double>), cudaMemcpyDeviceToHost));
+    } else {
+      std::vector<V4<float>> tmp(n);
+      AFAR_CUDA(cudaMemcpy(tmp.data(), src, n * sizeof(V4<float>), cudaMemcpyDeviceToHost));
+      V4<double>* d = static_cast<V4<double>*>(dst);
+      for (size_t i = 0; i < n; ++i) d[i] = V4<double>{tmp[i].x, tmp[i].y, tmp[i].z, tmp[i].w};
+    }
+    return AFAR_OK;
+  };
+  if (out->faceFD && (st = get4(out->faceFD, s->fv, 2 * Nf, mixed))) return st;
+  if (out->gradFD && (st = get4(out->gradFD, s->grad, 2 * Nc, mixed))) return st;
+  if (out->Flux && (st = get4(out->Flux, s->flux, Nf + Nb, mixed))) return st;
+  if (out->FD && (st = get4(out->FD, s->W, Nc + Nb, mixed))) return st;
+  if (out->cFD) AFAR_CUDA(cudaMemcpy(out->cFD, s->U, Nc * sizeof(V4<double>), cudaMemcpyDeviceToHost));
+  if (out->Res) AFAR_CUDA(cudaMemcpy(out->Res, s->res_dbg, Nc * sizeof(V4<double>), cudaMemcpyDeviceToHost));
+  if (out->shockIndicator) AFAR_CUDA(cudaMemcpy(out->shockIndicator, s->si, 2 * (Nc + Nb), cudaMemcpyDeviceToHost));
+  if (out->limiter) {
+    if (f64) {
+      std::vector<V4<double>> tmp(Nc);
+      AFAR_CUDA(cudaMemcpy(tmp.data(), s->lim, Nc * sizeof(V4<double>), cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < Nc; ++i)
+        out->limiter[i] = afar_limiterFieldData{(float)tmp[i].x, (float)tmp[i].y, (float)tmp[i].z, (float)tmp[i].w};
+    } else {
+      AFAR_CUDA(cudaMemcpy(out->limiter, s->lim, Nc * sizeof(V4<float>), cudaMemcpyDeviceToHost));
+    }
+  }
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_debug_limiter64(afar_solver* s, double* lim) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!lim) return (set_error("null output"), AFAR_ERR_ARGUMENT);
+  const size_t Nc = s->Nc;
+  if (s->policy == AFAR_POLICY_FP64) {
+    AFAR_CUDA(cudaMemcpy(lim, s->lim, Nc * sizeof(V4<double>), cudaMemcpyDeviceToHost));
+  } else {
+    std::vector<float> tmp(4 * Nc);
+    AFAR_CUDA(cudaMemcpy(tmp.data(), s->lim, Nc * sizeof(V4<float>), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < 4 * Nc; ++i) lim[i] = tmp[i];
+  }
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_upload_state(afar_solver* s, const afar_basicFieldData* FD, const afar_conservedFieldData* cFD,
+                                         const afar_conservedFieldData* cFDold) {
+  if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  const size_t Nc = s->Nc, Nb = s->Nb;
+  if (FD) {
+    if (s->policy == AFAR_POLICY_MIXED) {
+      std::vector<V4<float>> tmp(Nc + Nb);
+      for (size_t i = 0; i < Nc + Nb; ++i)
+        tmp[i] = V4<float>{(float)FD[i].p, (float)FD[i].Ux, (float)FD[i].Uy, (float)FD[i].T};
+      AFAR_CUDA(cudaMemcpy(s->W, tmp.data(), sizeof(V4<float>) * (Nc + Nb), cudaMemcpyHostToDevice));
+    } else {
+      AFAR_CUDA(cudaMemcpy(s->W, FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice));
+    }
+  }
+  if (cFD) AFAR_CUDA(cudaMemcpy(s->U, cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice));
+  if (cFDold) AFAR_CUDA(cudaMemcpy(s->U0, cFDold, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice));
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_download_state(afar_solver* s, afar_basicFieldData* FD, afar_conservedFieldData* cFD,
+                                           int8_t* shockIndicator) {
+  if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  const size_t Nc = s->Nc, Nb = s->Nb;
+  if (FD) {
+    if (s->policy == AFAR_POLICY_MIXED) {
+      std::vector<V4<float>> tmp(Nc + Nb);
+      AFAR_CUDA(cudaMemcpy(tmp.data(), s->W, sizeof(V4<float>) * (Nc + Nb), cudaMemcpyDeviceToHost));
+      for (size_t i = 0; i < Nc + Nb; ++i) FD[i] = afar_basicFieldData{tmp[i].x, tmp[i].y, tmp[i].z, tmp[i].w};
+    } else {
+      AFAR_CUDA(cudaMemcpy(FD, s->W, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyDeviceToHost));
+    }
+  }
+  if (cFD) AFAR_CUDA(cudaMemcpy(cFD, s->U, sizeof(V4<double>) * Nc, cudaMemcpyDeviceToHost));
+  if (shockIndicator) AFAR_CUDA(cudaMemcpy(shockIndicator, s->si, 2 * (Nc + Nb), cudaMemcpyDeviceToHost));
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_copyFieldDataDeviceToHost(afar_fieldPointer* h, afar_solver* s, int cellsNum,
+                                                      int totalBoundaryFacesNum) {
+  if (!h || !s) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  if (cellsNum != s->Nc || totalBoundaryFacesNum != s->Nb) {
+    set_error("afar_copyFieldDataDeviceToHost: sizes differ from the uploaded fields");
+    return AFAR_ERR_ARGUMENT;
+  }
+  return afar_download_state(s, h->FD, nullptr, h->shockIndicator);
+}
+
+extern "C" afar_status afar_download_ls_matrix(afar_solver* s, float* matrix) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!matrix) return (set_error("null output"), AFAR_ERR_ARGUMENT);
+  float* d = nullptr;
+  const size_t n = 2 * (size_t)s->maxM * s->Nc;
+  AFAR_CUDA(cudaMalloc(&d, n * sizeof(float)));
+  AFAR_CUDA(cudaMemsetAsync(d, 0, n * sizeof(float), s->stream));
+  const int gc = grid_for(s->Nc, kCellBlock);
+  void* scratch = nullptr;
+  const size_t sl = (s->policy == AFAR_POLICY_FP64 ? sizeof(V2<double>) : sizeof(V2<float>)) * (size_t)s->maxM * s->ldc;
+  AFAR_CUDA(cudaMalloc(&scratch, sl));
+  switch (s->policy) {
+    case AFAR_POLICY_REF:
+      k_setup_lsm<PolicyRef><<<gc, kCellBlock, 0, s->stream>>>(make_args<PolicyRef>(s), static_cast<V2<float>*>(scratch), d, s->maxM);
+      break;
+    case AFAR_POLICY_FP64:
+      k_setup_lsm<PolicyFP64><<<gc, kCellBlock, 0, s->stream>>>(make_args<PolicyFP64>(s), static_cast<V2<double>*>(scratch), d, s->maxM);
+      break;
+    default:
+      k_setup_lsm<PolicyMixed><<<gc, kCellBlock, 0, s->stream>>>(make_args<PolicyMixed>(s), static_cast<V2<float>*>(scratch), d, s->maxM);
+      break;
+  }
+  AFAR_CUDA(cudaGetLastError());
+  AFAR_CUDA(cudaMemcpyAsync(matrix, d, n * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  cudaFree(d);
+  cudaFree(scratch);
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_device_bytes(afar_solver* s, size_t* bytes) {
+  if (!s || !bytes) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  *bytes = s->bytes;
+  return AFAR_OK;
+}
+
+extern "C" int afar_launches_per_step(afar_solver* s) { return s && s->policy == AFAR_POLICY_REF ? 14 : 13; }
+
+extern "C" afar_status afar_freeFieldData(afar_solver* s) {
+  if (!s) return AFAR_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (void* p : s->allocs) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return AFAR_OK;
+}

@@ -1,0 +1,297 @@
+"""Host-side mirror of the reference's solver object over the libafar C ABI.
+
+``HostFields`` is the reference's host ``fieldPointer`` as numpy arrays (basicDataStructure.h).
+``precompute`` does what ``basicCUDAsolver::initFieldInfo`` + ``initStencilData`` do with OpenFOAM
+(basicCUDAsolver.cpp:122-851), in native code.  ``CudaSolver`` follows ``basicCUDAsolver``
+(basicCUDAsolver.h:44-52): construct = precompute + both ``setDeviceFieldData`` uploads,
+``set_delta_t`` = ``adjustTimeStep``, ``evolve(dt)`` = ``GPUevolve``, ``write_field`` =
+``copyFieldDataDeviceToHost``; plus ``run`` (graph-captured multi-step with a device-side CFL
+step) and ``stage_debug`` (per-stage intermediates for parity checks).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import check, lib, ptr
+from .mesh import FoamMesh
+
+_MEMBERS = [f[0] for f in _ffi.FieldPointer._fields_]
+
+
+@dataclasses.dataclass
+class CaseConfig:
+    """fvSchemes/controlDict settings the reference reads (basicCUDAsolver.cpp:55-68)."""
+    R: float = 1.0 / 1.4
+    Cv: float = 1.0 / 1.4 / 0.4
+    CFL: float = 0.5
+    shapeFactor: float = 10.0
+    stencilType: str = "edgeNeighbour"
+    cOrder: int = 5
+    fOrder: int = 4
+    nThreads: int = 0
+
+    def to_c(self):
+        c = _ffi.CaseConfig()
+        c.R, c.Cv, c.CFL, c.shapeFactor = self.R, self.Cv, self.CFL, self.shapeFactor
+        c.stencilType = {"faceNeighbour": 0, "edgeNeighbour": 1}[self.stencilType]
+        c.cOrder, c.fOrder, c.nThreads = self.cOrder, self.fOrder, self.nThreads
+        return c
+
+
+class HostFields:
+    """The reference's host field bundle as numpy arrays plus its integer sizes."""
+
+    def __init__(self, sizes: dict, arrays: dict):
+        self.sizes = dict(sizes)
+        self.a = dict(arrays)
+
+    def __getattr__(self, k):
+        a = self.__dict__.get("a", {})
+        if k in a:
+            return a[k]
+        raise AttributeError(k)
+
+    @property
+    def nc(self):
+        return self.sizes["cellsNum"]
+
+    @property
+    def nf(self):
+        return self.sizes["facesNum"]
+
+    @property
+    def nb(self):
+        return self.sizes["totalBoundaryFacesNum"]
+
+    def shapes(self):
+        s = self.sizes
+        nc, nf, nb = s["cellsNum"], s["facesNum"], s["totalBoundaryFacesNum"]
+        maxS, maxM, maxLB = s["maxStencilSize"], s["maxCompactStencilSize"], s["maxLocalBlockStencilSize"]
+        nblk = (nc + _ffi.BLOCKDIM - 1) // _ffi.BLOCKDIM
+        return {
+            "CELL": ((nc + nb, 2), np.float64), "FACE": ((nf + nb, 5), np.float64), "cellVolume": ((nc,), np.float64),
+            "FD": ((nc + nb, 4), np.float64), "limiter": ((nc, 4), np.float32),
+            "shockIndicator": ((2 * (nc + nb),), np.int8), "cFD": ((nc, 4), np.float64),
+            "cFDold": ((nc, 4), np.float64), "gradFD": ((nc, 8), np.float64), "Flux": ((nf + nb, 4), np.float64),
+            "Res": ((nc, 4), np.float64), "neighbour": ((2 * nf,), np.int32),
+            "boundaryFacesNum": ((s["patchesNum"],), np.int32), "boundaryFaceNeiLabel": ((nb,), np.int32),
+            "boundaryFacesType": ((nb,), np.uint8), "stencilSize": ((nc,), np.uint8),
+            "compactStencilSize": ((nc,), np.uint8), "RBFbasis": ((2 * (maxS + 1) * nf,), np.float32),
+            "faceFD": ((2 * nf, 4), np.float64), "extendStencil": (((maxLB - _ffi.BLOCKDIM) * nblk,), np.int32),
+            "extendStencilSize": ((nblk,), np.uint16), "compactExtendStencilSize": ((nblk,), np.uint16),
+            "localStencil": ((maxS * nc,), np.uint16), "matrix": ((2 * maxM * nc,), np.float32),
+            "cellFaces": ((maxM * nc,), np.int32), "minDeltaT": (((nf + 1023) // 1024,), np.float64),
+        }
+
+    def empty_like_outputs(self, names):
+        sh = self.shapes()
+        return {n: np.zeros(sh[n][0], dtype=sh[n][1]) for n in names}
+
+    def to_c(self, only=None):
+        fp = _ffi.FieldPointer()
+        for n in _MEMBERS:
+            if only is not None and n not in only:
+                continue
+            a = self.a.get(n)
+            if a is not None:
+                setattr(fp, n, ptr(np.ascontiguousarray(a)) if a.flags["C_CONTIGUOUS"] else None)
+        return fp
+
+    @staticmethod
+    def from_c(fp: _ffi.FieldPointer, sz: _ffi.FieldSizes):
+        sizes = {n: getattr(sz, n) for n, _ in _ffi.FieldSizes._fields_}
+        hf = HostFields(sizes, {})
+        for n, (shape, dt) in hf.shapes().items():
+            p = getattr(fp, n)
+            count = int(np.prod(shape))
+            if p is None or count == 0:
+                hf.a[n] = np.zeros(shape, dtype=dt)
+                continue
+            buf = (C.c_byte * (count * np.dtype(dt).itemsize)).from_address(p)
+            hf.a[n] = np.frombuffer(buf, dtype=dt).reshape(shape).copy()
+        return hf
+
+
+def poly_mesh_c(mesh: FoamMesh):
+    """afar_polyMesh view of a FoamMesh; returns (struct, keep-alive list)."""
+    keep = [np.ascontiguousarray(mesh.points, dtype=np.float64), np.ascontiguousarray(mesh.cell_ptr, dtype=np.int32),
+            np.ascontiguousarray(mesh.cell_pts, dtype=np.int32), np.ascontiguousarray(mesh.face_pts, dtype=np.int32),
+            np.ascontiguousarray(mesh.owner, dtype=np.int32), np.ascontiguousarray(mesh.neighbour, dtype=np.int32),
+            np.array([p[2] for p in mesh.patches], dtype=np.int32),
+            np.array([p[3] for p in mesh.patches], dtype=np.int32),
+            np.array([p[1] for p in mesh.patches], dtype=np.int32)]
+    m = _ffi.PolyMesh()
+    m.nPoints = keep[0].shape[0]
+    m.points = ptr(keep[0])
+    m.nCells = keep[1].shape[0] - 1
+    m.cellPointsOffset = ptr(keep[1])
+    m.cellPoints = ptr(keep[2])
+    m.nInternalFaces = keep[5].shape[0]
+    m.nFaces = keep[4].shape[0]
+    m.facePoints = ptr(keep[3])
+    m.owner = ptr(keep[4])
+    m.neighbour = ptr(keep[5])
+    m.nPatches = len(mesh.patches)
+    m.patchStart = ptr(keep[6])
+    m.patchSize = ptr(keep[7])
+    m.patchLabel = ptr(keep[8])
+    m.depth = mesh.depth
+    return m, keep
+
+
+def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_rbf64=False):
+    """Mesh + initial fields -> the reference's host field bundle (native precompute)."""
+    m, keep = poly_mesh_c(mesh)
+    Wc = np.ascontiguousarray(W_cells, dtype=np.float64)
+    Wb = None if W_boundary is None else np.ascontiguousarray(W_boundary, dtype=np.float64)
+    assert Wc.shape == (mesh.n_cells, 4)
+    if Wb is not None:
+        assert Wb.shape == (mesh.n_boundary_faces, 4)
+    fp = _ffi.FieldPointer()
+    sz = _ffi.FieldSizes()
+    c = cfg.to_c()
+    r64 = C.c_void_p()
+    st = lib().afar_precompute_fields(C.byref(m), C.byref(c), ptr(Wc), ptr(Wb), C.byref(fp), C.byref(sz),
+                                      C.byref(r64) if want_rbf64 else None)
+    check(st)
+    try:
+        hf = HostFields.from_c(fp, sz)
+        if want_rbf64:
+            n = hf.a["RBFbasis"].shape[0]
+            buf = (C.c_double * n).from_address(r64.value) if n else None
+            hf.a["RBFbasis64"] = np.frombuffer(buf, dtype=np.float64).copy() if n else np.zeros(0)
+    finally:
+        lib().afar_free_host_fields(C.byref(fp))
+        if want_rbf64 and r64.value:
+            C.CDLL(None).free(r64)
+    del keep
+    return hf
+
+
+def gauss_quadrature(mesh: FoamMesh, cfg: CaseConfig):
+    """Cell and boundary-face Gauss points/weights (CSR over cells then boundary faces)."""
+    m, keep = poly_mesh_c(mesh)
+    c = cfg.to_c()
+    total = C.c_int()
+    check(lib().afar_gauss_quadrature(C.byref(m), C.byref(c), None, None, None, C.byref(total)))
+    n = mesh.n_cells + mesh.n_boundary_faces
+    off = np.zeros(n + 1, dtype=np.int32)
+    pts = np.zeros((total.value, 2))
+    w = np.zeros(total.value)
+    check(lib().afar_gauss_quadrature(C.byref(m), C.byref(c), ptr(off), ptr(pts), ptr(w), C.byref(total)))
+    del keep
+    return off, pts, w
+
+
+class CudaSolver:
+    """The reference's basicCUDAsolver on libafar (one mesh, one GPU)."""
+
+    def __init__(self, fields: HostFields, cfg: CaseConfig, policy="ref", device=0):
+        self.cfg = cfg
+        self.fields = fields
+        self.policy = policy
+        self.h = C.c_void_p()
+        check(lib().afar_solver_create(C.byref(self.h), _ffi.POLICIES[policy], device))
+        s = fields.sizes
+        self._fp = fields.to_c()
+        check(lib().afar_setDeviceFieldData(self.h, C.byref(self._fp), s["cellsNum"], s["facesNum"],
+                                            s["totalBoundaryFacesNum"]))
+        if policy == "fp64" and "RBFbasis64" in fields.a:
+            r = fields.a["RBFbasis64"]
+            check(lib().afar_set_rbf_basis64(self.h, ptr(r), r.shape[0]))
+        check(lib().afar_setDeviceFieldDataStencil(
+            self.h, C.byref(self._fp), s["cellsNum"], s["facesNum"], s["patchesNum"], s["totalBoundaryFacesNum"],
+            s["maxStencilSize"], s["maxCompactStencilSize"], s["maxLocalBlockStencilSize"],
+            s["maxCompactLocalBlockStencilSize"]))
+        check(lib().afar_set_gas(self.h, cfg.R, cfg.Cv))
+
+    # -- reference-shaped calls (basicCUDAsolver.cpp:854-913)
+    def set_delta_t(self) -> float:
+        dt = C.c_double()
+        check(lib().afar_adjustTimeStep(self.h, self.fields.nf, self.cfg.R, self.cfg.Cv, self.cfg.CFL, C.byref(dt)))
+        return dt.value
+
+    def evolve(self, dt: float):
+        s = self.fields.sizes
+        check(lib().afar_GPUevolve(self.h, self.cfg.R, self.cfg.Cv, dt, s["cellsNum"], s["facesNum"],
+                                   s["totalBoundaryFacesNum"], s["maxStencilSize"], s["maxCompactStencilSize"],
+                                   s["maxLocalBlockStencilSize"], s["maxCompactLocalBlockStencilSize"]))
+
+    def write_field(self):
+        """FD (cells + ghosts) and the shock indicator, as copyFieldDataDeviceToHost."""
+        out = self.fields.empty_like_outputs(["FD", "shockIndicator"])
+        fp = _ffi.FieldPointer()
+        fp.FD = ptr(out["FD"])
+        fp.shockIndicator = ptr(out["shockIndicator"])
+        check(lib().afar_copyFieldDataDeviceToHost(C.byref(fp), self.h, self.fields.nc, self.fields.nb))
+        return out["FD"], out["shockIndicator"]
+
+    # -- native extensions
+    def run(self, n_steps: int, dt: float = 0.0, cfl: float | None = None, t_end: float = 0.0, wait=True):
+        cfl = self.cfg.CFL if cfl is None else cfl
+        f = lib().afar_run if wait else lib().afar_run_async
+        check(f(self.h, n_steps, dt, cfl, t_end))
+
+    def synchronize(self):
+        check(lib().afar_synchronize(self.h))
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        check(lib().afar_get_stream(self.h, C.byref(p)))
+        return p.value or 0
+
+    def time(self):
+        t, dt, n = C.c_double(), C.c_double(), C.c_longlong()
+        check(lib().afar_get_time(self.h, C.byref(t), C.byref(dt), C.byref(n)))
+        return t.value, dt.value, n.value
+
+    def set_time(self, t: float):
+        check(lib().afar_set_time(self.h, t))
+
+    def state(self):
+        out = self.fields.empty_like_outputs(["FD", "cFD", "shockIndicator"])
+        check(lib().afar_download_state(self.h, ptr(out["FD"]), ptr(out["cFD"]), ptr(out["shockIndicator"])))
+        return out
+
+    def upload_state(self, FD=None, cFD=None, cFDold=None):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (FD, cFD, cFDold)]
+        check(lib().afar_upload_state(self.h, *[ptr(a) for a in arrs]))
+
+    def stage_debug(self, stage: int, dt: float):
+        names = ["faceFD", "gradFD", "limiter", "shockIndicator", "Flux", "Res", "FD", "cFD"]
+        out = self.fields.empty_like_outputs(names)
+        fp = _ffi.FieldPointer()
+        for n in names:
+            setattr(fp, n, ptr(out[n]))
+        check(lib().afar_stage_debug(self.h, stage, dt, C.byref(fp)))
+        return out
+
+    def limiter64(self):
+        out = np.zeros((self.fields.nc, 4))
+        check(lib().afar_debug_limiter64(self.h, ptr(out)))
+        return out
+
+    def ls_matrix(self):
+        out = np.zeros_like(self.fields.a["matrix"])
+        check(lib().afar_download_ls_matrix(self.h, ptr(out)))
+        return out
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        check(lib().afar_device_bytes(self.h, C.byref(b)))
+        return b.value
+
+    def close(self):
+        if self.h:
+            lib().afar_freeFieldData(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,287 @@
+/*
+ * afar.h - C ABI of the GB300-native AFAR per-stage residual + SSP-RK3 solver.
+ *
+ * Three groups of entry points:
+ *
+ *  1. The reference data layout (the structs of the reference's
+ *     src/CUDA/cudaEuler2DmixO3RK3/basicDataStructure.h:10-160), kept byte-for-byte so that a
+ *     caller that fills the reference's host `fieldPointer` can pass the same arrays here.
+ *
+ *  2. The host precompute that the reference's solver object performs with OpenFOAM
+ *     (basicCUDAsolver.cpp:122-851 and src/gaussQuadrature/d2GaussQuadrature.C:3-547):
+ *     OpenFOAM-style polyMesh arrays in, the reference's host field bundle out.
+ *
+ *  3. The drop-in replacement of the reference's host<->device boundary
+ *     (src/CUDA/cudaEuler2DmixO3RK3/GPUevolve.h:6-59): same arguments and meaning, but an
+ *     opaque solver handle in place of the device-side fieldPointer and a status code in place
+ *     of printf + std::exit.  Plus native extensions: precision policy, device-resident
+ *     CFL time step, CUDA-graph stepping, per-stage parity hooks.
+ *
+ * Every entry point returns an afar_status; afar_last_error() returns the message of the last
+ * failure on the calling thread.  Calls on one solver handle must come from one host thread.
+ */
+#ifndef AFAR_H
+#define AFAR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------------------------- */
+/* status codes                                                                                 */
+/* ------------------------------------------------------------------------------------------- */
+typedef enum {
+  AFAR_OK = 0,
+  AFAR_ERR_ARGUMENT = 1,     /* a null pointer, a size out of range, an unknown option       */
+  AFAR_ERR_MESH = 2,         /* malformed mesh: bad orientation, non-2-D cell, bad patch     */
+  AFAR_ERR_LIMIT = 3,        /* a compile-time limit of the reference layout is exceeded     */
+  AFAR_ERR_CUDA = 4,         /* a CUDA runtime call failed                                    */
+  AFAR_ERR_STATE = 5,        /* call out of order (e.g. evolve before the stencil upload)    */
+  AFAR_ERR_NOT_FINITE = 6    /* a non-finite or non-positive state was detected              */
+} afar_status;
+
+const char* afar_last_error(void);
+
+/* ------------------------------------------------------------------------------------------- */
+/* 1. reference data layout: basicDataStructure.h:6-160                                         */
+/* ------------------------------------------------------------------------------------------- */
+#define AFAR_BLOCKDIM 128                 /* basicDataStructure.h:6 */
+#define AFAR_MAX_SHARED_MEMORY_SIZE 49152 /* basicDataStructure.h:7 */
+#define AFAR_MAX_VALID_STENCIL_SIZE 20    /* basicDataStructure.h:8 */
+
+typedef struct { double x, y; } afar_meshCellData;                          /* :10-14  */
+typedef struct { double x, y, magSf, Sfx, Sfy; } afar_meshFaceData;         /* :16-23  */
+typedef struct { double p, Ux, Uy, T; } afar_basicFieldData;                /* :25-31  */
+typedef struct { double rho, rhoUx, rhoUy, rhoE; } afar_conservedFieldData; /* :33-39  */
+typedef struct {                                                            /* :41-49  */
+  double gradPx, gradPy;
+  double gradUxx, gradUxy;
+  double gradUyx, gradUyy;
+  double gradTx, gradTy;
+} afar_gradientFieldData;
+typedef struct { double rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux; } afar_basicFluxData; /* :51-57 */
+typedef struct { double Rrho, RrhoUx, RrhoUy, RrhoE; } afar_residualFieldData;         /* :59-65 */
+typedef struct { float pLimiter, UxLimiter, UyLimiter, TLimiter; } afar_limiterFieldData; /* :67-73 */
+
+/* The reference's fieldPointer (basicDataStructure.h:75-160), host side.  Sizes:
+ *   CELL, FD: cellsNum + totalBoundaryFacesNum     FACE, Flux: facesNum + totalBoundaryFacesNum
+ *   cellVolume, cFD, cFDold, gradFD, Res, limiter, stencilSize, compactStencilSize: cellsNum
+ *   shockIndicator: 2*(cellsNum + totalBoundaryFacesNum)   neighbour, faceFD: 2*facesNum
+ *   boundaryFaceNeiLabel, boundaryFacesType: totalBoundaryFacesNum   boundaryFacesNum: patchesNum
+ *   RBFbasis: 2*(maxStencilSize+1)*facesNum    localStencil: maxStencilSize*cellsNum
+ *   matrix: 2*maxCompactStencilSize*cellsNum   cellFaces: maxCompactStencilSize*cellsNum
+ *   extendStencilSize, compactExtendStencilSize: nBlocks = ceil(cellsNum/128)
+ *   extendStencil: (maxLocalBlockStencilSize - 128)*nBlocks    minDeltaT: ceil(facesNum/1024) */
+typedef struct {
+  afar_meshCellData* CELL;
+  afar_meshFaceData* FACE;
+  double* cellVolume;
+  afar_basicFieldData* FD;
+  afar_limiterFieldData* limiter;
+  int8_t* shockIndicator;
+  afar_conservedFieldData* cFD;
+  afar_conservedFieldData* cFDold;
+  afar_gradientFieldData* gradFD;
+  afar_basicFluxData* Flux;
+  afar_residualFieldData* Res;
+  int* neighbour;
+  int* boundaryFacesNum;
+  int* boundaryFaceNeiLabel;
+  uint8_t* boundaryFacesType;
+  uint8_t* stencilSize;
+  uint8_t* compactStencilSize;
+  float* RBFbasis;
+  afar_basicFieldData* faceFD;
+  int* extendStencil;
+  uint16_t* extendStencilSize;
+  uint16_t* compactExtendStencilSize;
+  uint16_t* localStencil;
+  float* matrix;
+  int* cellFaces;
+  double* minDeltaT;
+} afar_fieldPointer;
+
+/* The integer sizes that travel beside the fieldPointer in the reference
+ * (basicCUDAsolver.h members cellsNum_ ... maxCompactLocalBlockStencilSize_). */
+typedef struct {
+  int cellsNum;
+  int facesNum;
+  int patchesNum;
+  int totalBoundaryFacesNum;
+  int maxStencilSize;
+  int maxCompactStencilSize;
+  int maxLocalBlockStencilSize;
+  int maxCompactLocalBlockStencilSize;
+} afar_fieldSizes;
+
+/* ------------------------------------------------------------------------------------------- */
+/* 2. host precompute (replaces basicCUDAsolver::initFieldInfo + initStencilData, which need    */
+/*    OpenFOAM: basicCUDAsolver.cpp:122-851; d2GaussQuadrature.C:3-547)                          */
+/* ------------------------------------------------------------------------------------------- */
+
+/* OpenFOAM-style 2-D polyMesh: the x-y cross-section of a one-cell-deep mesh.  Face f joins
+ * facePoints[2f] -> facePoints[2f+1]; its normal (Sf) points out of owner[f].  Internal faces
+ * come first (owner < neighbour), then the boundary faces patch by patch. */
+typedef struct {
+  int nPoints;
+  const double* points;           /* [2*nPoints] x, y */
+  int nCells;
+  const int* cellPointsOffset;    /* [nCells+1] CSR offsets */
+  const int* cellPoints;          /* polygon vertices of each cell (3 or 4 per cell) */
+  int nInternalFaces;
+  int nFaces;                     /* internal + boundary */
+  const int* facePoints;          /* [2*nFaces] */
+  const int* owner;               /* [nFaces] */
+  const int* neighbour;           /* [nInternalFaces] */
+  int nPatches;
+  const int* patchStart;          /* [nPatches] first face of each patch */
+  const int* patchSize;           /* [nPatches] */
+  const int* patchLabel;          /* [nPatches] cudaEulerBCs label (cudaEulerBCs.h:56-61) */
+  double depth;                   /* extrusion depth (cell volume = area*depth) */
+} afar_polyMesh;
+
+#define AFAR_STENCIL_FACE_NEIGHBOUR 0  /* basicCUDAsolver.cpp:333-355 */
+#define AFAR_STENCIL_EDGE_NEIGHBOUR 1  /* basicCUDAsolver.cpp:356-375 */
+
+/* The case settings the reference reads from fvSchemes/controlDict
+ * (basicCUDAsolver.cpp:55-68; d2GaussQuadrature.C:12-13). */
+typedef struct {
+  double R;            /* CUDA.R */
+  double Cv;           /* CUDA.Cv */
+  double CFL;          /* controlDict maxCo */
+  double shapeFactor;  /* top-level shapeFactor, default 10 */
+  int stencilType;     /* AFAR_STENCIL_* */
+  int cOrder;          /* gaussQuadrature.cOrder, default 5 */
+  int fOrder;          /* gaussQuadrature.fOrder, default 4 */
+  int nThreads;        /* host threads for the precompute; <=0: all */
+} afar_caseConfig;
+
+void afar_default_case_config(afar_caseConfig* cfg);
+
+/* Builds the reference's host field bundle.  W_cells: [4*nCells] (p,Ux,Uy,T) initial cell values;
+ * W_boundary: [4*nBoundaryFaces] initial patch values (the reference takes OpenFOAM's patch values,
+ * basicCUDAsolver.cpp:189-192,231-234), or NULL to copy the owner cell's values.
+ * Arrays in *host are allocated by the library; release them with afar_free_host_fields.
+ * RBFbasis64 (optional, may be NULL): receives a malloc'd double copy of the O3 weights before
+ * their rounding to float (2*(maxStencilSize+1)*facesNum), for the FP64 policy; free() it. */
+afar_status afar_precompute_fields(const afar_polyMesh* mesh, const afar_caseConfig* cfg,
+                                   const double* W_cells, const double* W_boundary,
+                                   afar_fieldPointer* host, afar_fieldSizes* sizes,
+                                   double** RBFbasis64);
+void afar_free_host_fields(afar_fieldPointer* host);
+
+/* Cell and boundary-face Gauss points/weights (d2GaussQuadrature layout) as CSR lists over
+ * nCells + nBoundaryFaces members; boundary-face weights are divided by |Sf| like
+ * basicCUDAsolver.cpp:444-457.  offsets: [nCells+nBoundaryFaces+1]; pts: [2*total]; w: [total].
+ * Call with pts == NULL to get the total in *total. */
+afar_status afar_gauss_quadrature(const afar_polyMesh* mesh, const afar_caseConfig* cfg,
+                                  int* offsets, double* pts, double* w, int* total);
+
+/* ------------------------------------------------------------------------------------------- */
+/* 3. host<->device boundary: GPUevolve.h:6-59                                                  */
+/* ------------------------------------------------------------------------------------------- */
+typedef struct afar_solver afar_solver;
+
+#define AFAR_POLICY_REF 0    /* the reference's own casts: float stencils/weights/limiters/dissipation */
+#define AFAR_POLICY_FP64 1   /* FP64 end to end                                                       */
+#define AFAR_POLICY_MIXED 2  /* FP32 reconstruction + flux, FP64 conserved accumulation and update    */
+
+/* Creates an empty solver on a CUDA device with a precision policy. */
+afar_status afar_solver_create(afar_solver** solver, int policy, int device);
+
+/* Replaces setDeviceFieldData(devicePtr, hostPtr, cellsNum, facesNum, totalBoundaryFacesNum)
+ * (GPUevolve.h:8-14, GPUevolve.cu:13-64): uploads CELL, FACE, cellVolume, FD, cFD (cFDold = cFD)
+ * and zeroes the shock indicator. */
+afar_status afar_setDeviceFieldData(afar_solver* solver, const afar_fieldPointer* host,
+                                    int cellsNum, int facesNum, int totalBoundaryFacesNum);
+
+/* Replaces the 10-argument setDeviceFieldData (GPUevolve.h:16-27, GPUevolve.cu:67-148):
+ * uploads the stencil/operator arrays and builds the least-squares matrix on the device. */
+afar_status afar_setDeviceFieldDataStencil(afar_solver* solver, const afar_fieldPointer* host,
+                                           int cellsNum, int facesNum, int patchesNum,
+                                           int totalBoundaryFacesNum, int maxStencilSize,
+                                           int maxCompactStencilSize, int maxLocalBlockStencilSize,
+                                           int maxCompactLocalBlockStencilSize);
+
+/* Replaces adjustTimeStep (GPUevolve.h:31-38, GPUevolve.cu:177-204): CFL time step from the
+ * current state, min over internal faces (and 1e5). */
+afar_status afar_adjustTimeStep(afar_solver* solver, int facesNum, double R, double Cv, double CFL,
+                                double* deltaT);
+
+/* Replaces GPUevolve (GPUevolve.h:40-53, GPUevolve.cu:207-306): one SSP-RK3 step of deltaT. */
+afar_status afar_GPUevolve(afar_solver* solver, double R, double Cv, double deltaT, int cellsNum,
+                           int facesNum, int totalBoundaryFacesNum, int maxStencilSize,
+                           int maxCompactStencilSize, int maxLocalBlockStencilSize,
+                           int maxCompactLocalBlockStencilSize);
+
+/* Replaces copyFieldDataDeviceToHost (GPUevolve.h:56-61, GPUevolve.cu:309-318): FD and the
+ * shock indicator (2 entries per cell/ghost) to host->FD and host->shockIndicator. */
+afar_status afar_copyFieldDataDeviceToHost(afar_fieldPointer* host, afar_solver* solver,
+                                           int cellsNum, int totalBoundaryFacesNum);
+
+/* Replaces freeFieldData (GPUevolve.h:29, GPUevolve.cu:151-174); frees every device array and
+ * the handle. */
+afar_status afar_freeFieldData(afar_solver* solver);
+
+/* ---- native extensions ---------------------------------------------------------------------- */
+
+/* Gas constants (fvSchemes CUDA.R, CUDA.Cv) for afar_run/afar_stage_debug; afar_GPUevolve sets
+ * them from its own arguments like the reference. */
+afar_status afar_set_gas(afar_solver* solver, double R, double Cv);
+
+/* The FP64 policy reads the O3 weights in double when they are given here (same layout as
+ * RBFbasis, from afar_precompute_fields' RBFbasis64) before afar_setDeviceFieldDataStencil;
+ * otherwise it widens the float weights. */
+afar_status afar_set_rbf_basis64(afar_solver* solver, const double* RBFbasis64, size_t count);
+
+/* Runs nSteps SSP-RK3 steps as one replay of a captured CUDA graph per step.  deltaT > 0: fixed
+ * step; deltaT <= 0: CFL step computed on the device each step from (R, Cv, CFL) (the
+ * adjustTimeStep + GPUevolve pair of the reference's time loop, cudaEuler2DmixO3RK3solver.cpp:53-64,
+ * with no host round trip).  tEnd > 0 clips the last step to land on tEnd; steps after that are
+ * no-ops.  Waits for the steps to finish and reports device errors. */
+afar_status afar_run(afar_solver* solver, int nSteps, double deltaT, double CFL, double tEnd);
+
+/* Same as afar_run but only enqueues the steps on the solver's stream (no wait). */
+afar_status afar_run_async(afar_solver* solver, int nSteps, double deltaT, double CFL, double tEnd);
+afar_status afar_synchronize(afar_solver* solver);
+
+/* The solver's CUDA stream (a cudaStream_t), for event timing by the caller. */
+afar_status afar_get_stream(afar_solver* solver, void** stream);
+
+/* Simulated time, last step size and number of steps taken on the device. */
+afar_status afar_get_time(afar_solver* solver, double* t, double* lastDeltaT, long long* steps);
+afar_status afar_set_time(afar_solver* solver, double t);
+
+/* Runs RK stage k (0..2) of step size deltaT and copies every intermediate of that stage, in the
+ * reference layout, into the non-NULL members of *out: faceFD, gradFD, limiter (after the BVD
+ * transform), shockIndicator, Flux, Res (before the update zeroes it), FD, cFD.  The parity hook
+ * for per-stage comparison with the reference kernels. */
+afar_status afar_stage_debug(afar_solver* solver, int stage, double deltaT, afar_fieldPointer* out);
+
+/* The current limiter (4 per cell) widened to double: the FP64 policy keeps double limiters. */
+afar_status afar_debug_limiter64(afar_solver* solver, double* limiter);
+
+/* Overwrites the state: FD (cells + ghosts), cFD and cFDold (cells); NULL members are skipped. */
+afar_status afar_upload_state(afar_solver* solver, const afar_basicFieldData* FD,
+                              const afar_conservedFieldData* cFD,
+                              const afar_conservedFieldData* cFDold);
+afar_status afar_download_state(afar_solver* solver, afar_basicFieldData* FD,
+                                afar_conservedFieldData* cFD, int8_t* shockIndicator);
+
+/* The least-squares gradient matrix the device built (2*maxCompactStencilSize*cellsNum floats
+ * in the reference layout; the FP64 policy keeps doubles internally and returns them rounded). */
+afar_status afar_download_ls_matrix(afar_solver* solver, float* matrix);
+
+/* Device memory held by the solver, in bytes. */
+afar_status afar_device_bytes(afar_solver* solver, size_t* bytes);
+
+/* Number of kernel launches one afar_run step issues on this solver (for accounting). */
+int afar_launches_per_step(afar_solver* solver);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFAR_H */
