@@ -51,6 +51,7 @@ struct StageArgs {
   const V2<double>* bn;       // Nb unit normal of each boundary face
   const uint8_t* btype;       // Nb cudaEulerBCs label
   const double* vol;          // Nc
+  const double* vinv;         // Nc 1/V (policies without the reference's divisions)
   const uint8_t* nS;          // Nc stencil size
   const uint8_t* nM;          // Nc faces per cell (compact stencil size)
   const int* sten;            // [maxS][ldc]
@@ -70,7 +71,7 @@ struct StageArgs {
   V4<typename P::F>* flux;    // Nf+Nb
   StepCtl* ctl;
   V4<double>* res_dbg;        // optional residual dump (parity hook)
-  double R, Cv;
+  double R, Cv, invR, gamma;
 };
 
 // limiterProcess (reference cudaLimiter.h:35-50)
@@ -87,12 +88,202 @@ __device__ __forceinline__ void limiter_process(S& limiter, S& phif, const S phi
   limiter = fmn(limiter, yy);
 }
 
+// Faces per cell: triangles and quadrilaterals, the only cells the reference's quadrature accepts
+// (d2GaussQuadrature.C:65-148); the stencil upload rejects larger compact stencils.
+constexpr int kMaxFaces = 4;
+
 // reconstruct (reference cudaLimiter.h:53-316): LS gradient, stencil min/max, raw limiter,
 // O3 RBF face values of this cell's side of each internal face, troubled-cell flag.
+// One pass over the stencil: each member's state is gathered once and feeds the gradient and
+// min/max (compact members) and the O3 sums of every face side at once, all in registers.  The
+// loads of a batch of members (indices, gathers, weights) are issued together, so several are in
+// flight per thread; no shared memory, so occupancy is set by registers alone.  Every sum is
+// still accumulated in stencil order, as in the reference.
 template <class P>
 __global__ void __launch_bounds__(128) k_reconstruct(StageArgs<P> a) {
   using S = typename P::S;
   using G = typename P::G;
+  using WT = typename P::W;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int ldc = a.ldc;
+  const int nS = a.nS[c], nM = a.nM[c];
+  const int wrow = a.maxS + 1;
+  int fid[kMaxFaces];
+  bool inner[kMaxFaces];
+  V2<S> lm[kMaxFaces];
+#pragma unroll
+  for (int fi = 0; fi < kMaxFaces; ++fi) {
+    fid[fi] = fi < nM ? a.cf[fi * ldc + c] : 1;
+    inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
+    lm[fi] = fi < nM ? a.lsm[fi * ldc + c] : V2<S>{S(0), S(0)};
+  }
+  const V4<WT> wc = a.W[c];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  G acc[kMaxFaces][4];
+#pragma unroll
+  for (int fi = 0; fi < kMaxFaces; ++fi) {  // each face side's O3 sum starts with the cell's own term
+    const S w0 = inner[fi] ? a.wts[(size_t)(fi * wrow) * ldc + c] : S(0);
+    acc[fi][0] = w0 * pc;
+    acc[fi][1] = w0 * uxc;
+    acc[fi][2] = w0 * uyc;
+    acc[fi][3] = w0 * tc;
+  }
+  G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
+  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
+  S pn[kMaxFaces];  // pressure of the cell across each face
+  {  // members 0..3: the face neighbours (compact stencil) come first
+    int j[kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) j[u] = u < nS ? a.sten[u * ldc + c] : c;
+    V4<WT> wj[kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) wj[u] = a.W[j[u]];
+    S wv[kMaxFaces][kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u)
+#pragma unroll
+      for (int fi = 0; fi < kMaxFaces; ++fi)
+        wv[u][fi] = (u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + u + 1) * ldc + c] : S(0);
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) {
+      if (u < nS) {
+        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        if (u < nM) {  // reference :148-169 and :190-205
+          const S M1 = lm[u].x, M2 = lm[u].y;
+          S dphi = vx - pc;
+          gPx += M1 * dphi;
+          gPy += M2 * dphi;
+          dphi = vy - uxc;
+          gUxx += M1 * dphi;
+          gUyx += M2 * dphi;
+          dphi = vz - uyc;
+          gUxy += M1 * dphi;
+          gUyy += M2 * dphi;
+          dphi = vw - tc;
+          gTx += M1 * dphi;
+          gTy += M2 * dphi;
+          pMax = fmx(vx, pMax);
+          pMin = fmn(vx, pMin);
+          uxMax = fmx(vy, uxMax);
+          uxMin = fmn(vy, uxMin);
+          uyMax = fmx(vz, uyMax);
+          uyMin = fmn(vz, uyMin);
+          tMax = fmx(vw, tMax);
+          tMin = fmn(vw, tMin);
+          pn[u] = vx;
+        }
+#pragma unroll
+        for (int fi = 0; fi < kMaxFaces; ++fi) {
+          acc[fi][0] += wv[u][fi] * vx;
+          acc[fi][1] += wv[u][fi] * vy;
+          acc[fi][2] += wv[u][fi] * vz;
+          acc[fi][3] += wv[u][fi] * vw;
+        }
+      }
+    }
+  }
+  constexpr int U = sizeof(WT) == 4 ? 4 : 2;
+  for (int ci0 = kMaxFaces; ci0 < nS; ci0 += U) {  // the rest of the stencil: O3 sums only
+    int j[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) j[u] = (ci0 + u < nS) ? a.sten[(ci0 + u) * ldc + c] : c;
+    V4<WT> wj[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) wj[u] = a.W[j[u]];
+    S wv[U][kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int fi = 0; fi < kMaxFaces; ++fi)
+        wv[u][fi] = (ci0 + u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + ci0 + u + 1) * ldc + c] : S(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (ci0 + u < nS) {
+        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+#pragma unroll
+        for (int fi = 0; fi < kMaxFaces; ++fi) {
+          acc[fi][0] += wv[u][fi] * vx;
+          acc[fi][1] += wv[u][fi] * vy;
+          acc[fi][2] += wv[u][fi] * vz;
+          acc[fi][3] += wv[u][fi] * vw;
+        }
+      }
+    }
+  }
+  a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
+  a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
+
+  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
+  V4<S> L;
+  int8_t flag0;
+  if (fab(tMax - tMin) < VSMALL) {  // reference :208-233
+    L = V4<S>{S(1), S(1), S(1), S(1)};
+#pragma unroll
+    for (int fi = 0; fi < kMaxFaces; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      V4<G> o;
+      o.x = (G)(pc) + gPx * dx + gPy * dy;
+      o.y = (G)(uxc) + gUxx * dx + gUyx * dy;
+      o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
+      o.w = (G)(tc) + gTx * dx + gTy * dy;
+      a.fv[2 * f + isNei] = o;
+    }
+    flag0 = 0;
+  } else {  // reference :235-314
+    S lp = S(2), lux = S(2), luy = S(2), lt = S(2);
+    S smooth = S(0);
+    bool notTrouble = true;
+#pragma unroll
+    for (int fi = 0; fi < kMaxFaces; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      const V2<S> rf = a.sr[fi * ldc + c];
+      const S deltaR = rf.x, fraction = rf.y;
+      const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
+      S phif;
+      V4<G> o;
+      limiter_process(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
+      o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
+      notTrouble = phif > S(0);
+      smooth = fmx(smooth, fab((S(1) - fraction) * pc + fraction * pn[fi] - phif) / deltaR +
+                               (pf <= S(0)) * AFAR_LIT(S, 1e20) + (phif <= S(0)) * AFAR_LIT(S, 1e20));
+      limiter_process(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
+      o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
+      limiter_process(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
+      o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
+      limiter_process(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
+      o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
+      notTrouble = phif > S(0);
+      a.fv[2 * f + isNei] = o;
+    }
+    L.x = fmx(lp, S(0)) * notTrouble;
+    L.y = fmx(lux, S(0)) * notTrouble;
+    L.z = fmx(luy, S(0)) * notTrouble;
+    L.w = fmx(lt, S(0)) * notTrouble;
+    smooth = smooth / (S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
+    flag0 = (smooth > S(1));
+  }
+  a.lim[c] = L;
+  a.si[2 * c] = flag0;
+}
+
+// reconstruct for the FP64-heavy policies (ref, fp64): the stencil values are staged in shared
+// memory in batches (indices, then gathers), then each face side's O3 sum runs over the staged
+// values with its weights loaded eight at a time.  These policies are bound by the FP64 pipe, so
+// the kernel keeps the per-face loop (no work on missing face slots) and a small register set.
+template <class P>
+__global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
+  using S = typename P::S;
+  using G = typename P::G;
+  using WT = typename P::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V4<S>* sv = reinterpret_cast<V4<S>*>(smem_raw);  // [maxS][blockDim] staged stencil values
   const int t = threadIdx.x, B = blockDim.x;
@@ -100,11 +291,19 @@ __global__ void __launch_bounds__(128) k_reconstruct(StageArgs<P> a) {
   if (c >= a.Nc) return;
   const int ldc = a.ldc;
   const int nS = a.nS[c], nM = a.nM[c];
-  const V4<typename P::W> wc = a.W[c];
+  const V4<WT> wc = a.W[c];
   const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
-  for (int i = 0; i < nS; ++i) {
-    const V4<typename P::W> wj = a.W[a.sten[i * ldc + c]];
-    sv[i * B + t] = V4<S>{(S)wj.x, (S)wj.y, (S)wj.z, (S)wj.w};
+  constexpr int GB = 4;
+  for (int i0 = 0; i0 < nS; i0 += GB) {
+    int j[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) j[u] = (i0 + u < nS) ? a.sten[(i0 + u) * ldc + c] : c;
+    V4<WT> wj[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) wj[u] = a.W[j[u]];
+#pragma unroll
+    for (int u = 0; u < GB; ++u)
+      if (i0 + u < nS) sv[(i0 + u) * B + t] = V4<S>{(S)wj[u].x, (S)wj[u].y, (S)wj[u].z, (S)wj[u].w};
   }
 
   G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
@@ -180,13 +379,20 @@ __global__ void __launch_bounds__(128) k_reconstruct(StageArgs<P> a) {
       G uxf = wk * uxc;
       G uyf = wk * uyc;
       G tf = wk * tc;
-      for (int ci = 0; ci < nS; ++ci) {
-        wk = w[(size_t)(ci + 1) * ldc];
-        const V4<S> v = sv[ci * B + t];
-        pf += wk * v.x;
-        uxf += wk * v.y;
-        uyf += wk * v.z;
-        tf += wk * v.w;
+      for (int ci0 = 0; ci0 < nS; ci0 += 8) {  // weights in batches of eight; sums in stencil order
+        S wb[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) wb[u] = (ci0 + u < nS) ? w[(size_t)(ci0 + u + 1) * ldc] : S(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          if (ci0 + u < nS) {
+            const V4<S> v = sv[(ci0 + u) * B + t];
+            pf += wb[u] * v.x;
+            uxf += wb[u] * v.y;
+            uyf += wb[u] * v.z;
+            tf += wb[u] * v.w;
+          }
+        }
       }
       const S pnb = sv[fi * B + t].x;
       S phif;
@@ -238,11 +444,25 @@ __global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
   const int nS = a.nS[c], nM = a.nM[c];
   int8_t shockType = a.si[2 * c];
   int8_t shockTypeExt = shockType;
-  for (int ci = 0; ci < nM; ++ci) {
-    shockType += a.si[2 * a.sten[ci * ldc + c]];
-    shockTypeExt = shockType;
+  // troubled-cell flags of the stencil, eight index loads then eight flag loads at a time
+  for (int i0 = 0; i0 < nS; i0 += 8) {
+    int j[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) j[u] = (i0 + u < nS) ? a.sten[(i0 + u) * ldc + c] : c;
+    int8_t fl[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) fl[u] = a.si[2 * j[u]];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int ci = i0 + u;
+      if (ci < nM) {
+        shockType += fl[u];
+        shockTypeExt = shockType;
+      } else if (ci < nS) {
+        shockTypeExt += fl[u];
+      }
+    }
   }
-  for (int ci = nM; ci < nS; ++ci) shockTypeExt += a.si[2 * a.sten[ci * ldc + c]];
 
   const S tc = (S)a.W[c].w;
   const V4<G> g1 = a.grad[2 * c + 1];
@@ -647,6 +867,78 @@ __device__ __forceinline__ V4<double> boundary_value(const int type, const V4<do
   }
 }
 
+// Error-free float addition (Knuth two-sum): s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float& s, float& e, const float a, const float b) {
+  s = a + b;
+  const float bp = s - a;
+  e = (a - (s - bp)) + (b - bp);
+}
+
+// The mixed policy's gather + update.  FP64 is kept where accumulation needs it and nowhere else:
+// the residual of the float fluxes is summed error-free as a float pair, the RK combine of the
+// conserved state is FP64, and the pressure is the FP64 difference rhoE - |rhoU|^2/(2 rho) with
+// 1/rho from a float reciprocal refined by one FP64 Newton step (relative error ~1e-14) instead of
+// an FP64 division (a long sequence on GB300's FP64 pipe).
+template <class P>
+__device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c, const double deltaT,
+                                             const double beta1, const double beta2, const double beta3,
+                                             const int last_stage) {
+  const int ldc = a.ldc;
+  const int nM = a.nM[c];
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  constexpr int MB = 4;
+  for (int f0 = 0; f0 < nM; f0 += MB) {
+    int fid[MB];
+#pragma unroll
+    for (int u = 0; u < MB; ++u) fid[u] = (f0 + u < nM) ? a.cf[(f0 + u) * ldc + c] : 1;
+    V4<float> fl[MB];
+#pragma unroll
+    for (int u = 0; u < MB; ++u) fl[u] = reinterpret_cast<const V4<float>*>(a.flux)[abs(fid[u]) - 1];
+#pragma unroll
+    for (int u = 0; u < MB; ++u) {
+      if (f0 + u < nM) {
+        const float sgn = fid[u] > 0 ? 1.f : -1.f;
+        const float x[4] = {sgn * fl[u].x, sgn * fl[u].y, sgn * fl[u].z, sgn * fl[u].w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          float s, e;
+          two_sum(s, e, hi[k], x[k]);
+          hi[k] = s;
+          lo[k] += e;
+        }
+      }
+    }
+  }
+  if (a.res_dbg) a.res_dbg[c] = V4<double>{(double)hi[0] + lo[0], (double)hi[1] + lo[1], (double)hi[2] + lo[2],
+                                          (double)hi[3] + lo[3]};
+  const float s3 = (float)(-beta3 * deltaT * a.vinv[c]);
+  const V4<double> o = a.U0[c];
+  const V4<double> u = a.U[c];
+  const double rho = fma(beta2, u.x, beta1 * o.x) + (double)(s3 * (hi[0] + lo[0]));
+  const double rhoUx = fma(beta2, u.y, beta1 * o.y) + (double)(s3 * (hi[1] + lo[1]));
+  const double rhoUy = fma(beta2, u.z, beta1 * o.z) + (double)(s3 * (hi[2] + lo[2]));
+  const double rhoE = fma(beta2, u.w, beta1 * o.w) + (double)(s3 * (hi[3] + lo[3]));
+  const V4<double> un{rho, rhoUx, rhoUy, rhoE};
+  a.U[c] = un;
+  if (last_stage) a.U0[c] = un;
+  const float irf = __frcp_rn((float)rho);
+  double ir = (double)irf;
+  ir = ir * fma(-rho, ir, 2.0);
+  const double gamma = a.gamma;  // R/Cv + 1, computed once on the host like GPUevolve.cu:222
+  const double p = (gamma - 1.0) * fma(-0.5 * ir, fma(rhoUx, rhoUx, rhoUy * rhoUy), rhoE);
+  const float pf = (float)p;
+  const V4<float> wn{pf, (float)rhoUx * irf, (float)rhoUy * irf, pf * irf * (float)a.invR};
+  reinterpret_cast<V4<float>*>(a.W)[c] = wn;
+  for (int fi = 0; fi < nM; ++fi) {
+    const int f = abs(a.cf[fi * ldc + c]) - 1;
+    if (f < a.Nf) continue;
+    const int b = f - a.Nf;
+    const V4<double> g = boundary_value(a.btype[b], V4<double>{(double)wn.x, (double)wn.y, (double)wn.z, (double)wn.w},
+                                        a.bn[b]);
+    reinterpret_cast<V4<float>*>(a.W)[a.Nc + b] = V4<float>{(float)g.x, (float)g.y, (float)g.z, (float)g.w};
+  }
+}
+
 // evaluateResidual + updateFieldData + updateBoundaryFieldData (+ storeConservedFieldData on the
 // last stage), reference cudaFieldOperation.h:183-268, cudaEulerBCs.h:64-95: signed gather of the
 // face fluxes in the cell's face order (no atomics), SSP-RK3 combine, conserved -> primitive, and
@@ -660,33 +952,61 @@ __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double bet
   if (!(deltaT > 0.0)) return;  // past t_end: the step is a no-op
   const int ldc = a.ldc;
   const int nM = a.nM[c];
+  if constexpr (P::id == PolicyMixed::id) {
+    update_mixed(a, c, deltaT, beta1, beta2, beta3, last_stage);
+    return;
+  }
   double Rrho = 0.0, RrhoUx = 0.0, RrhoUy = 0.0, RrhoE = 0.0;
-  for (int fi = 0; fi < nM; ++fi) {
-    int f = a.cf[fi * ldc + c];
-    const int direction = (f > 0) - (f < 0);
-    f = abs(f) - 1;
-    const V4<typename P::F> fl = a.flux[f];
-    Rrho += direction * (double)fl.x;
-    RrhoUx += direction * (double)fl.y;
-    RrhoUy += direction * (double)fl.z;
-    RrhoE += direction * (double)fl.w;
+  constexpr int MB = 4;  // face ids, then fluxes, four loads in flight; sums keep the face order
+  for (int f0 = 0; f0 < nM; f0 += MB) {
+    int fid[MB];
+#pragma unroll
+    for (int u = 0; u < MB; ++u) fid[u] = (f0 + u < nM) ? a.cf[(f0 + u) * ldc + c] : 1;
+    V4<typename P::F> fl[MB];
+#pragma unroll
+    for (int u = 0; u < MB; ++u) fl[u] = a.flux[abs(fid[u]) - 1];
+#pragma unroll
+    for (int u = 0; u < MB; ++u) {
+      if (f0 + u < nM) {
+        const int direction = (fid[u] > 0) - (fid[u] < 0);
+        Rrho += direction * (double)fl[u].x;
+        RrhoUx += direction * (double)fl[u].y;
+        RrhoUy += direction * (double)fl[u].z;
+        RrhoE += direction * (double)fl[u].w;
+      }
+    }
   }
   if (a.res_dbg) a.res_dbg[c] = V4<double>{Rrho, RrhoUx, RrhoUy, RrhoE};
-  const double V = a.vol[c];
   const V4<double> o = a.U0[c];
   const V4<double> u = a.U[c];
-  const double rho = beta1 * o.x + beta2 * u.x + beta3 * deltaT * (-Rrho / V);
-  const double rhoUx = beta1 * o.y + beta2 * u.y + beta3 * deltaT * (-RrhoUx / V);
-  const double rhoUy = beta1 * o.z + beta2 * u.z + beta3 * deltaT * (-RrhoUy / V);
-  const double rhoE = beta1 * o.w + beta2 * u.w + beta3 * deltaT * (-RrhoE / V);
-  const V4<double> un{rho, rhoUx, rhoUy, rhoE};
+  const double R = a.R;
+  const double gamma = a.gamma;  // R/Cv + 1, computed once on the host like GPUevolve.cu:222
+  using WT = typename P::W;
+  V4<double> un;
+  V4<WT> wn;
+  if constexpr (P::exact_blend) {  // the reference's eight divisions (cudaFieldOperation.h:229-242)
+    const double V = a.vol[c];
+    const double rho = beta1 * o.x + beta2 * u.x + beta3 * deltaT * (-Rrho / V);
+    const double rhoUx = beta1 * o.y + beta2 * u.y + beta3 * deltaT * (-RrhoUx / V);
+    const double rhoUy = beta1 * o.z + beta2 * u.z + beta3 * deltaT * (-RrhoUy / V);
+    const double rhoE = beta1 * o.w + beta2 * u.w + beta3 * deltaT * (-RrhoE / V);
+    un = V4<double>{rho, rhoUx, rhoUy, rhoE};
+    const double p = (gamma - 1.0) * (rhoE - 0.5 * (rhoUx * rhoUx + rhoUy * rhoUy) / rho);
+    wn = V4<WT>{(WT)p, (WT)(rhoUx / rho), (WT)(rhoUy / rho), (WT)(p / (R * rho))};
+  } else {  // FP64 is scarce on GB300: 1/V precomputed, one division for 1/rho
+    const double s3 = -beta3 * deltaT * a.vinv[c];
+    const double rho = beta1 * o.x + beta2 * u.x + s3 * Rrho;
+    const double rhoUx = beta1 * o.y + beta2 * u.y + s3 * RrhoUx;
+    const double rhoUy = beta1 * o.z + beta2 * u.z + s3 * RrhoUy;
+    const double rhoE = beta1 * o.w + beta2 * u.w + s3 * RrhoE;
+    un = V4<double>{rho, rhoUx, rhoUy, rhoE};
+    const double ir = 1.0 / rho;
+    const double ux = rhoUx * ir, uy = rhoUy * ir;
+    const double p = (gamma - 1.0) * (rhoE - 0.5 * (rhoUx * ux + rhoUy * uy));
+    wn = V4<WT>{(WT)p, (WT)ux, (WT)uy, (WT)(p * ir * a.invR)};
+  }
   a.U[c] = un;
   if (last_stage) a.U0[c] = un;
-  const double R = a.R;
-  const double gamma = a.R / a.Cv + 1.0;
-  const double p = (gamma - 1.0) * (rhoE - 0.5 * (rhoUx * rhoUx + rhoUy * rhoUy) / rho);
-  using WT = typename P::W;
-  const V4<WT> wn{(WT)p, (WT)(rhoUx / rho), (WT)(rhoUy / rho), (WT)(p / (R * rho))};
   a.W[c] = wn;
   for (int fi = 0; fi < nM; ++fi) {
     const int f = abs(a.cf[fi * ldc + c]) - 1;

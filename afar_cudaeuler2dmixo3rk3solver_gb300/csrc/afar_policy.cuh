@@ -83,6 +83,17 @@ __device__ __forceinline__ double erfc_(double a) { return erfc(a); }
 __device__ __forceinline__ float exp_(float a) { return expf(a); }
 __device__ __forceinline__ double exp_(double a) { return exp(a); }
 
+// Asynchronous global->shared copies (cp.async, cache in L1): a thread issues all of its stencil
+// gathers and weight loads back to back and waits once, instead of one dependent load at a time.
+// Sizes 4, 8 or 16 bytes; both addresses aligned to the size.
+template <int N>
+__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
+  static_assert(N == 4 || N == 8 || N == 16, "cp.async size");
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // cond ? a : b.  The reference writes these selections as arithmetic blends
 // (c1*a + c2*b with c1, c2 in {0,1}); the ref policy keeps the blend so that signed zeros and
 // non-finite operands propagate the same way.

@@ -98,6 +98,11 @@ __global__ void k_init_ctl(StepCtl* ctl) {
   }
 }
 
+__global__ void k_reciprocal(int n, const double* in, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = 1.0 / in[i];
+}
+
 template <class A, class B>
 __global__ void k_convert4(int n, const V4<A>* in, V4<B>* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -120,6 +125,7 @@ struct afar_solver {
   V2<double>* cellC = nullptr;
   FaceRaw* faceRaw = nullptr;
   double* vol = nullptr;
+  double* vinv = nullptr;
   int2* on = nullptr;
   int* bnei = nullptr;
   uint8_t* btype = nullptr;
@@ -147,6 +153,7 @@ struct afar_solver {
   void* lim = nullptr;
   void* fv = nullptr;
   void* flux = nullptr;
+  void* snap = nullptr;       // device snapshot of W, U, U0, step control
   std::vector<double> rbf64;  // optional FP64 weights awaiting the stencil upload
   cudaGraphExec_t graph = nullptr;
   size_t bytes = 0;
@@ -203,16 +210,31 @@ StageArgs<P> make_args(afar_solver* s) {
   a.si = s->si;
   a.fv = static_cast<V4<G>*>(s->fv);
   a.flux = static_cast<V4<typename P::F>*>(s->flux);
+  a.vinv = s->vinv;
   a.ctl = s->ctl;
   a.res_dbg = nullptr;
   a.R = s->R;
   a.Cv = s->Cv;
+  a.invR = s->R > 0.0 ? 1.0 / s->R : 0.0;
+  a.gamma = s->Cv > 0.0 ? s->R / s->Cv + 1.0 : 0.0;
   return a;
 }
 
+// The mixed policy reconstructs in one register pass (k_reconstruct); the FP64-bound policies use
+// the shared-memory staged variant, which keeps their FP64 work per face slot.
 template <class P>
 size_t recon_smem(const afar_solver* s) {
+  if constexpr (P::id == PolicyMixed::id) return 0;
   return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
+}
+
+template <class P>
+void launch_reconstruct(afar_solver* s, const StageArgs<P>& a) {
+  const int gc = grid_for(s->Nc, kCellBlock);
+  if constexpr (P::id == PolicyMixed::id)
+    k_reconstruct<P><<<gc, kCellBlock, 0, s->stream>>>(a);
+  else
+    k_reconstruct_staged<P><<<gc, kCellBlock, recon_smem<P>(s), s->stream>>>(a);
 }
 
 // Enqueues one RK stage.  dt_stage: fuse the CFL reduction into the flux kernel.
@@ -243,7 +265,7 @@ void enqueue_flux(afar_solver* s, const StageArgs<P>& a, bool dt_stage) {
 template <class P>
 void enqueue_stage(afar_solver* s, const StageArgs<P>& a, int k, bool dt_stage) {
   const int gc = grid_for(s->Nc, kCellBlock);
-  k_reconstruct<P><<<gc, kCellBlock, recon_smem<P>(s), s->stream>>>(a);
+  launch_reconstruct<P>(s, a);
   k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
   enqueue_flux<P>(s, a, dt_stage);
   k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
@@ -308,8 +330,9 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaFree(fxy));
   AFAR_CUDA(cudaFree(fsr));
-  const size_t smem = recon_smem<P>(s);
-  AFAR_CUDA(cudaFuncSetAttribute(k_reconstruct<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if constexpr (P::id != PolicyMixed::id)
+    AFAR_CUDA(cudaFuncSetAttribute(k_reconstruct_staged<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)recon_smem<P>(s)));
   return AFAR_OK;
 }
 
@@ -400,6 +423,7 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   if ((st = dalloc_t(s, &s->cellC, Nc + Nb))) return st;
   if ((st = dalloc_t(s, &s->faceRaw, Nf + Nb))) return st;
   if ((st = dalloc_t(s, &s->vol, Nc))) return st;
+  if ((st = dalloc_t(s, &s->vinv, Nc))) return st;
   if ((st = dalloc_t(s, &s->U, Nc))) return st;
   if ((st = dalloc_t(s, &s->U0, Nc))) return st;
   if ((st = dalloc_t(s, &s->si, 2 * (Nc + Nb)))) return st;
@@ -409,6 +433,7 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   AFAR_CUDA(cudaMemcpyAsync(s->cellC, h->CELL, sizeof(V2<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->faceRaw, h->FACE, sizeof(FaceRaw) * (Nf + Nb), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->vol, h->cellVolume, sizeof(double) * Nc, cudaMemcpyHostToDevice, s->stream));
+  k_reciprocal<<<grid_for(Nc, 256), 256, 0, s->stream>>>((int)Nc, s->vol, s->vinv);
   AFAR_CUDA(cudaMemcpyAsync(s->U, h->cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->U0, h->cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemsetAsync(s->si, 0, 2 * (Nc + Nb), s->stream));
@@ -471,7 +496,8 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
     return AFAR_ERR_ARGUMENT;
   }
   if (maxStencilSize < 1 || maxStencilSize > AFAR_MAX_VALID_STENCIL_SIZE || maxCompactStencilSize < 1 ||
-      maxCompactStencilSize > maxStencilSize || maxLocalBlockStencilSize < AFAR_BLOCKDIM ||
+      maxCompactStencilSize > maxStencilSize || maxCompactStencilSize > kMaxFaces ||
+      maxLocalBlockStencilSize < AFAR_BLOCKDIM ||
       maxCompactLocalBlockStencilSize < AFAR_BLOCKDIM || patchesNum < 0) {
     set_error("afar_setDeviceFieldDataStencil: stencil sizes out of range (maxS %d, maxM %d, maxLB %d)",
               maxStencilSize, maxCompactStencilSize, maxLocalBlockStencilSize);
@@ -699,6 +725,76 @@ extern "C" afar_status afar_run_async(afar_solver* s, int nSteps, double deltaT,
   return run_impl(s, nSteps, deltaT, CFL, tEnd, false);
 }
 
+extern "C" afar_status afar_run_timed(afar_solver* s, int nSteps, double dt, double CFL, double tEnd, float* ms) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!ms) return (set_error("null output"), AFAR_ERR_ARGUMENT);
+  if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
+  if ((st = ensure_graph(s, s->R, s->Cv))) return st;
+  cudaEvent_t e0, e1;
+  AFAR_CUDA(cudaEventCreate(&e0));
+  AFAR_CUDA(cudaEventCreate(&e1));
+  k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, tEnd);
+  AFAR_CUDA(cudaEventRecord(e0, s->stream));
+  for (int i = 0; i < nSteps; ++i) AFAR_CUDA(cudaGraphLaunch(s->graph, s->stream));
+  AFAR_CUDA(cudaEventRecord(e1, s->stream));
+  AFAR_CUDA(cudaEventSynchronize(e1));
+  AFAR_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_profile_step(afar_solver* s, double dt, double CFL, float ms[5]) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!ms) return (set_error("null output"), AFAR_ERR_ARGUMENT);
+  if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
+  cudaEvent_t ev[32];
+  for (int i = 0; i < 32; ++i) AFAR_CUDA(cudaEventCreate(&ev[i]));
+  k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, 0.0);
+  int n = 0;
+  int kind[32];
+  auto mark = [&](int k) {
+    cudaEventRecord(ev[n], s->stream);
+    kind[n++] = k;
+  };
+  auto body = [&](auto tag) {
+    using P = decltype(tag);
+    const StageArgs<P> a = make_args<P>(s);
+    const int gc = grid_for(s->Nc, kCellBlock);
+    mark(-1);
+    for (int k = 0; k < 3; ++k) {
+      launch_reconstruct<P>(s, a);
+      mark(0);
+      k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
+      mark(1);
+      enqueue_flux<P>(s, a, k == 0);
+      mark(2);
+      k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+      mark(3);
+    }
+    k_finish_step<<<1, 32, 0, s->stream>>>(s->ctl);
+    mark(4);
+  };
+  switch (s->policy) {
+    case AFAR_POLICY_REF: body(PolicyRef{}); break;
+    case AFAR_POLICY_FP64: body(PolicyFP64{}); break;
+    default: body(PolicyMixed{}); break;
+  }
+  AFAR_CUDA(cudaEventSynchronize(ev[n - 1]));
+  for (int k = 0; k < 5; ++k) ms[k] = 0.f;
+  for (int i = 1; i < n; ++i) {
+    float t = 0.f;
+    AFAR_CUDA(cudaEventElapsedTime(&t, ev[i - 1], ev[i]));
+    ms[kind[i]] += t;
+  }
+  for (int i = 0; i < 32; ++i) cudaEventDestroy(ev[i]);
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
 extern "C" afar_status afar_synchronize(afar_solver* s) {
   if (!s) return (set_error("null solver"), AFAR_ERR_ARGUMENT);
   AFAR_CUDA(cudaSetDevice(s->device));
@@ -750,7 +846,7 @@ extern "C" afar_status afar_stage_debug(afar_solver* s, int stage, double deltaT
     using P = decltype(tag);
     StageArgs<P> a = make_args<P>(s);
     a.res_dbg = s->res_dbg;
-    k_reconstruct<P><<<gc, kCellBlock, recon_smem<P>(s), s->stream>>>(a);
+    launch_reconstruct<P>(s, a);
     k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
     enqueue_flux<P>(s, a, false);
     k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[stage], kBeta2[stage], kBeta3[stage], stage == 2);
@@ -857,6 +953,31 @@ extern "C" afar_status afar_copyFieldDataDeviceToHost(afar_fieldPointer* h, afar
     return AFAR_ERR_ARGUMENT;
   }
   return afar_download_state(s, h->FD, nullptr, h->shockIndicator);
+}
+
+extern "C" afar_status afar_state_snapshot(afar_solver* s, int op) {
+  if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  if (op != AFAR_SNAPSHOT_SAVE && op != AFAR_SNAPSHOT_RESTORE) return (set_error("unknown snapshot op %d", op), AFAR_ERR_ARGUMENT);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  const size_t wb = w_size(s->policy) * (size_t)(s->Nc + s->Nb);
+  const size_t ub = sizeof(V4<double>) * (size_t)s->Nc;
+  if (op == AFAR_SNAPSHOT_SAVE && !s->snap) {
+    afar_status st = dalloc(s, &s->snap, wb + 2 * ub + sizeof(StepCtl));
+    if (st) return st;
+  }
+  if (!s->snap) return (set_error("restore without a saved snapshot"), AFAR_ERR_STATE);
+  char* p = static_cast<char*>(s->snap);
+  void* dst[4] = {p, p + wb, p + wb + ub, p + wb + 2 * ub};
+  void* src[4] = {s->W, s->U, s->U0, s->ctl};
+  const size_t n[4] = {wb, ub, ub, sizeof(StepCtl)};
+  for (int i = 0; i < 4; ++i) {
+    if (op == AFAR_SNAPSHOT_SAVE)
+      AFAR_CUDA(cudaMemcpyAsync(dst[i], src[i], n[i], cudaMemcpyDeviceToDevice, s->stream));
+    else
+      AFAR_CUDA(cudaMemcpyAsync(src[i], dst[i], n[i], cudaMemcpyDeviceToDevice, s->stream));
+  }
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  return AFAR_OK;
 }
 
 extern "C" afar_status afar_download_ls_matrix(afar_solver* s, float* matrix) {

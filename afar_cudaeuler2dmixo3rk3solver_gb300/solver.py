@@ -239,6 +239,30 @@ class CudaSolver:
     def synchronize(self):
         check(lib().afar_synchronize(self.h))
 
+    def run_timed(self, n_steps: int, dt: float = 0.0, cfl: float | None = None, t_end: float = 0.0) -> float:
+        """Device milliseconds of n_steps graph-replayed steps (CUDA events on the solver stream)."""
+        cfl = self.cfg.CFL if cfl is None else cfl
+        ms = C.c_float()
+        check(lib().afar_run_timed(self.h, n_steps, dt, cfl, t_end, C.byref(ms)))
+        return ms.value
+
+    def profile_step(self, dt: float = 0.0, cfl: float | None = None):
+        """Device ms per kernel kind over one step: reconstruct, bvd, flux, update, bookkeeping."""
+        cfl = self.cfg.CFL if cfl is None else cfl
+        ms = (C.c_float * 5)()
+        check(lib().afar_profile_step(self.h, dt, cfl, ms))
+        return dict(zip(["reconstruct", "bvd", "flux", "update", "bookkeeping"], [float(x) for x in ms]))
+
+    def launches_per_step(self) -> int:
+        return lib().afar_launches_per_step(self.h)
+
+    def save(self):
+        """In-device checkpoint of the state (bit-exact resume with restore())."""
+        check(lib().afar_state_snapshot(self.h, 0))
+
+    def restore(self):
+        check(lib().afar_state_snapshot(self.h, 1))
+
     def stream(self) -> int:
         p = C.c_void_p()
         check(lib().afar_get_stream(self.h, C.byref(p)))

@@ -1,0 +1,418 @@
+#!/usr/bin/env python3
+"""Benchmark: cell-RK3-steps/s of the AFAR stage on the Mach 3 forward-facing-step workload.
+
+Workload (one GPU): channel [0,3]x[0,1] with the step [0.6,3]x[0,0.2] removed, Delaunay
+triangulation of ~1M seeded jittered points (jitter 0.3h), RCM-renumbered: about 2.0M triangles,
+3.0M internal faces.  Inflow rho=1.4, p=1, u=3 (label 3), slip walls (label 2), outflow (label 4),
+edge-neighbour stencils, R = 1/1.4, Cv = R/0.4, CFL 0.3, device-side CFL step every step.
+Synthetic, seeded inputs; the working set (~1.5 GB) is larger than L2, so no L2 flush is needed.
+
+Our arm (default): K timed steps per precision policy, graph-replayed, CUDA events on the solver's
+stream; `value` is the mixed policy (FP32 reconstruction/flux, FP64 accumulation); the fp64 and ref
+policies are reported beside it.  `e2e` is the same metric through the reference-shaped C ABI
+(adjustTimeStep + GPUevolve each step, state uploaded from pinned host memory before and the
+fields copied back after).  `cpu_baseline` is the CPU oracle (the reference's algorithm restated
+in C, OpenMP on all host cores) on a bounded sample.  `reference_gpu` is the reference's own CUDA
+kernels (compiled from its sources) on the same inputs.
+
+--impl reference: the reference arm.  The reference has no CPU implementation of this path, so it
+times the CPU restatement (oracle, ref policy, all host cores), a bounded number of steps per run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-RK3-steps/s"
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--points", type=int, default=1_000_000)
+    ap.add_argument("--cfl", type=float, default=0.2)
+    ap.add_argument("--chunk", type=int, default=50,
+                    help="timed steps per chunk; every chunk restarts from the same post-warm-up state")
+    ap.add_argument("--policies", default="mixed,fp64,ref")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")  # host-side barrier and max only; no data-path collective
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+
+        def reader():
+            for line in self.proc.stdout:
+                self.rows.append([x.strip() for x in line.split(",")])
+
+        self.thread = threading.Thread(target=reader, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm = []
+        smax = None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------ workload
+def make_workload(points: int, seed: int, cfl: float):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+
+    t0 = time.time()
+    m = mesh.forward_step_triangles(points, seed=seed)
+    W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
+    cfg = CaseConfig(stencilType="edgeNeighbour", CFL=cfl)
+    hf = precompute(m, cfg, W, Wb, want_rbf64=True)
+    return m, hf, cfg, time.time() - t0
+
+
+def algorithmic_bytes_per_step(hf, policy: str) -> float:
+    """Compulsory HBM bytes of one RK3 step (three stages + the CFL step), counting each compulsory
+    array once per stage and no intermediate (gradients, limiters, flags, face values, fluxes):
+      B_stage = sum_cells [8 wW + 96 + 24 + 2 m wO + 4 S + 4 m + 2]
+              + sum_internal_faces [40 + 8 + (S_own + 1 + S_nei + 1) wO]
+              + sum_boundary_faces [40 + 4 + 1 + 4 wW]
+      B_step  = 3 B_stage + Nc (4 wW + 16) + 48 Nf
+    wW = bytes per primitive word (8 ref/fp64, 4 mixed); wO = operator word (4 ref/mixed, 8 fp64)."""
+    wW = 4 if policy == "mixed" else 8
+    wO = 8 if policy == "fp64" else 4
+    S = hf.stencilSize.astype(np.float64)
+    m = hf.compactStencilSize.astype(np.float64)
+    nb = hf.neighbour.reshape(-1, 2)
+    cells = np.sum(8 * wW + 96 + 24 + 2 * m * wO + 4 * S + 4 * m + 2)
+    faces = np.sum(40 + 8 + (S[nb[:, 0]] + 1 + S[nb[:, 1]] + 1) * wO)
+    bfaces = hf.nb * (40 + 4 + 1 + 4 * wW)
+    return 3.0 * (cells + faces + bfaces) + hf.nc * (4 * wW + 16) + 48.0 * hf.nf
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------------------------------------------ arms
+def cpu_oracle_rate(hf, cfg, target_s: float = 10.0, max_steps: int = 20, policy="ref"):
+    """The oracle (the reference's algorithm restated in C) on all host cores: cell-steps/s over a
+    bounded sample of about target_s seconds (whole RK3 steps of the full mesh)."""
+    from oracle.oracle import Oracle, max_threads
+
+    o = Oracle(hf, cfg.R, cfg.Cv, policy)
+    st = o.new_state()
+    dt = o.delta_t(st["FD"], cfg.CFL)
+    tw = time.perf_counter()
+    o.evolve(st, dt)  # warm-up (first touch of the work arrays)
+    tw = time.perf_counter() - tw
+    steps = int(max(2, min(max_steps, round(target_s / max(tw, 1e-3)))))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt = o.delta_t(st["FD"], cfg.CFL)
+        o.evolve(st, dt)
+    el = time.perf_counter() - t0
+    return hf.nc * steps / el, max_threads(), el, steps
+
+
+def run_reference_arm(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+
+    b.build_all()
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl)
+    rate, cores, el, steps = cpu_oracle_rate(hf, cfg, target_s=20.0, max_steps=max(2, args.steps))
+    sample = (f"{steps} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle (ref policy), "
+              f"{el:.1f} s")
+    line = {
+        "metric": METRIC, "value": rate, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": steps,
+        "warmup": 1, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Delaunay mesh, uniform Mach 3 inflow)",
+        "impl": "reference",
+        "config": {"workload": "mach3_forward_step_tri", "cells": hf.nc, "internal_faces": hf.nf,
+                   "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
+                   "parallelism": "replicas"},
+        "cpu_baseline": {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference has no CPU implementation of the path; this is its algorithm restated in C "
+                "(oracle/afar_oracle.c), OpenMP over all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def reference_gpu_rate(hf, cfg, steps: int):
+    """The reference's own kernels (cubin compiled from its sources) on the same inputs: its time
+    loop (adjustTimeStep with the host round trip, then GPUevolve) and the kernels alone."""
+    from oracle import ref_harness
+
+    ref_harness.build()
+    if not ref_harness.available():
+        return None
+    r = ref_harness.RefKernels(hf)
+    dt = r.adjust_dt(cfg.R, cfg.Cv, cfg.CFL)
+    r.evolve(2, cfg.R, cfg.Cv, dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt = r.adjust_dt(cfg.R, cfg.Cv, cfg.CFL)
+        r.evolve(1, cfg.R, cfg.Cv, dt)
+    loop_s = time.perf_counter() - t0
+    ms = r.evolve(steps, cfg.R, cfg.Cv, dt)
+    r.close()
+    return {"value": hf.nc * steps / loop_s, "unit": "cell-steps/s", "kernels_only": hf.nc * steps / (ms * 1e-3),
+            "sample": f"{steps} steps of the same mesh", "cubin": os.path.basename(ref_harness.cubin_path()),
+            "note": "reference kernels compiled from its sources for Blackwell; time loop with adjustTimeStep"}
+
+
+def run_ours(args, dist: Dist):
+    import ctypes as C
+
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver, _ffi
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+
+    b.build_all()
+    device = dist.local
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl)
+    K, Wm = args.steps, max(3, args.warmup)
+    hbm, peak_kind = peaks()
+    policies = [p for p in args.policies.split(",") if p]
+    results = {}
+    sampler = ClockSampler(device)
+    solvers = {}
+    chunks = [min(args.chunk, K - i) for i in range(0, K, args.chunk)]
+    for pol in policies:
+        s = CudaSolver(hf, cfg, policy=pol, device=device)
+        s.run(Wm)  # warm-up steps (graph capture, first touch)
+        s.save()   # every timed chunk restarts here, so every timed step is a physical one
+        solvers[pol] = s
+    dist.barrier()
+    sampler.start()
+    for pol in policies:
+        s = solvers[pol]
+        ms = 0.0
+        finite = True
+        for n in chunks:
+            s.restore()
+            s.synchronize()
+            dist.barrier()
+            ms += dist.max(s.run_timed(n))
+            st = s.state()
+            W_ = st["FD"][:hf.nc]
+            finite &= bool(np.isfinite(st["cFD"]).all() and (W_[:, 0] > 0).all() and (W_[:, 3] > 0).all())
+        results[pol] = {"ms": ms, "finite": finite, "launches": s.launches_per_step()}
+    clocks = sampler.stop()
+    for pol in policies:
+        s = solvers[pol]
+        s.restore()
+        prof = s.profile_step()
+        results[pol]["kernels_ms"] = prof
+        results[pol]["device_bytes"] = s.device_bytes()
+
+    # e2e through the reference-shaped C ABI with host buffers (mixed policy)
+    pol0 = policies[0]
+    import torch
+
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    FD_h, cFD_h = pin(hf.FD), pin(hf.cFD)
+    out_FD = pin(np.zeros_like(hf.FD))
+    out_si = pin(np.zeros(2 * (hf.nc + hf.nb), dtype=np.int8))
+    s = solvers[pol0]
+    s.synchronize()
+    dist.barrier()
+    check = _ffi.check
+    L = _ffi.lib()
+    sz = hf.sizes
+    dtv = C.c_double()
+    fp = _ffi.FieldPointer()
+    fp.FD = out_FD.ctypes.data
+    fp.shockIndicator = out_si.ctypes.data
+    t0 = time.perf_counter()
+    for n in chunks:  # per chunk: state in from pinned host memory, n reference-shaped steps, fields out
+        check(L.afar_upload_state(s.h, FD_h.ctypes.data, cFD_h.ctypes.data, cFD_h.ctypes.data))
+        for _ in range(n):
+            check(L.afar_adjustTimeStep(s.h, hf.nf, cfg.R, cfg.Cv, cfg.CFL, C.byref(dtv)))
+            check(L.afar_GPUevolve(s.h, cfg.R, cfg.Cv, dtv.value, sz["cellsNum"], sz["facesNum"],
+                                   sz["totalBoundaryFacesNum"], sz["maxStencilSize"], sz["maxCompactStencilSize"],
+                                   sz["maxLocalBlockStencilSize"], sz["maxCompactLocalBlockStencilSize"]))
+        check(L.afar_copyFieldDataDeviceToHost(C.byref(fp), s.h, hf.nc, hf.nb))
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_finite = bool(np.isfinite(out_FD).all() and (out_FD[:hf.nc, 0] > 0).all())
+    h2d = (FD_h.nbytes + 2 * cFD_h.nbytes) * len(chunks) / K + 24
+    d2h = (out_FD.nbytes + out_si.nbytes) * len(chunks) / K + 8
+
+    cpu = None
+    refgpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        rate, cores, el, cs = cpu_oracle_rate(hf, cfg)
+        cpu = {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{cs} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle, ref policy, "
+                         f"{el:.1f} s"}
+    if dist.rank == 0 and not args.no_reference_gpu:
+        try:
+            refgpu = reference_gpu_rate(hf, cfg, min(K, 50))
+        except Exception as e:  # the harness is test infrastructure; report, do not fail the bench
+            refgpu = {"unavailable": str(e)[:200]}
+
+    for s in solvers.values():
+        s.close()
+    if dist.rank != 0:
+        return
+    n = dist.world
+    head = results[pol0]
+    ms_step = head["ms"] / K
+    value = n * hf.nc * K / (head["ms"] * 1e-3)
+    bstep = algorithmic_bytes_per_step(hf, pol0)
+    achieved = bstep / (ms_step * 1e-3) / 1e9
+    prof = head["kernels_ms"]
+    tot = sum(prof.values())
+    dom = max(prof, key=prof.get)
+    by_policy = {}
+    for pol in policies:
+        r = results[pol]
+        b_s = algorithmic_bytes_per_step(hf, pol)
+        by_policy[pol] = {
+            "value": hf.nc * K / (r["ms"] * 1e-3), "ms_per_step": r["ms"] / K, "finite": r["finite"],
+            "algorithmic_GBps": b_s / (r["ms"] / K * 1e-3) / 1e9, "bytes_per_cell_step": b_s / hf.nc,
+            "kernels_ms_per_step": r["kernels_ms"], "launches_per_step": r["launches"],
+            "device_bytes": r["device_bytes"],
+        }
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": n, "steps": K, "warmup": Wm,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if pol0 == "mixed" else "f64",
+        "data": "synthetic (seeded Delaunay mesh, uniform Mach 3 inflow)",
+        "config": {"workload": "mach3_forward_step_tri", "policy": pol0, "cells": hf.nc, "internal_faces": hf.nf,
+                   "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
+                   "max_stencil": hf.sizes["maxStencilSize"], "dt": "device CFL step every step",
+                   "l2": "working set > L2 (no flush needed)", "parallelism": "replicas" if n > 1 else "single",
+                   "timed_chunks": chunks, "chunk_start": f"state after {Wm} warm-up steps (device snapshot)",
+                   "setup_s": round(setup_s, 1)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_kind": peak_kind,
+                     "granularity": "one RK3 step (one CUDA-graph launch of all stage kernels)",
+                     "dominant_kernel": dom, "dominant_share": prof[dom] / tot if tot else None},
+        "clocks": clocks,
+        "gpu_launches": K * head["launches"] + 1,
+        "e2e": {"value": n * hf.nc * K / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "finite": e2e_finite,
+                "path": "per chunk: afar_upload_state (pinned host), n x (afar_adjustTimeStep + afar_GPUevolve), "
+                        "afar_copyFieldDataDeviceToHost"},
+        "policies": by_policy,
+        "cpu_baseline": cpu,
+        "reference_gpu": refgpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference_arm(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -251,6 +251,16 @@ afar_status afar_synchronize(afar_solver* solver);
 /* The solver's CUDA stream (a cudaStream_t), for event timing by the caller. */
 afar_status afar_get_stream(afar_solver* solver, void** stream);
 
+/* afar_run with CUDA events recorded on the solver's stream around the steps; *ms receives the
+ * device time of the nSteps steps. */
+afar_status afar_run_timed(afar_solver* solver, int nSteps, double deltaT, double CFL, double tEnd, float* ms);
+
+/* Runs one step kernel by kernel (not as a graph) with events between the kernels and returns
+ * the device time of each kind summed over the three stages: ms[0] reconstruct, ms[1] BVD switch,
+ * ms[2] face flux (with the CFL kernel where the policy runs one), ms[3] gather + RK update,
+ * ms[4] step bookkeeping. */
+afar_status afar_profile_step(afar_solver* solver, double deltaT, double CFL, float ms[5]);
+
 /* Simulated time, last step size and number of steps taken on the device. */
 afar_status afar_get_time(afar_solver* solver, double* t, double* lastDeltaT, long long* steps);
 afar_status afar_set_time(afar_solver* solver, double t);
@@ -270,6 +280,13 @@ afar_status afar_upload_state(afar_solver* solver, const afar_basicFieldData* FD
                               const afar_conservedFieldData* cFDold);
 afar_status afar_download_state(afar_solver* solver, afar_basicFieldData* FD,
                                 afar_conservedFieldData* cFD, int8_t* shockIndicator);
+
+/* In-device checkpoint of the whole solver state (primitive + conserved fields, RK stage start,
+ * time and step count): op 0 saves, op 1 restores (bit-exact resume).  The snapshot lives in
+ * device memory next to the state; restore without a prior save is an error. */
+#define AFAR_SNAPSHOT_SAVE 0
+#define AFAR_SNAPSHOT_RESTORE 1
+afar_status afar_state_snapshot(afar_solver* solver, int op);
 
 /* The least-squares gradient matrix the device built (2*maxCompactStencilSize*cellsNum floats
  * in the reference layout; the FP64 policy keeps doubles internally and returns them rounded). */
