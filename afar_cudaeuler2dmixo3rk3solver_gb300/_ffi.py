@@ -93,6 +93,8 @@ def lib():
             "afar_run_timed": (S, [_p, C.c_int, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_float)]),
             "afar_profile_step": (S, [_p, C.c_double, C.c_double, C.POINTER(C.c_float)]),
             "afar_state_snapshot": (S, [_p, C.c_int]),
+            "afar_adjustTimeStep_noalloc": (S, [_p, _p, _p, _p, C.c_int, C.c_double, C.c_double, C.c_double, _p,
+                                                _p]),
             "afar_get_time": (S, [_p, C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
             "afar_set_time": (S, [_p, C.c_double]),
             "afar_stage_debug": (S, [_p, C.c_int, C.c_double, C.POINTER(FieldPointer)]),
@@ -131,5 +133,5 @@ EXPORTED = [
     "afar_set_rbf_basis64", "afar_run", "afar_run_async", "afar_synchronize", "afar_get_stream", "afar_get_time",
     "afar_set_time", "afar_stage_debug", "afar_debug_limiter64", "afar_upload_state", "afar_download_state",
     "afar_download_ls_matrix", "afar_device_bytes", "afar_launches_per_step", "afar_run_timed",
-    "afar_profile_step", "afar_state_snapshot",
+    "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc",
 ]

@@ -54,6 +54,7 @@ def build_lib(force=False, verbose=False) -> str:
     headers.append(os.path.join(ROOT, "include", "afar.h"))
     units = [
         ("afar_solver.cu", "nvcc"),
+        ("afar_noalloc.cu", "nvcc"),
         ("afar_precompute.cpp", "cxx"),
         ("afar_error.cpp", "cxx"),
     ]
