@@ -100,7 +100,7 @@ constexpr int kMaxFaces = 4;
 // flight per thread; no shared memory, so occupancy is set by registers alone.  Every sum is
 // still accumulated in stencil order, as in the reference.
 template <class P>
-__global__ void __launch_bounds__(128) k_reconstruct(StageArgs<P> a) {
+__global__ void __launch_bounds__(128, 5) k_reconstruct(StageArgs<P> a) {
   using S = typename P::S;
   using G = typename P::G;
   using WT = typename P::W;
@@ -802,13 +802,23 @@ __global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
       const StepCtl* ctl = a.ctl;
       if (!(ctl->dt_fixed > 0.0)) {  // setDeltaT, cudaFieldOperation.h:140-157
         const V2<double> g = a.dtg[id];
-        const double deltaR = g.x, fraction = g.y;
-        const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
-        const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
-        dtf = CFL * deltaR * msf /
-              ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
-               fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
-               sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
+        if constexpr (P::id == PolicyMixed::id) {
+          // the mixed policy estimates the Courant step in FP32 (an estimate, not an accumulation;
+          // in FP64 its division and square root made this launch FP64-pipe bound)
+          const float deltaR = (float)g.x, fraction = (float)g.y;
+          const float cfl = (float)ctl->cfl, gR = (float)(a.gamma * a.R);
+          dtf = cfl * deltaR * magSf /
+                ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
+                 sqrtf(gR * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+        } else {
+          const double deltaR = g.x, fraction = g.y;
+          const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
+          const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
+          dtf = CFL * deltaR * msf /
+                ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
+                 fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
+                 sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
+        }
       }
     }
   } else if (id < a.Nf + a.Nb) {  // boundary faces, reference :254-270
@@ -913,11 +923,18 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
                                           (double)hi[3] + lo[3]};
   const float s3 = (float)(-beta3 * deltaT * a.vinv[c]);
   const V4<double> o = a.U0[c];
-  const V4<double> u = a.U[c];
-  const double rho = fma(beta2, u.x, beta1 * o.x) + (double)(s3 * (hi[0] + lo[0]));
-  const double rhoUx = fma(beta2, u.y, beta1 * o.y) + (double)(s3 * (hi[1] + lo[1]));
-  const double rhoUy = fma(beta2, u.z, beta1 * o.z) + (double)(s3 * (hi[2] + lo[2]));
-  const double rhoE = fma(beta2, u.w, beta1 * o.w) + (double)(s3 * (hi[3] + lo[3]));
+  V4<double> base;
+  if (beta2 == 0.0 && beta1 == 1.0) {  // first RK stage: U = Un + increment, U itself not read
+    base = o;
+  } else {
+    const V4<double> u = a.U[c];
+    base = V4<double>{fma(beta2, u.x, beta1 * o.x), fma(beta2, u.y, beta1 * o.y), fma(beta2, u.z, beta1 * o.z),
+                      fma(beta2, u.w, beta1 * o.w)};
+  }
+  const double rho = base.x + (double)(s3 * (hi[0] + lo[0]));
+  const double rhoUx = base.y + (double)(s3 * (hi[1] + lo[1]));
+  const double rhoUy = base.z + (double)(s3 * (hi[2] + lo[2]));
+  const double rhoE = base.w + (double)(s3 * (hi[3] + lo[3]));
   const V4<double> un{rho, rhoUx, rhoUy, rhoE};
   a.U[c] = un;
   if (last_stage) a.U0[c] = un;
@@ -946,9 +963,12 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
 template <class P>
 __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double beta1, const double beta2,
                                                 const double beta3, const int last_stage) {
+  __shared__ double s_dt;  // the step size, read once per block
+  if (threadIdx.x == 0) s_dt = step_dt(a.ctl);
+  __syncthreads();
+  const double deltaT = s_dt;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.Nc) return;
-  const double deltaT = step_dt(a.ctl);
   if (!(deltaT > 0.0)) return;  // past t_end: the step is a no-op
   const int ldc = a.ldc;
   const int nM = a.nM[c];
