@@ -104,6 +104,13 @@ def lib():
             "afar_download_ls_matrix": (S, [_p, _p]),
             "afar_device_bytes": (S, [_p, C.POINTER(C.c_size_t)]),
             "afar_launches_per_step": (C.c_int, [_p]),
+            "afar_set_step_params": (S, [_p, C.c_double, C.c_double, C.c_double]),
+            "afar_batch_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),
+            "afar_batch_add": (S, [_p, _p]),
+            "afar_batch_remove": (S, [_p, _p]),
+            "afar_batch_size": (S, [_p, C.POINTER(C.c_int)]),
+            "afar_batch_run": (S, [_p, C.c_int, C.POINTER(C.c_float)]),
+            "afar_batch_destroy": (S, [_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -133,5 +140,7 @@ EXPORTED = [
     "afar_set_rbf_basis64", "afar_run", "afar_run_async", "afar_synchronize", "afar_get_stream", "afar_get_time",
     "afar_set_time", "afar_stage_debug", "afar_debug_limiter64", "afar_upload_state", "afar_download_state",
     "afar_download_ls_matrix", "afar_device_bytes", "afar_launches_per_step", "afar_run_timed",
-    "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc",
+    "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc", "afar_set_step_params",
+    "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
+    "afar_batch_destroy",
 ]

@@ -100,11 +100,11 @@ constexpr int kMaxFaces = 4;
 // flight per thread; no shared memory, so occupancy is set by registers alone.  Every sum is
 // still accumulated in stencil order, as in the reference.
 template <class P>
-__global__ void __launch_bounds__(128, 5) k_reconstruct(StageArgs<P> a) {
+__device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk) {
   using S = typename P::S;
   using G = typename P::G;
   using WT = typename P::W;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blk * blockDim.x + threadIdx.x;
   if (c >= a.Nc) return;
   const int ldc = a.ldc;
   const int nS = a.nS[c], nM = a.nM[c];
@@ -280,14 +280,14 @@ __global__ void __launch_bounds__(128, 5) k_reconstruct(StageArgs<P> a) {
 // values with its weights loaded eight at a time.  These policies are bound by the FP64 pipe, so
 // the kernel keeps the per-face loop (no work on missing face slots) and a small register set.
 template <class P>
-__global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
+__device__ __forceinline__ void recon_staged_body(const StageArgs<P>& a, const int blk) {
   using S = typename P::S;
   using G = typename P::G;
   using WT = typename P::W;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V4<S>* sv = reinterpret_cast<V4<S>*>(smem_raw);  // [maxS][blockDim] staged stencil values
   const int t = threadIdx.x, B = blockDim.x;
-  const int c = blockIdx.x * B + t;
+  const int c = blk * B + t;
   if (c >= a.Nc) return;
   const int ldc = a.ldc;
   const int nS = a.nS[c], nM = a.nM[c];
@@ -435,10 +435,10 @@ __device__ __forceinline__ S to_venkat(const S y) {
 // BVDindicator (reference cudaLimiter.h:319-464): stencil flag counts, BVD test on T, final
 // switch type, limiter transform.
 template <class P>
-__global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
+__device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
   using S = typename P::S;
   using G = typename P::G;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blk * blockDim.x + threadIdx.x;
   if (c >= a.Nc) return;
   const int ldc = a.ldc;
   const int nS = a.nS[c], nM = a.nM[c];
@@ -732,12 +732,12 @@ __global__ void __launch_bounds__(128) k_flux_ref_layout(RFlux* __restrict__ Flu
 // only, which holds on every mesh with Nf >= Nb).  DT: also reduce the CFL step of the reference's
 // setDeltaT (cudaFieldOperation.h:124-180) from the state at the start of the step.
 template <class P, bool DT>
-__global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
+__device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) {
   using S = typename P::S;
   using G = typename P::G;
   using D = typename P::D;
   using RC = typename P::RC;
-  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  const int id = blk * blockDim.x + threadIdx.x;
   double dtf = 1e5;
   if (id < a.Nf) {
     const int2 on = a.on[id];
@@ -961,13 +961,13 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
 // face fluxes in the cell's face order (no atomics), SSP-RK3 combine, conserved -> primitive, and
 // the ghost state of this cell's boundary faces from the new state.
 template <class P>
-__global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double beta1, const double beta2,
-                                                const double beta3, const int last_stage) {
-  __shared__ double s_dt;  // the step size, read once per block
+__device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk, const double beta1,
+                                            const double beta2, const double beta3, const int last_stage) {
+  __shared__ double s_dt;  // the step size, read once per block (a block never spans two solves)
   if (threadIdx.x == 0) s_dt = step_dt(a.ctl);
   __syncthreads();
   const double deltaT = s_dt;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = blk * blockDim.x + threadIdx.x;
   if (c >= a.Nc) return;
   if (!(deltaT > 0.0)) return;  // past t_end: the step is a no-op
   const int ldc = a.ldc;
@@ -1038,7 +1038,74 @@ __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double bet
   }
 }
 
+// ------------------------------------------------------------------------- by-value kernels
+// The reference-parity policy passes its arguments by value (its flux runs k_flux_ref_layout).
+template <class P>
+__global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
+  recon_staged_body<P>(a, blockIdx.x);
+}
+template <class P>
+__global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
+  bvd_body<P>(a, blockIdx.x);
+}
+template <class P>
+__global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double beta1, const double beta2,
+                                                const double beta3, const int last_stage) {
+  update_body<P>(a, blockIdx.x, beta1, beta2, beta3, last_stage);
+}
+
+// ------------------------------------------------------------------------- batch kernels
+// Many independent solves in one launch: block b works on solve map[b].x, as that solve's block
+// map[b].y (map == nullptr: one solve, tab[0], block b).  A block never spans two solves, so
+// block-level reductions (the CFL minimum, the step size) stay within one solve.  A single solve
+// of the fp64/mixed policies runs these same kernels on a one-entry table, so its result is
+// bitwise the same alone and in a batch.
+template <class P>
+__global__ void __launch_bounds__(128, 5) kb_reconstruct(const StageArgs<P>* __restrict__ tab,
+                                                         const int2* __restrict__ map) {
+  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  recon_body<P>(tab[m.x], m.y);
+}
+template <class P>
+__global__ void __launch_bounds__(128) kb_reconstruct_staged(const StageArgs<P>* __restrict__ tab,
+                                                             const int2* __restrict__ map) {
+  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  recon_staged_body<P>(tab[m.x], m.y);
+}
+template <class P>
+__global__ void __launch_bounds__(128) kb_bvd(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
+  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  bvd_body<P>(tab[m.x], m.y);
+}
+template <class P, bool DT>
+__global__ void __launch_bounds__(256) kb_flux(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
+  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  flux_body<P, DT>(tab[m.x], m.y);
+}
+template <class P>
+__global__ void __launch_bounds__(128) kb_update(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map,
+                                                 const double beta1, const double beta2, const double beta3,
+                                                 const int last_stage) {
+  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  update_body<P>(tab[m.x], m.y, beta1, beta2, beta3, last_stage);
+}
+
 // Closes a step: advance time, record the step, re-arm the CFL minimum for the next step.
+__device__ __forceinline__ void finish_one(StepCtl* ctl) {
+  const double dt = step_dt(ctl);
+  if (dt > 0.0) {
+    ctl->t += dt;
+    ctl->steps += 1;
+    ctl->last_dt = dt;
+  }
+  ctl->dt_bits = (unsigned long long)__double_as_longlong(1e5);
+}
+template <class P>
+__global__ void kb_finish_step(const StageArgs<P>* __restrict__ tab, const int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) finish_one(tab[i].ctl);
+}
+
 __global__ void k_finish_step(StepCtl* ctl) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     const double dt = step_dt(ctl);

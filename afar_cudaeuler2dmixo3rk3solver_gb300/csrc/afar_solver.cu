@@ -9,6 +9,8 @@
 
 #include <cstring>
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "afar_internal.h"
@@ -139,6 +141,7 @@ struct afar_solver {
   V2<double>* dtg = nullptr;
   V2<double>* bn = nullptr;
   V4<double>* res_dbg = nullptr;
+  void* args = nullptr;  // device StageArgs: [0] stepping, [1] stage debug (fp64/mixed policies)
   StepCtl* ctl = nullptr;
   unsigned long long* dt_bits = nullptr;
   // policy-typed device arrays (element size depends on the policy)
@@ -220,7 +223,36 @@ StageArgs<P> make_args(afar_solver* s) {
   return a;
 }
 
-// The mixed policy reconstructs in one register pass (k_reconstruct); the FP64-bound policies use
+// Device slot size of one StageArgs (any policy).
+constexpr size_t kArgsSlot =
+    (std::max({sizeof(StageArgs<PolicyRef>), sizeof(StageArgs<PolicyFP64>), sizeof(StageArgs<PolicyMixed>)}) + 255) /
+    256 * 256;
+
+// Copies a solver's StageArgs into its device slot (read by the kb_* kernels).  Not during capture.
+template <class P>
+afar_status upload_args(afar_solver* s, int slot, const StageArgs<P>& a) {
+  void* dst = static_cast<char*>(s->args) + slot * kArgsSlot;
+  AFAR_CUDA(cudaMemcpyAsync(dst, &a, sizeof(a), cudaMemcpyHostToDevice, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  return AFAR_OK;
+}
+
+// cudaFuncAttributeMaxDynamicSharedMemorySize of a staged reconstruct kernel only grows (per
+// device), so solvers and batches of different stencil sizes never lower one another's limit.
+template <class K>
+afar_status raise_smem_limit(K kernel, int device, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = done[{reinterpret_cast<const void*>(kernel), device}];
+  if (bytes > cur) {
+    AFAR_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+  }
+  return AFAR_OK;
+}
+
+// The mixed policy reconstructs in one register pass (recon_body); the FP64-bound policies use
 // the shared-memory staged variant, which keeps their FP64 work per face slot.
 template <class P>
 size_t recon_smem(const afar_solver* s) {
@@ -228,54 +260,82 @@ size_t recon_smem(const afar_solver* s) {
   return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
 }
 
+// One solve's stage launches.  The ref policy passes its arguments by value (k_*); fp64/mixed run
+// the batched kernels (kb_*) on the solver's one-entry device table, so one solve executes the
+// same code alone and inside a batch.
 template <class P>
-void launch_reconstruct(afar_solver* s, const StageArgs<P>& a) {
-  const int gc = grid_for(s->Nc, kCellBlock);
-  if constexpr (P::id == PolicyMixed::id)
-    k_reconstruct<P><<<gc, kCellBlock, 0, s->stream>>>(a);
-  else
-    k_reconstruct_staged<P><<<gc, kCellBlock, recon_smem<P>(s), s->stream>>>(a);
-}
+struct Stage {
+  afar_solver* s;
+  StageArgs<P> a;          // host copy (ref policy)
+  const StageArgs<P>* da;  // device copy (fp64/mixed)
+  static constexpr bool kByValue = P::id == PolicyRef::id;
+  int gc() const { return grid_for(s->Nc, kCellBlock); }
 
-// Enqueues one RK stage.  dt_stage: fuse the CFL reduction into the flux kernel.
-// The face flux of one stage.  The ref policy runs the reference-layout kernel (its fused
-// multiply-adds then fall where the reference's do) and, on the first stage, the CFL step as a
-// kernel of its own like the reference's setDeltaT; the other policies fuse the CFL reduction
-// into the flux kernel.
-template <class P>
-void enqueue_flux(afar_solver* s, const StageArgs<P>& a, bool dt_stage) {
-  if constexpr (P::id == PolicyRef::id) {
-    if (dt_stage && s->Nf > 0)
-      k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
-    const int gr = grid_for(std::max(s->Nf, s->Nb), 128);
-    k_flux_ref_layout<<<gr, 128, 0, s->stream>>>(
-        reinterpret_cast<RFlux*>(s->flux), reinterpret_cast<const RField*>(s->W), reinterpret_cast<const RGrad*>(s->grad),
-        reinterpret_cast<const RLim*>(s->lim), reinterpret_cast<const RField*>(s->fv), s->si,
-        reinterpret_cast<const RCell*>(s->cellC), reinterpret_cast<const RFace*>(s->faceRaw),
-        reinterpret_cast<const int*>(s->on), s->Nf, s->Nc, s->Nb, a.R, a.Cv);
-  } else {
-    const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
-    if (dt_stage)
-      k_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(a);
+  void reconstruct() const {
+    if constexpr (kByValue)
+      k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
+    else if constexpr (P::id == PolicyMixed::id)
+      kb_reconstruct<P><<<gc(), kCellBlock, 0, s->stream>>>(da, nullptr);
     else
-      k_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(a);
+      kb_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(da, nullptr);
   }
+  void bvd() const {
+    if constexpr (kByValue)
+      k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
+    else
+      kb_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(da, nullptr);
+  }
+  // The face flux.  The ref policy runs the reference-layout kernel (its fused multiply-adds then
+  // fall where the reference's do) and, on the first stage, the CFL step as a kernel of its own
+  // like the reference's setDeltaT; the other policies fuse the CFL reduction into the flux.
+  void flux(bool dt_stage) const {
+    if constexpr (kByValue) {
+      if (dt_stage && s->Nf > 0)
+        k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
+      const int gr = grid_for(std::max(s->Nf, s->Nb), 128);
+      k_flux_ref_layout<<<gr, 128, 0, s->stream>>>(
+          reinterpret_cast<RFlux*>(s->flux), reinterpret_cast<const RField*>(s->W),
+          reinterpret_cast<const RGrad*>(s->grad), reinterpret_cast<const RLim*>(s->lim),
+          reinterpret_cast<const RField*>(s->fv), s->si, reinterpret_cast<const RCell*>(s->cellC),
+          reinterpret_cast<const RFace*>(s->faceRaw), reinterpret_cast<const int*>(s->on), s->Nf, s->Nc, s->Nb, a.R,
+          a.Cv);
+    } else {
+      const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
+      if (dt_stage)
+        kb_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(da, nullptr);
+      else
+        kb_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(da, nullptr);
+    }
+  }
+  void update(int k) const {
+    if constexpr (kByValue)
+      k_update<P><<<gc(), kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+    else
+      kb_update<P><<<gc(), kCellBlock, 0, s->stream>>>(da, nullptr, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+  }
+};
+
+// Stage launcher of a solver; debug = true writes the residual copy (afar_stage_debug).
+template <class P>
+afar_status make_stage(afar_solver* s, bool debug, Stage<P>* out) {
+  out->s = s;
+  out->a = make_args<P>(s);
+  if (debug) out->a.res_dbg = s->res_dbg;
+  const int slot = debug ? 1 : 0;
+  out->da = reinterpret_cast<const StageArgs<P>*>(static_cast<char*>(s->args) + slot * kArgsSlot);
+  if constexpr (!Stage<P>::kByValue) return upload_args<P>(s, slot, out->a);
+  return AFAR_OK;
 }
 
 template <class P>
-void enqueue_stage(afar_solver* s, const StageArgs<P>& a, int k, bool dt_stage) {
-  const int gc = grid_for(s->Nc, kCellBlock);
-  launch_reconstruct<P>(s, a);
-  k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
-  enqueue_flux<P>(s, a, dt_stage);
-  k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
-}
-
-template <class P>
-void enqueue_step(afar_solver* s) {
-  const StageArgs<P> a = make_args<P>(s);
-  for (int k = 0; k < 3; ++k) enqueue_stage<P>(s, a, k, k == 0);
-  k_finish_step<<<1, 32, 0, s->stream>>>(s->ctl);
+void enqueue_step(const Stage<P>& st) {
+  for (int k = 0; k < 3; ++k) {
+    st.reconstruct();
+    st.bvd();
+    st.flux(k == 0);
+    st.update(k);
+  }
+  k_finish_step<<<1, 32, 0, st.s->stream>>>(st.s->ctl);
 }
 
 template <class P>
@@ -330,9 +390,8 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaFree(fxy));
   AFAR_CUDA(cudaFree(fsr));
-  if constexpr (P::id != PolicyMixed::id)
-    AFAR_CUDA(cudaFuncSetAttribute(k_reconstruct_staged<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)recon_smem<P>(s)));
+  if constexpr (P::id == PolicyRef::id) return raise_smem_limit(k_reconstruct_staged<P>, s->device, recon_smem<P>(s));
+  if constexpr (P::id == PolicyFP64::id) return raise_smem_limit(kb_reconstruct_staged<P>, s->device, recon_smem<P>(s));
   return AFAR_OK;
 }
 
@@ -342,13 +401,23 @@ afar_status capture_graph(afar_solver* s) {
     s->graph = nullptr;
   }
   cudaGraph_t g = nullptr;
-  AFAR_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  auto capture = [&](auto tag) -> afar_status {
+    using P = decltype(tag);
+    Stage<P> st;
+    afar_status r = make_stage<P>(s, false, &st);  // uploads the argument table before the capture
+    if (r) return r;
+    AFAR_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step<P>(st);
+    AFAR_CUDA(cudaStreamEndCapture(s->stream, &g));
+    return AFAR_OK;
+  };
+  afar_status r;
   switch (s->policy) {
-    case AFAR_POLICY_REF: enqueue_step<PolicyRef>(s); break;
-    case AFAR_POLICY_FP64: enqueue_step<PolicyFP64>(s); break;
-    default: enqueue_step<PolicyMixed>(s); break;
+    case AFAR_POLICY_REF: r = capture(PolicyRef{}); break;
+    case AFAR_POLICY_FP64: r = capture(PolicyFP64{}); break;
+    default: r = capture(PolicyMixed{}); break;
   }
-  AFAR_CUDA(cudaStreamEndCapture(s->stream, &g));
+  if (r) return r;
   const cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) {
@@ -609,6 +678,7 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
   }
   if (st) return st;
   if ((st = dalloc_t(s, &s->res_dbg, (size_t)Nc))) return st;
+  if ((st = dalloc(s, &s->args, 2 * kArgsSlot))) return st;
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   s->have_stencil = true;
   return AFAR_OK;
@@ -760,29 +830,32 @@ extern "C" afar_status afar_profile_step(afar_solver* s, double dt, double CFL, 
     cudaEventRecord(ev[n], s->stream);
     kind[n++] = k;
   };
-  auto body = [&](auto tag) {
+  auto body = [&](auto tag) -> afar_status {
     using P = decltype(tag);
-    const StageArgs<P> a = make_args<P>(s);
-    const int gc = grid_for(s->Nc, kCellBlock);
+    Stage<P> sg;
+    afar_status r = make_stage<P>(s, false, &sg);
+    if (r) return r;
     mark(-1);
     for (int k = 0; k < 3; ++k) {
-      launch_reconstruct<P>(s, a);
+      sg.reconstruct();
       mark(0);
-      k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
+      sg.bvd();
       mark(1);
-      enqueue_flux<P>(s, a, k == 0);
+      sg.flux(k == 0);
       mark(2);
-      k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+      sg.update(k);
       mark(3);
     }
     k_finish_step<<<1, 32, 0, s->stream>>>(s->ctl);
     mark(4);
+    return AFAR_OK;
   };
   switch (s->policy) {
-    case AFAR_POLICY_REF: body(PolicyRef{}); break;
-    case AFAR_POLICY_FP64: body(PolicyFP64{}); break;
-    default: body(PolicyMixed{}); break;
+    case AFAR_POLICY_REF: st = body(PolicyRef{}); break;
+    case AFAR_POLICY_FP64: st = body(PolicyFP64{}); break;
+    default: st = body(PolicyMixed{}); break;
   }
+  if (st) return st;
   AFAR_CUDA(cudaEventSynchronize(ev[n - 1]));
   for (int k = 0; k < 5; ++k) ms[k] = 0.f;
   for (int i = 1; i < n; ++i) {
@@ -839,23 +912,25 @@ extern "C" afar_status afar_stage_debug(afar_solver* s, int stage, double deltaT
   if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
   k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, deltaT, 1.0, 0.0);
   const size_t Nc = s->Nc, Nf = s->Nf, Nb = s->Nb;
-  const int gc = grid_for(s->Nc, kCellBlock);
   const bool mixed = s->policy == AFAR_POLICY_MIXED;
   const bool f64 = s->policy == AFAR_POLICY_FP64;
-  auto run = [&](auto tag) {
+  auto run = [&](auto tag) -> afar_status {
     using P = decltype(tag);
-    StageArgs<P> a = make_args<P>(s);
-    a.res_dbg = s->res_dbg;
-    launch_reconstruct<P>(s, a);
-    k_bvd<P><<<gc, kCellBlock, 0, s->stream>>>(a);
-    enqueue_flux<P>(s, a, false);
-    k_update<P><<<gc, kCellBlock, 0, s->stream>>>(a, kBeta1[stage], kBeta2[stage], kBeta3[stage], stage == 2);
+    Stage<P> sg;
+    afar_status r = make_stage<P>(s, true, &sg);
+    if (r) return r;
+    sg.reconstruct();
+    sg.bvd();
+    sg.flux(false);
+    sg.update(stage);
+    return AFAR_OK;
   };
   switch (s->policy) {
-    case AFAR_POLICY_REF: run(PolicyRef{}); break;
-    case AFAR_POLICY_FP64: run(PolicyFP64{}); break;
-    default: run(PolicyMixed{}); break;
+    case AFAR_POLICY_REF: st = run(PolicyRef{}); break;
+    case AFAR_POLICY_FP64: st = run(PolicyFP64{}); break;
+    default: st = run(PolicyMixed{}); break;
   }
+  if (st) return st;
   AFAR_CUDA(cudaGetLastError());
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   // copy out in the reference layout
@@ -1027,5 +1102,209 @@ extern "C" afar_status afar_freeFieldData(afar_solver* s) {
   for (void* p : s->allocs) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
+  return AFAR_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// step parameters and batches
+
+extern "C" afar_status afar_set_step_params(afar_solver* s, double dt, double CFL, double tEnd) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!(dt > 0.0) && !(CFL > 0.0)) return (set_error("afar_set_step_params: deltaT or CFL must be positive"), AFAR_ERR_ARGUMENT);
+  k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, tEnd);
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+struct afar_batch {
+  int policy = AFAR_POLICY_MIXED;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<afar_solver*> members;
+  void* tab = nullptr;  // StageArgs<P>[members]
+  size_t tab_bytes = 0;
+  int2* cmap = nullptr;  // per cell block: (member, block within member)
+  int2* fmap = nullptr;  // per face block
+  size_t cmap_n = 0, fmap_n = 0;
+  int ncb = 0, nfb = 0;
+  size_t smem = 0;  // dynamic shared memory of the staged reconstruct (largest member)
+  cudaGraphExec_t graph = nullptr;
+  bool dirty = true;
+};
+
+namespace {
+
+template <class P>
+afar_status batch_build(afar_batch* b) {
+  std::vector<StageArgs<P>> tab;
+  std::vector<int2> cm, fm;
+  size_t smem = 0;
+  for (size_t i = 0; i < b->members.size(); ++i) {
+    afar_solver* s = b->members[i];
+    tab.push_back(make_args<P>(s));
+    const int nc = grid_for(s->Nc, kCellBlock), nf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
+    for (int k = 0; k < nc; ++k) cm.push_back(int2{(int)i, k});
+    for (int k = 0; k < nf; ++k) fm.push_back(int2{(int)i, k});
+    smem = std::max(smem, recon_smem<P>(s));
+  }
+  auto grow = [&](void** p, size_t* cap, size_t need) -> afar_status {
+    if (need > *cap) {
+      if (*p) cudaFree(*p);
+      *p = nullptr;
+      AFAR_CUDA(cudaMalloc(p, need));
+      *cap = need;
+    }
+    return AFAR_OK;
+  };
+  afar_status st;
+  size_t cap_c = b->cmap_n * sizeof(int2), cap_f = b->fmap_n * sizeof(int2);
+  if ((st = grow(&b->tab, &b->tab_bytes, std::max<size_t>(1, tab.size()) * sizeof(StageArgs<P>)))) return st;
+  if ((st = grow(reinterpret_cast<void**>(&b->cmap), &cap_c, std::max<size_t>(1, cm.size()) * sizeof(int2)))) return st;
+  if ((st = grow(reinterpret_cast<void**>(&b->fmap), &cap_f, std::max<size_t>(1, fm.size()) * sizeof(int2)))) return st;
+  b->cmap_n = cap_c / sizeof(int2);
+  b->fmap_n = cap_f / sizeof(int2);
+  if (!tab.empty()) {
+    AFAR_CUDA(cudaMemcpyAsync(b->tab, tab.data(), tab.size() * sizeof(StageArgs<P>), cudaMemcpyHostToDevice, b->stream));
+    AFAR_CUDA(cudaMemcpyAsync(b->cmap, cm.data(), cm.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    AFAR_CUDA(cudaMemcpyAsync(b->fmap, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+  }
+  AFAR_CUDA(cudaStreamSynchronize(b->stream));
+  b->ncb = (int)cm.size();
+  b->nfb = (int)fm.size();
+  b->smem = smem;
+  if constexpr (P::id != PolicyMixed::id) {
+    if ((st = raise_smem_limit(kb_reconstruct_staged<P>, b->device, smem))) return st;
+  }
+  // capture one step of the whole batch
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (tab.empty()) {
+    b->dirty = false;
+    return AFAR_OK;
+  }
+  const StageArgs<P>* t = static_cast<const StageArgs<P>*>(b->tab);
+  cudaGraph_t g = nullptr;
+  AFAR_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  for (int k = 0; k < 3; ++k) {
+    if constexpr (P::id == PolicyMixed::id)
+      kb_reconstruct<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap);
+    else
+      kb_reconstruct_staged<P><<<b->ncb, kCellBlock, b->smem, b->stream>>>(t, b->cmap);
+    kb_bvd<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap);
+    if (k == 0)
+      kb_flux<P, true><<<b->nfb, kFaceBlock, 0, b->stream>>>(t, b->fmap);
+    else
+      kb_flux<P, false><<<b->nfb, kFaceBlock, 0, b->stream>>>(t, b->fmap);
+    kb_update<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+  }
+  kb_finish_step<P><<<grid_for((long long)tab.size(), 128), 128, 0, b->stream>>>(t, (int)tab.size());
+  AFAR_CUDA(cudaStreamEndCapture(b->stream, &g));
+  const cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    b->graph = nullptr;
+    set_error("batch graph instantiation failed: %s", cudaGetErrorString(e));
+    return AFAR_ERR_CUDA;
+  }
+  b->dirty = false;
+  return AFAR_OK;
+}
+
+}  // namespace
+
+extern "C" afar_status afar_batch_create(afar_batch** out, int policy, int device) {
+  if (!out || (policy != AFAR_POLICY_MIXED && policy != AFAR_POLICY_FP64)) {
+    set_error("afar_batch_create: null output or policy other than fp64/mixed");
+    return AFAR_ERR_ARGUMENT;
+  }
+  *out = nullptr;
+  AFAR_CUDA(cudaSetDevice(device));
+  afar_batch* b = new afar_batch();
+  b->policy = policy;
+  b->device = device;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    set_error("cudaStreamCreate failed");
+    return AFAR_ERR_CUDA;
+  }
+  *out = b;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_batch_add(afar_batch* b, afar_solver* s) {
+  if (!b || !s) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (s->policy != b->policy || s->device != b->device)
+    return (set_error("afar_batch_add: member policy/device differ from the batch's"), AFAR_ERR_ARGUMENT);
+  if (!(s->R > 0.0)) return (set_error("afar_batch_add: call afar_set_gas on the member first"), AFAR_ERR_STATE);
+  if (!s->have_stencil)
+    return (set_error("afar_batch_add: upload the stencil (afar_setDeviceFieldDataStencil) first"), AFAR_ERR_STATE);
+  for (afar_solver* m : b->members)
+    if (m == s) return (set_error("afar_batch_add: already a member"), AFAR_ERR_STATE);
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));  // no pending work of the member on its own stream
+  b->members.push_back(s);
+  b->dirty = true;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_batch_remove(afar_batch* b, afar_solver* s) {
+  if (!b || !s) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  for (size_t i = 0; i < b->members.size(); ++i)
+    if (b->members[i] == s) {
+      AFAR_CUDA(cudaSetDevice(b->device));
+      AFAR_CUDA(cudaStreamSynchronize(b->stream));
+      b->members.erase(b->members.begin() + i);
+      b->dirty = true;
+      return AFAR_OK;
+    }
+  set_error("afar_batch_remove: not a member");
+  return AFAR_ERR_ARGUMENT;
+}
+
+extern "C" afar_status afar_batch_size(afar_batch* b, int* n) {
+  if (!b || !n) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  *n = (int)b->members.size();
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_batch_run(afar_batch* b, int nSteps, float* ms) {
+  if (!b || nSteps < 0) return (set_error("afar_batch_run: bad argument"), AFAR_ERR_ARGUMENT);
+  AFAR_CUDA(cudaSetDevice(b->device));
+  afar_status st;
+  if (b->dirty) {
+    st = b->policy == AFAR_POLICY_MIXED ? batch_build<PolicyMixed>(b) : batch_build<PolicyFP64>(b);
+    if (st) return st;
+  }
+  if (ms) *ms = 0.f;
+  if (b->members.empty() || nSteps == 0) return AFAR_OK;
+  cudaEvent_t e0, e1;
+  AFAR_CUDA(cudaEventCreate(&e0));
+  AFAR_CUDA(cudaEventCreate(&e1));
+  AFAR_CUDA(cudaEventRecord(e0, b->stream));
+  for (int i = 0; i < nSteps; ++i) AFAR_CUDA(cudaGraphLaunch(b->graph, b->stream));
+  AFAR_CUDA(cudaEventRecord(e1, b->stream));
+  AFAR_CUDA(cudaEventSynchronize(e1));
+  if (ms) AFAR_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_batch_destroy(afar_batch* b) {
+  if (!b) return AFAR_OK;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->tab) cudaFree(b->tab);
+  if (b->cmap) cudaFree(b->cmap);
+  if (b->fmap) cudaFree(b->fmap);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
   return AFAR_OK;
 }

@@ -304,6 +304,11 @@ class CudaSolver:
         check(lib().afar_download_ls_matrix(self.h, ptr(out)))
         return out
 
+    def set_step_params(self, dt: float = 0.0, cfl: float | None = None, t_end: float = 0.0):
+        """Step control used when this solver is stepped inside a Batch (fixed dt, or CFL; t_end clamps)."""
+        cfl = self.cfg.CFL if cfl is None else cfl
+        check(lib().afar_set_step_params(self.h, dt, cfl, t_end))
+
     def device_bytes(self) -> int:
         b = C.c_size_t()
         check(lib().afar_device_bytes(self.h, C.byref(b)))
@@ -313,6 +318,49 @@ class CudaSolver:
         if self.h:
             lib().afar_freeFieldData(self.h)
             self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several solves (meshes, states, step controls of their own) advanced by one graph of batched
+    launches: each kernel's grid covers the blocks of every member.  A member's result is bitwise the
+    one it gets when stepped alone.  Members join and leave between runs."""
+
+    def __init__(self, policy="mixed", device=0):
+        self.policy = policy
+        self.h = C.c_void_p()
+        self.members = []
+        check(lib().afar_batch_create(C.byref(self.h), _ffi.POLICIES[policy], device))
+
+    def add(self, solver: CudaSolver):
+        check(lib().afar_batch_add(self.h, solver.h))
+        self.members.append(solver)
+
+    def remove(self, solver: CudaSolver):
+        check(lib().afar_batch_remove(self.h, solver.h))
+        self.members.remove(solver)
+
+    def __len__(self):
+        n = C.c_int()
+        check(lib().afar_batch_size(self.h, C.byref(n)))
+        return n.value
+
+    def run(self, n_steps: int) -> float:
+        """Advance every member n_steps; returns device milliseconds (CUDA events on the batch stream)."""
+        ms = C.c_float()
+        check(lib().afar_batch_run(self.h, n_steps, C.byref(ms)))
+        return ms.value
+
+    def close(self):
+        if self.h:
+            lib().afar_batch_destroy(self.h)
+            self.h = C.c_void_p()
+            self.members = []
 
     def __del__(self):
         try:

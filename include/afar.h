@@ -281,6 +281,28 @@ afar_status afar_upload_state(afar_solver* solver, const afar_basicFieldData* FD
 afar_status afar_download_state(afar_solver* solver, afar_basicFieldData* FD,
                                 afar_conservedFieldData* cFD, int8_t* shockIndicator);
 
+/* Step control of one solver for afar_run-style stepping inside a batch: fixed deltaT (> 0) or
+ * the device CFL step, and an end time (<= 0: none). */
+afar_status afar_set_step_params(afar_solver* solver, double deltaT, double CFL, double tEnd);
+
+/* ---- batches: many independent solves stepped by the same kernel launches ------------------- */
+/* A batch steps all of its member solvers with one launch per stage kernel (13 per RK3 step,
+ * replayed as one CUDA graph): every block works on one member, so meshes of uneven size share the
+ * GPU without padding.  Each member keeps its own device data, time step (fixed or CFL, with its
+ * own step params), end time and step count, and its result is bitwise the same as when it is run
+ * alone.  Members join and leave between runs without moving their data.  Policies fp64 and mixed;
+ * all members of a batch share the batch's policy and device.  A member must not be stepped on its
+ * own while it belongs to a batch. */
+typedef struct afar_batch afar_batch;
+afar_status afar_batch_create(afar_batch** batch, int policy, int device);
+afar_status afar_batch_add(afar_batch* batch, afar_solver* solver);
+afar_status afar_batch_remove(afar_batch* batch, afar_solver* solver);
+afar_status afar_batch_size(afar_batch* batch, int* members);
+/* nSteps RK3 steps of every member; *ms (may be NULL) receives the device time (CUDA events on
+ * the batch stream).  Waits for completion. */
+afar_status afar_batch_run(afar_batch* batch, int nSteps, float* ms);
+afar_status afar_batch_destroy(afar_batch* batch);
+
 /* In-device checkpoint of the whole solver state (primitive + conserved fields, RK stage start,
  * time and step count): op 0 saves, op 1 restores (bit-exact resume).  The snapshot lives in
  * device memory next to the state; restore without a prior save is an error. */

@@ -50,6 +50,14 @@ def test_last_error_and_null_arguments():
     assert L.afar_solver_create(C.byref(C.c_void_p()), 7, 0) == 1
     assert L.afar_freeFieldData(None) == 0
     assert L.afar_launches_per_step(None) == 13
+    # batches: the reference-parity policy is not batched; null arguments are rejected before any CUDA call
+    assert L.afar_batch_create(C.byref(C.c_void_p()), 0, 0) == 1
+    assert L.afar_batch_create(None, 2, 0) == 1
+    assert L.afar_batch_add(None, None) == 1
+    assert L.afar_batch_size(None, None) == 1
+    assert L.afar_batch_run(None, 1, None) == 1
+    assert L.afar_batch_destroy(None) == 0
+    assert L.afar_set_step_params(None, 0.0, 0.3, 0.0) != 0
 
 
 @pytest.mark.skipif(gpu_available(), reason="checks the no-device error path")
