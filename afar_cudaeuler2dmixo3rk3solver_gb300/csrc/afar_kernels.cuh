@@ -1038,8 +1038,12 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
   }
 }
 
-// ------------------------------------------------------------------------- by-value kernels
-// The reference-parity policy passes its arguments by value (its flux runs k_flux_ref_layout).
+// ------------------------------------------------------------------------- single-solve kernels
+// One solve per launch, arguments by value (read from the parameter bank).
+template <class P>
+__global__ void __launch_bounds__(128, 5) k_reconstruct(StageArgs<P> a) {
+  recon_body<P>(a, blockIdx.x);
+}
 template <class P>
 __global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
   recon_staged_body<P>(a, blockIdx.x);
@@ -1048,6 +1052,10 @@ template <class P>
 __global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
   bvd_body<P>(a, blockIdx.x);
 }
+template <class P, bool DT>
+__global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
+  flux_body<P, DT>(a, blockIdx.x);
+}
 template <class P>
 __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double beta1, const double beta2,
                                                 const double beta3, const int last_stage) {
@@ -1055,38 +1063,39 @@ __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double bet
 }
 
 // ------------------------------------------------------------------------- batch kernels
-// Many independent solves in one launch: block b works on solve map[b].x, as that solve's block
-// map[b].y (map == nullptr: one solve, tab[0], block b).  A block never spans two solves, so
-// block-level reductions (the CFL minimum, the step size) stay within one solve.  A single solve
-// of the fp64/mixed policies runs these same kernels on a one-entry table, so its result is
-// bitwise the same alone and in a batch.
+// Many independent solves in one launch: block b works on solve map[b].x (its arguments are
+// tab[map[b].x]), as that solve's block map[b].y.  A block never spans two solves, so block-level
+// reductions (the CFL minimum, the step size) stay within one solve, and a solve's result does not
+// depend on which other solves share the batch.
 template <class P>
 __global__ void __launch_bounds__(128, 5) kb_reconstruct(const StageArgs<P>* __restrict__ tab,
                                                          const int2* __restrict__ map) {
-  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  const int2 m = map[blockIdx.x];
   recon_body<P>(tab[m.x], m.y);
 }
 template <class P>
 __global__ void __launch_bounds__(128) kb_reconstruct_staged(const StageArgs<P>* __restrict__ tab,
                                                              const int2* __restrict__ map) {
-  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  const int2 m = map[blockIdx.x];
   recon_staged_body<P>(tab[m.x], m.y);
 }
 template <class P>
-__global__ void __launch_bounds__(128) kb_bvd(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
-  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+// mixed: 32 registers, 16 blocks (the full 64 warps) per SM for this gather-bound kernel
+__global__ void __launch_bounds__(128, P::id == PolicyMixed::id ? 16 : 10) kb_bvd(
+    const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
+  const int2 m = map[blockIdx.x];
   bvd_body<P>(tab[m.x], m.y);
 }
 template <class P, bool DT>
 __global__ void __launch_bounds__(256) kb_flux(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
-  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  const int2 m = map[blockIdx.x];
   flux_body<P, DT>(tab[m.x], m.y);
 }
 template <class P>
 __global__ void __launch_bounds__(128) kb_update(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map,
                                                  const double beta1, const double beta2, const double beta3,
                                                  const int last_stage) {
-  const int2 m = map ? map[blockIdx.x] : make_int2(0, (int)blockIdx.x);
+  const int2 m = map[blockIdx.x];
   update_body<P>(tab[m.x], m.y, beta1, beta2, beta3, last_stage);
 }
 
@@ -1107,15 +1116,7 @@ __global__ void kb_finish_step(const StageArgs<P>* __restrict__ tab, const int n
 }
 
 __global__ void k_finish_step(StepCtl* ctl) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const double dt = step_dt(ctl);
-    if (dt > 0.0) {
-      ctl->t += dt;
-      ctl->steps += 1;
-      ctl->last_dt = dt;
-    }
-    ctl->dt_bits = (unsigned long long)__double_as_longlong(1e5);
-  }
+  if (threadIdx.x == 0 && blockIdx.x == 0) finish_one(ctl);
 }
 
 // The CFL step alone (adjustTimeStep of the drop-in API): min over internal faces into *bits.

@@ -141,7 +141,6 @@ struct afar_solver {
   V2<double>* dtg = nullptr;
   V2<double>* bn = nullptr;
   V4<double>* res_dbg = nullptr;
-  void* args = nullptr;  // device StageArgs: [0] stepping, [1] stage debug (fp64/mixed policies)
   StepCtl* ctl = nullptr;
   unsigned long long* dt_bits = nullptr;
   // policy-typed device arrays (element size depends on the policy)
@@ -223,20 +222,6 @@ StageArgs<P> make_args(afar_solver* s) {
   return a;
 }
 
-// Device slot size of one StageArgs (any policy).
-constexpr size_t kArgsSlot =
-    (std::max({sizeof(StageArgs<PolicyRef>), sizeof(StageArgs<PolicyFP64>), sizeof(StageArgs<PolicyMixed>)}) + 255) /
-    256 * 256;
-
-// Copies a solver's StageArgs into its device slot (read by the kb_* kernels).  Not during capture.
-template <class P>
-afar_status upload_args(afar_solver* s, int slot, const StageArgs<P>& a) {
-  void* dst = static_cast<char*>(s->args) + slot * kArgsSlot;
-  AFAR_CUDA(cudaMemcpyAsync(dst, &a, sizeof(a), cudaMemcpyHostToDevice, s->stream));
-  AFAR_CUDA(cudaStreamSynchronize(s->stream));
-  return AFAR_OK;
-}
-
 // cudaFuncAttributeMaxDynamicSharedMemorySize of a staged reconstruct kernel only grows (per
 // device), so solvers and batches of different stencil sizes never lower one another's limit.
 template <class K>
@@ -260,36 +245,26 @@ size_t recon_smem(const afar_solver* s) {
   return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
 }
 
-// One solve's stage launches.  The ref policy passes its arguments by value (k_*); fp64/mixed run
-// the batched kernels (kb_*) on the solver's one-entry device table, so one solve executes the
-// same code alone and inside a batch.
+// One solve's stage launches, arguments by value.  The ref policy reconstructs in the staged
+// kernel and runs the reference-layout flux; fp64 reconstructs staged, mixed in registers.
 template <class P>
 struct Stage {
   afar_solver* s;
-  StageArgs<P> a;          // host copy (ref policy)
-  const StageArgs<P>* da;  // device copy (fp64/mixed)
-  static constexpr bool kByValue = P::id == PolicyRef::id;
+  StageArgs<P> a;
   int gc() const { return grid_for(s->Nc, kCellBlock); }
 
   void reconstruct() const {
-    if constexpr (kByValue)
+    if constexpr (P::id == PolicyMixed::id)
+      k_reconstruct<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
+    else
       k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
-    else if constexpr (P::id == PolicyMixed::id)
-      kb_reconstruct<P><<<gc(), kCellBlock, 0, s->stream>>>(da, nullptr);
-    else
-      kb_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(da, nullptr);
   }
-  void bvd() const {
-    if constexpr (kByValue)
-      k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
-    else
-      kb_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(da, nullptr);
-  }
+  void bvd() const { k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a); }
   // The face flux.  The ref policy runs the reference-layout kernel (its fused multiply-adds then
   // fall where the reference's do) and, on the first stage, the CFL step as a kernel of its own
   // like the reference's setDeltaT; the other policies fuse the CFL reduction into the flux.
   void flux(bool dt_stage) const {
-    if constexpr (kByValue) {
+    if constexpr (P::id == PolicyRef::id) {
       if (dt_stage && s->Nf > 0)
         k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
       const int gr = grid_for(std::max(s->Nf, s->Nb), 128);
@@ -302,28 +277,22 @@ struct Stage {
     } else {
       const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
       if (dt_stage)
-        kb_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(da, nullptr);
+        k_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(a);
       else
-        kb_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(da, nullptr);
+        k_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(a);
     }
   }
   void update(int k) const {
-    if constexpr (kByValue)
-      k_update<P><<<gc(), kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
-    else
-      kb_update<P><<<gc(), kCellBlock, 0, s->stream>>>(da, nullptr, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+    k_update<P><<<gc(), kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
   }
 };
 
-// Stage launcher of a solver; debug = true writes the residual copy (afar_stage_debug).
+// Stage launcher of a solver; debug = true also writes the residual copy (afar_stage_debug).
 template <class P>
 afar_status make_stage(afar_solver* s, bool debug, Stage<P>* out) {
   out->s = s;
   out->a = make_args<P>(s);
   if (debug) out->a.res_dbg = s->res_dbg;
-  const int slot = debug ? 1 : 0;
-  out->da = reinterpret_cast<const StageArgs<P>*>(static_cast<char*>(s->args) + slot * kArgsSlot);
-  if constexpr (!Stage<P>::kByValue) return upload_args<P>(s, slot, out->a);
   return AFAR_OK;
 }
 
@@ -390,8 +359,8 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaFree(fxy));
   AFAR_CUDA(cudaFree(fsr));
-  if constexpr (P::id == PolicyRef::id) return raise_smem_limit(k_reconstruct_staged<P>, s->device, recon_smem<P>(s));
-  if constexpr (P::id == PolicyFP64::id) return raise_smem_limit(kb_reconstruct_staged<P>, s->device, recon_smem<P>(s));
+  if constexpr (P::id != PolicyMixed::id)
+    return raise_smem_limit(k_reconstruct_staged<P>, s->device, recon_smem<P>(s));
   return AFAR_OK;
 }
 
@@ -678,7 +647,6 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
   }
   if (st) return st;
   if ((st = dalloc_t(s, &s->res_dbg, (size_t)Nc))) return st;
-  if ((st = dalloc(s, &s->args, 2 * kArgsSlot))) return st;
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   s->have_stencil = true;
   return AFAR_OK;
@@ -1125,7 +1093,7 @@ struct afar_batch {
   std::vector<afar_solver*> members;
   void* tab = nullptr;  // StageArgs<P>[members]
   size_t tab_bytes = 0;
-  int2* cmap = nullptr;  // per cell block: (member, block within member)
+  int2* cmap = nullptr;  // per cell block: (member, block within the member)
   int2* fmap = nullptr;  // per face block
   size_t cmap_n = 0, fmap_n = 0;
   int ncb = 0, nfb = 0;
@@ -1141,6 +1109,7 @@ afar_status batch_build(afar_batch* b) {
   std::vector<StageArgs<P>> tab;
   std::vector<int2> cm, fm;
   size_t smem = 0;
+  afar_status st;
   for (size_t i = 0; i < b->members.size(); ++i) {
     afar_solver* s = b->members[i];
     tab.push_back(make_args<P>(s));
@@ -1158,7 +1127,6 @@ afar_status batch_build(afar_batch* b) {
     }
     return AFAR_OK;
   };
-  afar_status st;
   size_t cap_c = b->cmap_n * sizeof(int2), cap_f = b->fmap_n * sizeof(int2);
   if ((st = grow(&b->tab, &b->tab_bytes, std::max<size_t>(1, tab.size()) * sizeof(StageArgs<P>)))) return st;
   if ((st = grow(reinterpret_cast<void**>(&b->cmap), &cap_c, std::max<size_t>(1, cm.size()) * sizeof(int2)))) return st;

@@ -289,10 +289,13 @@ afar_status afar_set_step_params(afar_solver* solver, double deltaT, double CFL,
 /* A batch steps all of its member solvers with one launch per stage kernel (13 per RK3 step,
  * replayed as one CUDA graph): every block works on one member, so meshes of uneven size share the
  * GPU without padding.  Each member keeps its own device data, time step (fixed or CFL, with its
- * own step params), end time and step count, and its result is bitwise the same as when it is run
- * alone.  Members join and leave between runs without moving their data.  Policies fp64 and mixed;
- * all members of a batch share the batch's policy and device.  A member must not be stepped on its
- * own while it belongs to a batch. */
+ * own step params), end time and step count.  A member's result does not depend on which other
+ * solves share its batch (bitwise); it agrees with afar_run of the same solve to the policy's
+ * rounding (the batched kernels read their arguments from a device table, afar_run's from kernel
+ * parameters, and the compiler may fuse a multiply-add differently in the two).  Members join and
+ * leave between runs without moving their data.  Policies fp64 and mixed; all members of a batch
+ * share the batch's policy and device; a solver belongs to at most one batch at a time and must
+ * not be stepped on its own while it belongs to one.  Not thread-safe: one host thread per batch. */
 typedef struct afar_batch afar_batch;
 afar_status afar_batch_create(afar_batch** batch, int policy, int device);
 afar_status afar_batch_add(afar_batch* batch, afar_solver* solver);
