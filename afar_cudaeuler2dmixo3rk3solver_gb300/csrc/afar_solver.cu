@@ -141,6 +141,7 @@ struct afar_solver {
   V2<double>* dtg = nullptr;
   V2<double>* bn = nullptr;
   V4<double>* res_dbg = nullptr;
+  afar_batch* batch = nullptr;  // the batch this solver belongs to, if any
   StepCtl* ctl = nullptr;
   unsigned long long* dt_bits = nullptr;
   // policy-typed device arrays (element size depends on the policy)
@@ -407,6 +408,15 @@ afar_status check_ready(afar_solver* s) {
     return AFAR_ERR_STATE;
   }
   AFAR_CUDA(cudaSetDevice(s->device));
+  return AFAR_OK;
+}
+
+// Stepping a batch member on its own would race with (and desynchronise) the batch.
+afar_status check_not_batched(afar_solver* s) {
+  if (s->batch) {
+    set_error("the solver belongs to a batch: step it with afar_batch_run or remove it first");
+    return AFAR_ERR_STATE;
+  }
   return AFAR_OK;
 }
 
@@ -713,7 +723,7 @@ extern "C" afar_status afar_adjustTimeStep(afar_solver* s, int facesNum, double 
 
 static afar_status run_impl(afar_solver* s, int nSteps, double dt, double CFL, double tEnd, bool wait) {
   afar_status st = check_ready(s);
-  if (st) return st;
+  if (st || (st = check_not_batched(s))) return st;
   if (nSteps < 0 || (!(dt > 0.0) && !(CFL > 0.0))) {
     set_error("afar_run: nSteps must be >= 0 and either deltaT > 0 or CFL > 0");
     return AFAR_ERR_ARGUMENT;
@@ -765,7 +775,7 @@ extern "C" afar_status afar_run_async(afar_solver* s, int nSteps, double deltaT,
 
 extern "C" afar_status afar_run_timed(afar_solver* s, int nSteps, double dt, double CFL, double tEnd, float* ms) {
   afar_status st = check_ready(s);
-  if (st) return st;
+  if (st || (st = check_not_batched(s))) return st;
   if (!ms) return (set_error("null output"), AFAR_ERR_ARGUMENT);
   if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
   if ((st = ensure_graph(s, s->R, s->Cv))) return st;
@@ -786,7 +796,7 @@ extern "C" afar_status afar_run_timed(afar_solver* s, int nSteps, double dt, dou
 
 extern "C" afar_status afar_profile_step(afar_solver* s, double dt, double CFL, float ms[5]) {
   afar_status st = check_ready(s);
-  if (st) return st;
+  if (st || (st = check_not_batched(s))) return st;
   if (!ms) return (set_error("null output"), AFAR_ERR_ARGUMENT);
   if (!(s->R > 0.0)) return (set_error("call afar_set_gas (or afar_GPUevolve) first"), AFAR_ERR_STATE);
   cudaEvent_t ev[32];
@@ -872,7 +882,7 @@ extern "C" afar_status afar_set_time(afar_solver* s, double t) {
 
 extern "C" afar_status afar_stage_debug(afar_solver* s, int stage, double deltaT, afar_fieldPointer* out) {
   afar_status st = check_ready(s);
-  if (st) return st;
+  if (st || (st = check_not_batched(s))) return st;
   if (stage < 0 || stage > 2 || !(deltaT > 0.0) || !out) {
     set_error("afar_stage_debug: stage must be 0..2, deltaT > 0, out non-null");
     return AFAR_ERR_ARGUMENT;
@@ -1064,6 +1074,7 @@ extern "C" int afar_launches_per_step(afar_solver* s) { return s && s->policy ==
 
 extern "C" afar_status afar_freeFieldData(afar_solver* s) {
   if (!s) return AFAR_OK;
+  if (s->batch) afar_batch_remove(s->batch, s);  // the batch forgets a freed member
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->graph) cudaGraphExecDestroy(s->graph);
@@ -1212,10 +1223,10 @@ extern "C" afar_status afar_batch_add(afar_batch* b, afar_solver* s) {
   if (!(s->R > 0.0)) return (set_error("afar_batch_add: call afar_set_gas on the member first"), AFAR_ERR_STATE);
   if (!s->have_stencil)
     return (set_error("afar_batch_add: upload the stencil (afar_setDeviceFieldDataStencil) first"), AFAR_ERR_STATE);
-  for (afar_solver* m : b->members)
-    if (m == s) return (set_error("afar_batch_add: already a member"), AFAR_ERR_STATE);
+  if (s->batch) return (set_error("afar_batch_add: the solver already belongs to a batch"), AFAR_ERR_STATE);
   AFAR_CUDA(cudaStreamSynchronize(s->stream));  // no pending work of the member on its own stream
   b->members.push_back(s);
+  s->batch = b;
   b->dirty = true;
   return AFAR_OK;
 }
@@ -1227,6 +1238,7 @@ extern "C" afar_status afar_batch_remove(afar_batch* b, afar_solver* s) {
       AFAR_CUDA(cudaSetDevice(b->device));
       AFAR_CUDA(cudaStreamSynchronize(b->stream));
       b->members.erase(b->members.begin() + i);
+      s->batch = nullptr;
       b->dirty = true;
       return AFAR_OK;
     }
@@ -1268,6 +1280,7 @@ extern "C" afar_status afar_batch_destroy(afar_batch* b) {
   if (!b) return AFAR_OK;
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (afar_solver* m : b->members) m->batch = nullptr;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->tab) cudaFree(b->tab);
   if (b->cmap) cudaFree(b->cmap);

@@ -404,3 +404,42 @@ def vortex_fields(xy, strength=5.0, xc=5.0, yc=5.0, u0=1.0, v0=1.0, R=R_GAS, gam
     p = rho ** gamma
     T = p / (R * rho)
     return np.stack([p, u, v, T], axis=1)
+
+
+# Isentropic vortex workload.  The reference has no periodic patch type, so the vortex travels in
+# a box wide enough that its perturbation at the outlet (label 4) boundary stays below 1e-10.
+VORTEX_BOX = (-7.0, 9.0)  # square [-7, 9]^2; the vortex starts at (0, 0) and moves with (1, 1)
+
+
+def vortex_box(n, renumber=True):
+    """n x n quads on the vortex box, outlet (label 4) on every side."""
+    lo, hi = VORTEX_BOX
+    return quad_grid(n, n, lo, hi, lo, hi, renumber=renumber)
+
+
+def conserved_from_primitive(W, R=R_GAS, Cv=CV_GAS):
+    """(p, Ux, Uy, T) -> (rho, rho Ux, rho Uy, rho E) with E = Cv T + |U|^2 / 2."""
+    p, u, v, T = W[:, 0], W[:, 1], W[:, 2], W[:, 3]
+    rho = p / (R * T)
+    return np.stack([rho, rho * u, rho * v, rho * (Cv * T + 0.5 * (u * u + v * v))], axis=1)
+
+
+def primitive_from_conserved(U, R=R_GAS, Cv=CV_GAS):
+    rho = U[:, 0]
+    u = U[:, 1] / rho
+    v = U[:, 2] / rho
+    T = (U[:, 3] / rho - 0.5 * (u * u + v * v)) / Cv
+    return np.stack([rho * R * T, u, v, T], axis=1)
+
+
+def vortex_cell_averages(mesh: FoamMesh, quadrature, t, strength=5.0, R=R_GAS, gamma=GAMMA):
+    """Cell averages of the conserved variables of the exact solution at time t (the vortex centre
+    at (t, t)), from Gauss points/weights (offsets, points, weights over cells first)."""
+    off, pts, w = quadrature
+    nc = mesh.n_cells
+    npts = int(off[nc])
+    W = vortex_fields(pts[:npts], strength=strength, xc=t, yc=t, R=R, gamma=gamma)
+    U = conserved_from_primitive(W, R=R, Cv=R / (gamma - 1.0)) * w[:npts, None]
+    sums = np.add.reduceat(U, off[:nc], axis=0)
+    wsum = np.add.reduceat(w[:npts], off[:nc])
+    return sums / wsum[:, None]

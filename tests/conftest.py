@@ -71,3 +71,47 @@ def rel_err(a, b):
     scale = np.maximum(np.abs(b), bmax * 1e-3 + 1e-300)
     d = np.where(same, 0.0, np.abs(a - b) / scale)
     return float(np.nanmax(np.where(np.isnan(d), np.inf, d)))
+
+
+VORTEX_T_END = 2.0
+
+
+def vortex_case(n, cfg, want_rbf64=False):
+    """The isentropic vortex on n x n quads of the [-7, 9]^2 box: mesh, Gauss rules, initial cell
+    averages (conserved U0, primitive W0), boundary ghosts Wb and the precomputed host fields."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import gauss_quadrature, precompute
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import mesh as M
+
+    m = M.vortex_box(n)
+    quad = gauss_quadrature(m, cfg)
+    U0 = M.vortex_cell_averages(m, quad, 0.0)
+    W0 = M.primitive_from_conserved(U0)
+    Wb = M.vortex_fields(m.boundary_face_centres(), xc=0.0, yc=0.0)
+    hf = precompute(m, cfg, W0, Wb, want_rbf64=want_rbf64)
+    return m, quad, U0, W0, Wb, hf
+
+
+def vortex_l1(m, quad, rho, t=VORTEX_T_END):
+    """Area-weighted L1 error of the density cell averages against the exact solution at t."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import mesh as M
+
+    exact = M.vortex_cell_averages(m, quad, t)[:, 0]
+    area = m.cell_areas()
+    return float(np.sum(np.abs(rho - exact) * area) / np.sum(area))
+
+
+def oracle_vortex(n, cfg, policy="fp64"):
+    """The CPU oracle's run of the vortex to VORTEX_T_END: (final state, steps, L1 error)."""
+    from oracle.oracle import Oracle
+
+    m, quad, U0, W0, Wb, hf = vortex_case(n, cfg, want_rbf64=policy == "fp64")
+    o = Oracle(hf, cfg.R, cfg.Cv, policy)
+    st = {"FD": np.concatenate([W0, Wb]), "cFD": U0.copy(), "cFDold": U0.copy(),
+          "si": np.zeros(2 * (hf.nc + hf.nb), dtype=np.int8)}
+    t, steps = 0.0, 0
+    while t < VORTEX_T_END:
+        dt = min(o.delta_t(st["FD"], cfg.CFL), VORTEX_T_END - t)
+        o.evolve(st, dt)
+        t += dt
+        steps += 1
+    return st, steps, vortex_l1(m, quad, st["cFD"][:, 0])

@@ -174,4 +174,21 @@ def test_batch_rejects_bad_members(cases):
     assert e.value.status == 5
     with pytest.raises(AfarError):
         batch.remove(f)
+    with pytest.raises(AfarError) as e:
+        m.run(1)  # a member is stepped by its batch only
+    assert e.value.status == 5
+    other = Batch("mixed")
+    with pytest.raises(AfarError) as e:
+        other.add(m)  # one batch at a time
+    assert e.value.status == 5
+    m2 = _make(cases, "mixed_riemann", "mixed")
+    batch.add(m2)
+    assert len(batch) == 2
+    batch.members.remove(m2)
+    m2.close()  # freeing a member takes it out of its batch
+    assert len(batch) == 1
+    assert batch.run(1) > 0.0
+    batch.remove(m)
+    m.run(1)  # stepping alone again after leaving
+    other.close()
     batch.close()
