@@ -52,6 +52,7 @@ struct StageArgs {
   const uint8_t* btype;       // Nb cudaEulerBCs label
   const double* vol;          // Nc
   const double* vinv;         // Nc 1/V (policies without the reference's divisions)
+  const float* vinvf;         // Nc 1/V as float (mixed)
   const uint8_t* nS;          // Nc stencil size
   const uint8_t* nM;          // Nc faces per cell (compact stencil size)
   const int* sten;            // [maxS][ldc]
@@ -62,8 +63,8 @@ struct StageArgs {
   const S* wts;               // [maxM*(maxS+1)][ldc]
   // state and stage intermediates
   V4<typename P::W>* W;       // Nc+Nb
-  V4<double>* U;              // Nc
-  V4<double>* U0;             // Nc
+  V4<double>* U;              // Nc conserved state (mixed: DF4 float pairs, same 32 bytes)
+  V4<double>* U0;             // Nc state at the start of the step (mixed: DF4)
   V4<G>* grad;                // 2Nc
   V4<S>* lim;                 // Nc
   int8_t* si;                 // 2(Nc+Nb): [2c] troubled-cell flag, [2c+1] final switch type
@@ -72,6 +73,7 @@ struct StageArgs {
   StepCtl* ctl;
   V4<double>* res_dbg;        // optional residual dump (parity hook)
   double R, Cv, invR, gamma;
+  float gm1f, invRf;  // gamma - 1 and 1/R as floats (mixed)
 };
 
 // limiterProcess (reference cudaLimiter.h:35-50)
@@ -884,14 +886,13 @@ __device__ __forceinline__ void two_sum(float& s, float& e, const float a, const
   e = (a - (s - bp)) + (b - bp);
 }
 
-// The mixed policy's gather + update.  FP64 is kept where accumulation needs it and nowhere else:
-// the residual of the float fluxes is summed error-free as a float pair, the RK combine of the
-// conserved state is FP64, and the pressure is the FP64 difference rhoE - |rhoU|^2/(2 rho) with
-// 1/rho from a float reciprocal refined by one FP64 Newton step (relative error ~1e-14) instead of
-// an FP64 division (a long sequence on GB300's FP64 pipe).
+// The mixed policy's gather + update, with no FP64 arithmetic on the path (GB300's FP64 pipe is
+// 1/53 of FP32): the residual of the float fluxes is summed error-free as a float pair, the
+// conserved state U, Un is stored and combined as float pairs (DF4, ~48 bits), and the pressure is
+// the float-pair difference rhoE - |rhoU|^2/(2 rho) (the cancellation at high Mach costs no
+// precision), rounded once to float.  k = {beta3*dt, beta1 (hi, lo), beta2 (hi, lo)} of the stage.
 template <class P>
-__device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c, const double deltaT,
-                                             const double beta1, const double beta2, const double beta3,
+__device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c, const float* k, const bool first,
                                              const int last_stage) {
   const int ldc = a.ldc;
   const int nM = a.nM[c];
@@ -910,41 +911,39 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
         const float sgn = fid[u] > 0 ? 1.f : -1.f;
         const float x[4] = {sgn * fl[u].x, sgn * fl[u].y, sgn * fl[u].z, sgn * fl[u].w};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          float s, e;
-          two_sum(s, e, hi[k], x[k]);
-          hi[k] = s;
-          lo[k] += e;
+        for (int q = 0; q < 4; ++q) {
+          const DF t = df_two_sum(hi[q], x[q]);
+          hi[q] = t.hi;
+          lo[q] = __fadd_rn(lo[q], t.lo);
         }
       }
     }
   }
   if (a.res_dbg) a.res_dbg[c] = V4<double>{(double)hi[0] + lo[0], (double)hi[1] + lo[1], (double)hi[2] + lo[2],
                                           (double)hi[3] + lo[3]};
-  const float s3 = (float)(-beta3 * deltaT * a.vinv[c]);
-  const V4<double> o = a.U0[c];
-  V4<double> base;
-  if (beta2 == 0.0 && beta1 == 1.0) {  // first RK stage: U = Un + increment, U itself not read
-    base = o;
-  } else {
-    const V4<double> u = a.U[c];
-    base = V4<double>{fma(beta2, u.x, beta1 * o.x), fma(beta2, u.y, beta1 * o.y), fma(beta2, u.z, beta1 * o.z),
-                      fma(beta2, u.w, beta1 * o.w)};
+  const float s3 = -k[0] * a.vinvf[c];
+  DF4* const U = reinterpret_cast<DF4*>(a.U);
+  DF4* const U0 = reinterpret_cast<DF4*>(a.U0);
+  const DF4 o = U0[c];
+  DF base[4] = {{o.hi.x, o.lo.x}, {o.hi.y, o.lo.y}, {o.hi.z, o.lo.z}, {o.hi.w, o.lo.w}};
+  if (!first) {  // stages 2, 3: beta1 Un + beta2 U (stage 1 is Un + increment, U not read)
+    const DF4 u = U[c];
+    const DF b1{k[1], k[2]}, b2{k[3], k[4]};
+    const DF uu[4] = {{u.hi.x, u.lo.x}, {u.hi.y, u.lo.y}, {u.hi.z, u.lo.z}, {u.hi.w, u.lo.w}};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) base[q] = df_add(df_mul(b1, base[q]), df_mul(b2, uu[q]));
   }
-  const double rho = base.x + (double)(s3 * (hi[0] + lo[0]));
-  const double rhoUx = base.y + (double)(s3 * (hi[1] + lo[1]));
-  const double rhoUy = base.z + (double)(s3 * (hi[2] + lo[2]));
-  const double rhoE = base.w + (double)(s3 * (hi[3] + lo[3]));
-  const V4<double> un{rho, rhoUx, rhoUy, rhoE};
-  a.U[c] = un;
-  if (last_stage) a.U0[c] = un;
-  const float irf = __frcp_rn((float)rho);
-  double ir = (double)irf;
-  ir = ir * fma(-rho, ir, 2.0);
-  const double gamma = a.gamma;  // R/Cv + 1, computed once on the host like GPUevolve.cu:222
-  const double p = (gamma - 1.0) * fma(-0.5 * ir, fma(rhoUx, rhoUx, rhoUy * rhoUy), rhoE);
-  const float pf = (float)p;
-  const V4<float> wn{pf, (float)rhoUx * irf, (float)rhoUy * irf, pf * irf * (float)a.invR};
+  DF un[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) un[q] = df_add(base[q], __fmul_rn(s3, __fadd_rn(hi[q], lo[q])));
+  const DF4 st{{un[0].hi, un[1].hi, un[2].hi, un[3].hi}, {un[0].lo, un[1].lo, un[2].lo, un[3].lo}};
+  U[c] = st;
+  if (last_stage) U0[c] = st;
+  const float irf = __frcp_rn(un[0].hi);
+  const DF ke2 = df_div(df_add(df_sqr(un[1]), df_sqr(un[2])), un[0], irf);  // |rhoU|^2 / rho
+  const DF e = df_add(un[3], DF{-0.5f * ke2.hi, -0.5f * ke2.lo});
+  const float pf = a.gm1f * __fadd_rn(e.hi, e.lo);
+  const V4<float> wn{pf, un[1].hi * irf, un[2].hi * irf, pf * irf * a.invRf};
   reinterpret_cast<V4<float>*>(a.W)[c] = wn;
   for (int fi = 0; fi < nM; ++fi) {
     const int f = abs(a.cf[fi * ldc + c]) - 1;
@@ -964,7 +963,17 @@ template <class P>
 __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk, const double beta1,
                                             const double beta2, const double beta3, const int last_stage) {
   __shared__ double s_dt;  // the step size, read once per block (a block never spans two solves)
-  if (threadIdx.x == 0) s_dt = step_dt(a.ctl);
+  __shared__ float s_k[5];  // mixed: beta3*dt and the float-pair betas, split once per block
+  if (threadIdx.x == 0) {
+    s_dt = step_dt(a.ctl);
+    if constexpr (P::id == PolicyMixed::id) {
+      s_k[0] = (float)(beta3 * s_dt);
+      s_k[1] = (float)beta1;
+      s_k[2] = (float)(beta1 - (double)s_k[1]);
+      s_k[3] = (float)beta2;
+      s_k[4] = (float)(beta2 - (double)s_k[3]);
+    }
+  }
   __syncthreads();
   const double deltaT = s_dt;
   const int c = blk * blockDim.x + threadIdx.x;
@@ -973,7 +982,7 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
   const int ldc = a.ldc;
   const int nM = a.nM[c];
   if constexpr (P::id == PolicyMixed::id) {
-    update_mixed(a, c, deltaT, beta1, beta2, beta3, last_stage);
+    update_mixed(a, c, s_k, beta2 == 0.0 && beta1 == 1.0, last_stage);
     return;
   }
   double Rrho = 0.0, RrhoUx = 0.0, RrhoUy = 0.0, RrhoE = 0.0;

@@ -107,4 +107,61 @@ __device__ __forceinline__ auto pick(bool c1, bool c2, A a, B b) -> decltype(a *
   }
 }
 
+// ---------------------------------------------------------------- float-pair ("double-float") values
+// A value hi + lo with |lo| <= ulp(hi)/2 (about 48 significant bits) built from FP32 operations
+// only, for the mixed policy's conserved state: GB300's FP64 pipe runs at 1/53 of FP32.  The
+// error-free transformations are Knuth's two-sum, Dekker's fast two-sum (|a| >= |b|) and the
+// FMA two-product; the explicitly rounded __fadd_rn/__fmul_rn keep the compiler from fusing a
+// product into a later sum, which would break the transformations.
+struct DF {
+  float hi, lo;
+};
+// The conserved state of one cell as float pairs: 32 bytes, like V4<double>.
+struct alignas(16) DF4 {
+  V4<float> hi, lo;
+};
+
+__device__ __forceinline__ DF df_two_sum(const float a, const float b) {
+  const float s = __fadd_rn(a, b);
+  const float bp = __fadd_rn(s, -a);
+  return DF{s, __fadd_rn(__fadd_rn(a, -__fadd_rn(s, -bp)), __fadd_rn(b, -bp))};
+}
+__device__ __forceinline__ DF df_fast_two_sum(const float a, const float b) {
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fadd_rn(b, -__fadd_rn(s, -a))};
+}
+// a + b, both float pairs (the accurate sum: two-sums of both parts).
+__device__ __forceinline__ DF df_add(const DF a, const DF b) {
+  DF s = df_two_sum(a.hi, b.hi);
+  const DF t = df_two_sum(a.lo, b.lo);
+  s = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.lo));
+}
+// a + b, b a float.
+__device__ __forceinline__ DF df_add(const DF a, const float b) {
+  const DF s = df_two_sum(a.hi, b);
+  return df_fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+// a * b.
+__device__ __forceinline__ DF df_mul(const DF a, const DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+// a * a.
+__device__ __forceinline__ DF df_sqr(const DF a) {
+  const float p = __fmul_rn(a.hi, a.hi);
+  const float e = __fmaf_rn(__fmul_rn(2.f, a.hi), a.lo, __fmaf_rn(a.hi, a.hi, -p));
+  return df_fast_two_sum(p, e);
+}
+// a / b given r ~ 1/b.hi: one correction of the float quotient, q = q0 + (a - q0 b) r.
+__device__ __forceinline__ DF df_div(const DF a, const DF b, const float r) {
+  const float q0 = __fmul_rn(a.hi, r);
+  const DF qb = df_mul(DF{q0, 0.f}, b);
+  const DF rem = df_add(a, DF{-qb.hi, -qb.lo});
+  return df_fast_two_sum(q0, __fmul_rn(__fadd_rn(rem.hi, rem.lo), r));
+}
+
 }  // namespace afar

@@ -100,9 +100,32 @@ __global__ void k_init_ctl(StepCtl* ctl) {
   }
 }
 
-__global__ void k_reciprocal(int n, const double* in, double* out) {
+__global__ void k_reciprocal(int n, const double* in, double* out, float* outf) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = 1.0 / in[i];
+  if (i < n) {
+    out[i] = 1.0 / in[i];
+    if (outf) outf[i] = (float)(1.0 / in[i]);
+  }
+}
+
+// The mixed policy's conserved state: double -> float pair in place (each thread rewrites its own
+// 32 bytes), and float pair -> double.
+__global__ void k_df_from_double(int n, V4<double>* u) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const V4<double> v = u[i];
+  DF4 d;
+  d.hi = V4<float>{(float)v.x, (float)v.y, (float)v.z, (float)v.w};
+  d.lo = V4<float>{(float)(v.x - (double)d.hi.x), (float)(v.y - (double)d.hi.y), (float)(v.z - (double)d.hi.z),
+                   (float)(v.w - (double)d.hi.w)};
+  reinterpret_cast<DF4*>(u)[i] = d;
+}
+__global__ void k_df_to_double(int n, const DF4* in, V4<double>* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DF4 d = in[i];
+  out[i] = V4<double>{(double)d.hi.x + (double)d.lo.x, (double)d.hi.y + (double)d.lo.y,
+                      (double)d.hi.z + (double)d.lo.z, (double)d.hi.w + (double)d.lo.w};
 }
 
 template <class A, class B>
@@ -128,6 +151,8 @@ struct afar_solver {
   FaceRaw* faceRaw = nullptr;
   double* vol = nullptr;
   double* vinv = nullptr;
+  float* vinvf = nullptr;  // mixed: 1/V as float
+  void* xfer = nullptr;    // mixed: staging for double <-> device-format copies, 32 B x (Nc + Nb)
   int2* on = nullptr;
   int* bnei = nullptr;
   uint8_t* btype = nullptr;
@@ -220,6 +245,9 @@ StageArgs<P> make_args(afar_solver* s) {
   a.Cv = s->Cv;
   a.invR = s->R > 0.0 ? 1.0 / s->R : 0.0;
   a.gamma = s->Cv > 0.0 ? s->R / s->Cv + 1.0 : 0.0;
+  a.gm1f = (float)(a.gamma - 1.0);
+  a.invRf = (float)a.invR;
+  a.vinvf = s->vinvf;
   return a;
 }
 
@@ -450,6 +478,62 @@ extern "C" afar_status afar_solver_create(afar_solver** out, int policy, int dev
   return AFAR_OK;
 }
 
+// Host <-> device state in the reference's double layout, ordered on the solver's stream.  The
+// mixed policy keeps W as float and U, Un as float pairs: the doubles are staged in `xfer` and
+// converted on the device.
+static afar_status put_state(afar_solver* s, const afar_basicFieldData* FD, const afar_conservedFieldData* cFD,
+                      const afar_conservedFieldData* cFDold) {
+  const size_t Nc = s->Nc, Nb = s->Nb;
+  const bool mixed = s->policy == AFAR_POLICY_MIXED;
+  if (FD) {
+    if (mixed) {
+      AFAR_CUDA(cudaMemcpyAsync(s->xfer, FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
+      k_convert4<double, float><<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>(
+          (int)(Nc + Nb), static_cast<const V4<double>*>(s->xfer), static_cast<V4<float>*>(s->W));
+    } else {
+      AFAR_CUDA(cudaMemcpyAsync(s->W, FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
+    }
+  }
+  const afar_conservedFieldData* src[2] = {cFD, cFDold};
+  V4<double>* dst[2] = {s->U, s->U0};
+  for (int i = 0; i < 2; ++i) {
+    if (!src[i]) continue;
+    AFAR_CUDA(cudaMemcpyAsync(dst[i], src[i], sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
+    if (mixed) k_df_from_double<<<grid_for(Nc, 256), 256, 0, s->stream>>>((int)Nc, dst[i]);
+  }
+  AFAR_CUDA(cudaGetLastError());
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  return AFAR_OK;
+}
+
+static afar_status get_state(afar_solver* s, afar_basicFieldData* FD, afar_conservedFieldData* cFD, int8_t* si) {
+  const size_t Nc = s->Nc, Nb = s->Nb;
+  const bool mixed = s->policy == AFAR_POLICY_MIXED;
+  if (FD) {
+    if (mixed) {
+      k_convert4<float, double><<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>(
+          (int)(Nc + Nb), static_cast<const V4<float>*>(s->W), static_cast<V4<double>*>(s->xfer));
+      AFAR_CUDA(cudaMemcpyAsync(FD, s->xfer, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyDeviceToHost, s->stream));
+      AFAR_CUDA(cudaStreamSynchronize(s->stream));  // xfer is reused below
+    } else {
+      AFAR_CUDA(cudaMemcpyAsync(FD, s->W, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyDeviceToHost, s->stream));
+    }
+  }
+  if (cFD) {
+    if (mixed) {
+      k_df_to_double<<<grid_for(Nc, 256), 256, 0, s->stream>>>((int)Nc, reinterpret_cast<const DF4*>(s->U),
+                                                               static_cast<V4<double>*>(s->xfer));
+      AFAR_CUDA(cudaMemcpyAsync(cFD, s->xfer, sizeof(V4<double>) * Nc, cudaMemcpyDeviceToHost, s->stream));
+    } else {
+      AFAR_CUDA(cudaMemcpyAsync(cFD, s->U, sizeof(V4<double>) * Nc, cudaMemcpyDeviceToHost, s->stream));
+    }
+  }
+  if (si) AFAR_CUDA(cudaMemcpyAsync(si, s->si, 2 * (Nc + Nb), cudaMemcpyDeviceToHost, s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  return AFAR_OK;
+}
+
 extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldPointer* h, int cellsNum, int facesNum,
                                                int totalBoundaryFacesNum) {
   if (!s || !h || !h->CELL || !h->FACE || !h->cellVolume || !h->FD || !h->cFD || cellsNum <= 0 || facesNum < 0 ||
@@ -472,6 +556,10 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   if ((st = dalloc_t(s, &s->faceRaw, Nf + Nb))) return st;
   if ((st = dalloc_t(s, &s->vol, Nc))) return st;
   if ((st = dalloc_t(s, &s->vinv, Nc))) return st;
+  if (s->policy == AFAR_POLICY_MIXED) {
+    if ((st = dalloc_t(s, &s->vinvf, Nc))) return st;
+    if ((st = dalloc(s, &s->xfer, sizeof(V4<double>) * (Nc + Nb)))) return st;
+  }
   if ((st = dalloc_t(s, &s->U, Nc))) return st;
   if ((st = dalloc_t(s, &s->U0, Nc))) return st;
   if ((st = dalloc_t(s, &s->si, 2 * (Nc + Nb)))) return st;
@@ -481,21 +569,12 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   AFAR_CUDA(cudaMemcpyAsync(s->cellC, h->CELL, sizeof(V2<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->faceRaw, h->FACE, sizeof(FaceRaw) * (Nf + Nb), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->vol, h->cellVolume, sizeof(double) * Nc, cudaMemcpyHostToDevice, s->stream));
-  k_reciprocal<<<grid_for(Nc, 256), 256, 0, s->stream>>>((int)Nc, s->vol, s->vinv);
-  AFAR_CUDA(cudaMemcpyAsync(s->U, h->cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
-  AFAR_CUDA(cudaMemcpyAsync(s->U0, h->cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
+  k_reciprocal<<<grid_for(Nc, 256), 256, 0, s->stream>>>((int)Nc, s->vol, s->vinv, s->vinvf);
   AFAR_CUDA(cudaMemsetAsync(s->si, 0, 2 * (Nc + Nb), s->stream));
-  if (s->policy == AFAR_POLICY_MIXED) {
-    V4<double>* tmp = nullptr;
-    AFAR_CUDA(cudaMalloc(&tmp, sizeof(V4<double>) * (Nc + Nb)));
-    AFAR_CUDA(cudaMemcpyAsync(tmp, h->FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
-    k_convert4<double, float><<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>((int)(Nc + Nb), tmp,
-                                                                            static_cast<V4<float>*>(s->W));
-    AFAR_CUDA(cudaStreamSynchronize(s->stream));
-    AFAR_CUDA(cudaFree(tmp));
-  } else {
-    AFAR_CUDA(cudaMemcpyAsync(s->W, h->FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
-  }
+  if ((st = put_state(s, reinterpret_cast<const afar_basicFieldData*>(h->FD),
+                      reinterpret_cast<const afar_conservedFieldData*>(h->cFD),
+                      reinterpret_cast<const afar_conservedFieldData*>(h->cFD))))
+    return st;
   k_init_ctl<<<1, 32, 0, s->stream>>>(s->ctl);
   // intermediates
   const size_t g = s->policy == AFAR_POLICY_MIXED ? sizeof(V4<float>) : sizeof(V4<double>);
@@ -927,7 +1006,8 @@ extern "C" afar_status afar_stage_debug(afar_solver* s, int stage, double deltaT
   if (out->gradFD && (st = get4(out->gradFD, s->grad, 2 * Nc, mixed))) return st;
   if (out->Flux && (st = get4(out->Flux, s->flux, Nf + Nb, mixed))) return st;
   if (out->FD && (st = get4(out->FD, s->W, Nc + Nb, mixed))) return st;
-  if (out->cFD) AFAR_CUDA(cudaMemcpy(out->cFD, s->U, Nc * sizeof(V4<double>), cudaMemcpyDeviceToHost));
+  if (out->cFD && (st = get_state(s, nullptr, reinterpret_cast<afar_conservedFieldData*>(out->cFD), nullptr)))
+    return st;
   if (out->Res) AFAR_CUDA(cudaMemcpy(out->Res, s->res_dbg, Nc * sizeof(V4<double>), cudaMemcpyDeviceToHost));
   if (out->shockIndicator) AFAR_CUDA(cudaMemcpy(out->shockIndicator, s->si, 2 * (Nc + Nb), cudaMemcpyDeviceToHost));
   if (out->limiter) {
@@ -962,40 +1042,14 @@ extern "C" afar_status afar_upload_state(afar_solver* s, const afar_basicFieldDa
                                          const afar_conservedFieldData* cFDold) {
   if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
   AFAR_CUDA(cudaSetDevice(s->device));
-  const size_t Nc = s->Nc, Nb = s->Nb;
-  if (FD) {
-    if (s->policy == AFAR_POLICY_MIXED) {
-      std::vector<V4<float>> tmp(Nc + Nb);
-      for (size_t i = 0; i < Nc + Nb; ++i)
-        tmp[i] = V4<float>{(float)FD[i].p, (float)FD[i].Ux, (float)FD[i].Uy, (float)FD[i].T};
-      AFAR_CUDA(cudaMemcpy(s->W, tmp.data(), sizeof(V4<float>) * (Nc + Nb), cudaMemcpyHostToDevice));
-    } else {
-      AFAR_CUDA(cudaMemcpy(s->W, FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice));
-    }
-  }
-  if (cFD) AFAR_CUDA(cudaMemcpy(s->U, cFD, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice));
-  if (cFDold) AFAR_CUDA(cudaMemcpy(s->U0, cFDold, sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice));
-  return AFAR_OK;
+  return put_state(s, FD, cFD, cFDold);
 }
 
 extern "C" afar_status afar_download_state(afar_solver* s, afar_basicFieldData* FD, afar_conservedFieldData* cFD,
                                            int8_t* shockIndicator) {
   if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
   AFAR_CUDA(cudaSetDevice(s->device));
-  AFAR_CUDA(cudaStreamSynchronize(s->stream));
-  const size_t Nc = s->Nc, Nb = s->Nb;
-  if (FD) {
-    if (s->policy == AFAR_POLICY_MIXED) {
-      std::vector<V4<float>> tmp(Nc + Nb);
-      AFAR_CUDA(cudaMemcpy(tmp.data(), s->W, sizeof(V4<float>) * (Nc + Nb), cudaMemcpyDeviceToHost));
-      for (size_t i = 0; i < Nc + Nb; ++i) FD[i] = afar_basicFieldData{tmp[i].x, tmp[i].y, tmp[i].z, tmp[i].w};
-    } else {
-      AFAR_CUDA(cudaMemcpy(FD, s->W, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyDeviceToHost));
-    }
-  }
-  if (cFD) AFAR_CUDA(cudaMemcpy(cFD, s->U, sizeof(V4<double>) * Nc, cudaMemcpyDeviceToHost));
-  if (shockIndicator) AFAR_CUDA(cudaMemcpy(shockIndicator, s->si, 2 * (Nc + Nb), cudaMemcpyDeviceToHost));
-  return AFAR_OK;
+  return get_state(s, FD, cFD, shockIndicator);
 }
 
 extern "C" afar_status afar_copyFieldDataDeviceToHost(afar_fieldPointer* h, afar_solver* s, int cellsNum,

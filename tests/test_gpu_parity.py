@@ -211,3 +211,25 @@ def test_mixed_policy_close_to_fp64(cases, name):
     rb = b.state()["cFD"][:, 0]
     l1 = np.mean(np.abs(ra - rb))
     assert l1 <= 1e-4, l1
+
+
+def test_mixed_state_round_trip(cases):
+    """The mixed policy keeps the conserved state as float pairs: upload -> download of doubles is
+    exact to the pair's ~48 bits, and the primitive state to float."""
+    hf, cfg = cases["quad_riemann"]
+    s = _solver(hf, cfg, "mixed")
+    rng = np.random.default_rng(11)
+    cfd = hf.cFD * (1.0 + 1e-3 * rng.standard_normal(hf.cFD.shape))
+    fd = hf.FD * (1.0 + 1e-3 * rng.standard_normal(hf.FD.shape))
+    s.upload_state(FD=fd, cFD=cfd, cFDold=cfd)
+    out = s.state()
+    assert np.abs(out["cFD"] - cfd).max() <= 2.0 ** -46 * np.abs(cfd).max()
+    assert np.abs(out["FD"] - fd).max() <= 2.0 ** -23 * np.abs(fd).max()
+    s.run(1, dt=1e-5)
+    s.save()
+    s.run(2, dt=1e-5)
+    a = s.state()
+    s.restore()
+    s.run(2, dt=1e-5)
+    b = s.state()
+    assert np.array_equal(a["cFD"], b["cFD"]) and np.array_equal(a["FD"], b["FD"])
