@@ -28,6 +28,7 @@ struct StepCtl {
   double cfl;
   double last_dt;
   long long steps;
+  unsigned err;  // bit 0: a bounded device wait gave up (the stage's results are not valid)
 };
 
 // The step of the current RK step: fixed or CFL, clipped to t_end; <= 0 means "no step".
@@ -94,38 +95,142 @@ __device__ __forceinline__ void limiter_process(S& limiter, S& phif, const S phi
 // (d2GaussQuadrature.C:65-148); the stencil upload rejects larger compact stencils.
 constexpr int kMaxFaces = 4;
 
-// reconstruct (reference cudaLimiter.h:53-316): LS gradient, stencil min/max, raw limiter,
-// O3 RBF face values of this cell's side of each internal face, troubled-cell flag.
-// One pass over the stencil: each member's state is gathered once and feeds the gradient and
-// min/max (compact members) and the O3 sums of every face side at once, all in registers.  The
-// loads of a batch of members (indices, gathers, weights) are issued together, so several are in
-// flight per thread; no shared memory, so occupancy is set by registers alone.  Every sum is
-// still accumulated in stencil order, as in the reference.
+// ---------------------------------------------------------------- mixed reconstruct, tile-staged
+// One CTA per 128-cell tile.  The tile's slice of every per-cell operator row (face ids, LS rows,
+// face offsets, (dr, fraction), stencil ids, O3 weights) and the cells' own states are contiguous
+// 128-element runs of the slot-major arrays, so the CTA fetches them with bulk copies (TMA unit,
+// one mbarrier) instead of per-thread loads: ~50 KB per tile in flight from a handful of lanes,
+// while registers stay free for the stencil gathers, which hit L2.
+constexpr int kTile = 128;
+struct ReconTile {
+  unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_bar, bytes;
+};
+__host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int maxS) {
+  ReconTile L;
+  unsigned o = 0;
+  L.off_cf = o;
+  o += maxM * kTile * 4;
+  L.off_lsm = o;
+  o += maxM * kTile * 8;
+  L.off_sg = o;
+  o += maxM * kTile * 8;
+  L.off_sr = o;
+  o += maxM * kTile * 8;
+  L.off_sten = o;
+  o += maxS * kTile * 4;
+  L.off_wts = o;
+  o += maxM * (maxS + 1) * kTile * 4;
+  L.off_w = o;
+  o += kTile * 16;
+  L.off_bar = o;
+  L.bytes = o + 16;
+  return L;
+}
+
+// Issues the bulk copies of tile `blk` (called by warp 0).  Rows of the slot-major arrays hold
+// ldc elements (a multiple of 32), so every slice is a multiple of 128 bytes and 16-byte aligned;
+// the own-state slice holds the tile's cells (16 bytes each).
 template <class P>
-__device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk) {
+__device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const int blk, const ReconTile& L,
+                                                 unsigned char* sm, unsigned long long* bar) {
+  const int lane = threadIdx.x;
+  const int c0 = blk * kTile;
+  const unsigned ne = (unsigned)min(kTile, a.ldc - c0);  // elements of a row slice
+  const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
+  const int M = a.maxM, S = a.maxS;
+  const int rows = 4 * M + S + M * (S + 1) + 1;
+  const unsigned total = ne * (M * (4 + 8 + 8 + 8) + S * 4 + M * (S + 1) * 4) + nw * 16;
+  if (lane == 0) mbar_arrive_expect_tx(bar, total);
+  __syncwarp();
+  for (int r = lane; r < rows; r += 32) {
+    void* dst;
+    const void* src;
+    unsigned bytes;
+    if (r < M) {
+      dst = sm + L.off_cf + r * kTile * 4;
+      src = a.cf + (size_t)r * a.ldc + c0;
+      bytes = ne * 4;
+    } else if (r < 2 * M) {
+      const int k = r - M;
+      dst = sm + L.off_lsm + k * kTile * 8;
+      src = a.lsm + (size_t)k * a.ldc + c0;
+      bytes = ne * 8;
+    } else if (r < 3 * M) {
+      const int k = r - 2 * M;
+      dst = sm + L.off_sg + k * kTile * 8;
+      src = a.sg + (size_t)k * a.ldc + c0;
+      bytes = ne * 8;
+    } else if (r < 4 * M) {
+      const int k = r - 3 * M;
+      dst = sm + L.off_sr + k * kTile * 8;
+      src = a.sr + (size_t)k * a.ldc + c0;
+      bytes = ne * 8;
+    } else if (r < 4 * M + S) {
+      const int k = r - 4 * M;
+      dst = sm + L.off_sten + k * kTile * 4;
+      src = a.sten + (size_t)k * a.ldc + c0;
+      bytes = ne * 4;
+    } else if (r < rows - 1) {
+      const int k = r - 4 * M - S;
+      dst = sm + L.off_wts + k * kTile * 4;
+      src = a.wts + (size_t)k * a.ldc + c0;
+      bytes = ne * 4;
+    } else {
+      dst = sm + L.off_w;
+      src = a.W + c0;
+      bytes = nw * 16;
+    }
+    bulk_to_smem(dst, src, bytes, bar);
+  }
+}
+
+// reconstruct (reference cudaLimiter.h:53-316) for the mixed policy from the staged tile: LS
+// gradient, stencil min/max, raw limiter, O3 RBF face values of this cell's side of each internal
+// face, troubled-cell flag.  One pass over the stencil: each member's state is gathered once (in
+// batches of 8, all in flight) and feeds the gradient and min/max (compact members) and the O3 sums
+// of every face side; every sum is accumulated in stencil order, as in the reference.  NF: the
+// largest number of faces of a cell (3 on all-triangle meshes, else 4).
+template <class P, int NF>
+__device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int blk, unsigned char* sm) {
   using S = typename P::S;
   using G = typename P::G;
   using WT = typename P::W;
-  const int c = blk * blockDim.x + threadIdx.x;
-  if (c >= a.Nc) return;
-  const int ldc = a.ldc;
-  const int nS = a.nS[c], nM = a.nM[c];
-  const int wrow = a.maxS + 1;
-  int fid[kMaxFaces];
-  bool inner[kMaxFaces];
-  V2<S> lm[kMaxFaces];
-#pragma unroll
-  for (int fi = 0; fi < kMaxFaces; ++fi) {
-    fid[fi] = fi < nM ? a.cf[fi * ldc + c] : 1;
-    inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
-    lm[fi] = fi < nM ? a.lsm[fi * ldc + c] : V2<S>{S(0), S(0)};
+  const ReconTile L = recon_tile_layout(a.maxM, a.maxS);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + L.off_bar);
+  const int t = threadIdx.x;
+  if (t == 0) mbar_init(bar, 1);
+  __syncthreads();
+  if (t < 32) recon_tile_fetch(a, blk, L, sm, bar);
+  const int c = blk * kTile + t;
+  const int nS = c < a.Nc ? a.nS[c] : 0, nM = c < a.Nc ? a.nM[c] : 0;
+  if (!mbar_wait_bounded(bar, 0)) {  // the copies did not land: flag it, give them a last chance, leave
+    if (t == 0) atomicOr(&a.ctl->err, 1u);
+    mbar_wait_bounded(bar, 0);
+    return;
   }
-  const V4<WT> wc = a.W[c];
-  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
-  G acc[kMaxFaces][4];
+  if (c >= a.Nc) return;
+  const int* s_cf = reinterpret_cast<const int*>(sm + L.off_cf);
+  const V2<S>* s_lsm = reinterpret_cast<const V2<S>*>(sm + L.off_lsm);
+  const V2<G>* s_sg = reinterpret_cast<const V2<G>*>(sm + L.off_sg);
+  const V2<S>* s_sr = reinterpret_cast<const V2<S>*>(sm + L.off_sr);
+  const int* s_sten = reinterpret_cast<const int*>(sm + L.off_sten);
+  const S* s_wts = reinterpret_cast<const S*>(sm + L.off_wts);
+  const V4<WT>* s_w = reinterpret_cast<const V4<WT>*>(sm + L.off_w);
+  const int wrow = a.maxS + 1;
+
+  int fid[NF];
+  bool inner[NF];
 #pragma unroll
-  for (int fi = 0; fi < kMaxFaces; ++fi) {  // each face side's O3 sum starts with the cell's own term
-    const S w0 = inner[fi] ? a.wts[(size_t)(fi * wrow) * ldc + c] : S(0);
+  for (int fi = 0; fi < NF; ++fi) {
+    fid[fi] = fi < nM ? s_cf[fi * kTile + t] : 1;
+    inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
+  }
+  const V4<WT> wc = s_w[t];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  G acc[NF][4];
+#pragma unroll
+  for (int fi = 0; fi < NF; ++fi) {  // each face side's O3 sum starts with the cell's own term
+    const S w0 = inner[fi] ? s_wts[(fi * wrow) * kTile + t] : S(0);
     acc[fi][0] = w0 * pc;
     acc[fi][1] = w0 * uxc;
     acc[fi][2] = w0 * uyc;
@@ -133,26 +238,22 @@ __device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk)
   }
   G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
   S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
-  S pn[kMaxFaces];  // pressure of the cell across each face
-  {  // members 0..3: the face neighbours (compact stencil) come first
-    int j[kMaxFaces];
+  S pn[NF];  // pressure of the cell across each face
 #pragma unroll
-    for (int u = 0; u < kMaxFaces; ++u) j[u] = u < nS ? a.sten[u * ldc + c] : c;
-    V4<WT> wj[kMaxFaces];
+  for (int fi = 0; fi < NF; ++fi) pn[fi] = S(0);
+  constexpr int U = 8;
+  for (int ci0 = 0; ci0 < nS; ci0 += U) {
+    V4<WT> wj[U];
 #pragma unroll
-    for (int u = 0; u < kMaxFaces; ++u) wj[u] = a.W[j[u]];
-    S wv[kMaxFaces][kMaxFaces];
+    for (int u = 0; u < U; ++u) wj[u] = a.W[ci0 + u < nS ? s_sten[(ci0 + u) * kTile + t] : c];
 #pragma unroll
-    for (int u = 0; u < kMaxFaces; ++u)
-#pragma unroll
-      for (int fi = 0; fi < kMaxFaces; ++fi)
-        wv[u][fi] = (u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + u + 1) * ldc + c] : S(0);
-#pragma unroll
-    for (int u = 0; u < kMaxFaces; ++u) {
-      if (u < nS) {
+    for (int u = 0; u < U; ++u) {
+      const int ci = ci0 + u;
+      if (ci < nS) {
         const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
-        if (u < nM) {  // reference :148-169 and :190-205
-          const S M1 = lm[u].x, M2 = lm[u].y;
+        if (ci < nM) {  // the face neighbours (compact stencil) come first: reference :148-169, :190-205
+          const V2<S> lm = s_lsm[ci * kTile + t];
+          const S M1 = lm.x, M2 = lm.y;
           S dphi = vx - pc;
           gPx += M1 * dphi;
           gPy += M2 * dphi;
@@ -173,42 +274,17 @@ __device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk)
           uyMin = fmn(vz, uyMin);
           tMax = fmx(vw, tMax);
           tMin = fmn(vw, tMin);
-          pn[u] = vx;
+#pragma unroll
+          for (int fi = 0; fi < NF; ++fi)
+            if (fi == ci) pn[fi] = vx;
         }
 #pragma unroll
-        for (int fi = 0; fi < kMaxFaces; ++fi) {
-          acc[fi][0] += wv[u][fi] * vx;
-          acc[fi][1] += wv[u][fi] * vy;
-          acc[fi][2] += wv[u][fi] * vz;
-          acc[fi][3] += wv[u][fi] * vw;
-        }
-      }
-    }
-  }
-  constexpr int U = sizeof(WT) == 4 ? 4 : 2;
-  for (int ci0 = kMaxFaces; ci0 < nS; ci0 += U) {  // the rest of the stencil: O3 sums only
-    int j[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) j[u] = (ci0 + u < nS) ? a.sten[(ci0 + u) * ldc + c] : c;
-    V4<WT> wj[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) wj[u] = a.W[j[u]];
-    S wv[U][kMaxFaces];
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int fi = 0; fi < kMaxFaces; ++fi)
-        wv[u][fi] = (ci0 + u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + ci0 + u + 1) * ldc + c] : S(0);
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      if (ci0 + u < nS) {
-        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
-#pragma unroll
-        for (int fi = 0; fi < kMaxFaces; ++fi) {
-          acc[fi][0] += wv[u][fi] * vx;
-          acc[fi][1] += wv[u][fi] * vy;
-          acc[fi][2] += wv[u][fi] * vz;
-          acc[fi][3] += wv[u][fi] * vw;
+        for (int fi = 0; fi < NF; ++fi) {
+          const S wv = inner[fi] ? s_wts[(fi * wrow + ci + 1) * kTile + t] : S(0);
+          acc[fi][0] += wv * vx;
+          acc[fi][1] += wv * vy;
+          acc[fi][2] += wv * vz;
+          acc[fi][3] += wv * vw;
         }
       }
     }
@@ -217,16 +293,16 @@ __device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk)
   a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
 
   const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
-  V4<S> L;
+  V4<S> Lm;
   int8_t flag0;
   if (fab(tMax - tMin) < VSMALL) {  // reference :208-233
-    L = V4<S>{S(1), S(1), S(1), S(1)};
+    Lm = V4<S>{S(1), S(1), S(1), S(1)};
 #pragma unroll
-    for (int fi = 0; fi < kMaxFaces; ++fi) {
+    for (int fi = 0; fi < NF; ++fi) {
       if (!inner[fi]) continue;
       const bool isNei = fid[fi] < 0;
       const int f = abs(fid[fi]) - 1;
-      const V2<G> d = a.sg[fi * ldc + c];
+      const V2<G> d = s_sg[fi * kTile + t];
       const G dx = d.x, dy = d.y;
       V4<G> o;
       o.x = (G)(pc) + gPx * dx + gPy * dy;
@@ -241,13 +317,13 @@ __device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk)
     S smooth = S(0);
     bool notTrouble = true;
 #pragma unroll
-    for (int fi = 0; fi < kMaxFaces; ++fi) {
+    for (int fi = 0; fi < NF; ++fi) {
       if (!inner[fi]) continue;
       const bool isNei = fid[fi] < 0;
       const int f = abs(fid[fi]) - 1;
-      const V2<G> d = a.sg[fi * ldc + c];
+      const V2<G> d = s_sg[fi * kTile + t];
       const G dx = d.x, dy = d.y;
-      const V2<S> rf = a.sr[fi * ldc + c];
+      const V2<S> rf = s_sr[fi * kTile + t];
       const S deltaR = rf.x, fraction = rf.y;
       const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
       S phif;
@@ -266,14 +342,14 @@ __device__ __forceinline__ void recon_body(const StageArgs<P>& a, const int blk)
       notTrouble = phif > S(0);
       a.fv[2 * f + isNei] = o;
     }
-    L.x = fmx(lp, S(0)) * notTrouble;
-    L.y = fmx(lux, S(0)) * notTrouble;
-    L.z = fmx(luy, S(0)) * notTrouble;
-    L.w = fmx(lt, S(0)) * notTrouble;
+    Lm.x = fmx(lp, S(0)) * notTrouble;
+    Lm.y = fmx(lux, S(0)) * notTrouble;
+    Lm.z = fmx(luy, S(0)) * notTrouble;
+    Lm.w = fmx(lt, S(0)) * notTrouble;
     smooth = smooth / (S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
     flag0 = (smooth > S(1));
   }
-  a.lim[c] = L;
+  a.lim[c] = Lm;
   a.si[2 * c] = flag0;
 }
 
@@ -1049,9 +1125,10 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
 
 // ------------------------------------------------------------------------- single-solve kernels
 // One solve per launch, arguments by value (read from the parameter bank).
-template <class P>
-__global__ void __launch_bounds__(128, 5) k_reconstruct(StageArgs<P> a) {
-  recon_body<P>(a, blockIdx.x);
+template <class P, int NF>
+__global__ void __launch_bounds__(kTile, 4) k_reconstruct_tile(StageArgs<P> a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  recon_tile_body<P, NF>(a, blockIdx.x, sm);
 }
 template <class P>
 __global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
@@ -1076,11 +1153,12 @@ __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double bet
 // tab[map[b].x]), as that solve's block map[b].y.  A block never spans two solves, so block-level
 // reductions (the CFL minimum, the step size) stay within one solve, and a solve's result does not
 // depend on which other solves share the batch.
-template <class P>
-__global__ void __launch_bounds__(128, 5) kb_reconstruct(const StageArgs<P>* __restrict__ tab,
-                                                         const int2* __restrict__ map) {
+template <class P, int NF>
+__global__ void __launch_bounds__(kTile, 4) kb_reconstruct_tile(const StageArgs<P>* __restrict__ tab,
+                                                                const int2* __restrict__ map) {
+  extern __shared__ __align__(128) unsigned char sm[];
   const int2 m = map[blockIdx.x];
-  recon_body<P>(tab[m.x], m.y);
+  recon_tile_body<P, NF>(tab[m.x], m.y, sm);
 }
 template <class P>
 __global__ void __launch_bounds__(128) kb_reconstruct_staged(const StageArgs<P>* __restrict__ tab,

@@ -83,16 +83,42 @@ __device__ __forceinline__ double erfc_(double a) { return erfc(a); }
 __device__ __forceinline__ float exp_(float a) { return expf(a); }
 __device__ __forceinline__ double exp_(double a) { return exp(a); }
 
-// Asynchronous global->shared copies (cp.async, cache in L1): a thread issues all of its stencil
-// gathers and weight loads back to back and waits once, instead of one dependent load at a time.
-// Sizes 4, 8 or 16 bytes; both addresses aligned to the size.
-template <int N>
-__device__ __forceinline__ void cp_async(void* smem, const void* gmem) {
-  static_assert(N == 4 || N == 8 || N == 16, "cp.async size");
-  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
-  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(N) : "memory");
+// Bulk global->shared copies (cp.async.bulk, the TMA unit's untiled form) completing on an
+// mbarrier.  Both addresses 16-byte aligned, size a multiple of 16.
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits for phase `parity` of the barrier for at most ~1 s of SM clocks; false if it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity))
+    if (clock64() - t0 > (1ll << 31)) return false;
+  return true;
+}
 
 // cond ? a : b.  The reference writes these selections as arithmetic blends
 // (c1*a + c2*b with c1, c2 in {0,1}); the ref policy keeps the blend so that signed zeros and

@@ -30,6 +30,7 @@ using namespace afar;
 namespace {
 
 constexpr int kCellBlock = 128;
+constexpr size_t kMaxDynamicSmem = 227 * 1024;  // per CTA on sm_103a
 constexpr int kFaceBlock = 256;
 // GPUevolve.cu:223-225: the reference's truncated SSP-RK3 coefficients
 constexpr double kBeta1[3] = {1.0, 0.75, 0.333333};
@@ -97,6 +98,7 @@ __global__ void k_init_ctl(StepCtl* ctl) {
     ctl->cfl = 0.5;
     ctl->last_dt = 0.0;
     ctl->steps = 0;
+    ctl->err = 0;
   }
 }
 
@@ -266,11 +268,11 @@ afar_status raise_smem_limit(K kernel, int device, size_t bytes) {
   return AFAR_OK;
 }
 
-// The mixed policy reconstructs in one register pass (recon_body); the FP64-bound policies use
-// the shared-memory staged variant, which keeps their FP64 work per face slot.
+// Dynamic shared memory of the reconstruct: the mixed policy stages a whole 128-cell tile of
+// operator rows (recon_tile_layout); the FP64-bound policies stage the stencil values.
 template <class P>
 size_t recon_smem(const afar_solver* s) {
-  if constexpr (P::id == PolicyMixed::id) return 0;
+  if constexpr (P::id == PolicyMixed::id) return recon_tile_layout(s->maxM, s->maxS).bytes;
   return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
 }
 
@@ -283,9 +285,12 @@ struct Stage {
   int gc() const { return grid_for(s->Nc, kCellBlock); }
 
   void reconstruct() const {
-    if constexpr (P::id == PolicyMixed::id)
-      k_reconstruct<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
-    else
+    if constexpr (P::id == PolicyMixed::id) {
+      if (s->maxM <= 3)
+        k_reconstruct_tile<P, 3><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
+      else
+        k_reconstruct_tile<P, 4><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
+    } else
       k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
   }
   void bvd() const { k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a); }
@@ -388,9 +393,16 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaFree(fxy));
   AFAR_CUDA(cudaFree(fsr));
-  if constexpr (P::id != PolicyMixed::id)
+  if constexpr (P::id != PolicyMixed::id) {
     return raise_smem_limit(k_reconstruct_staged<P>, s->device, recon_smem<P>(s));
-  return AFAR_OK;
+  } else {
+    if (recon_smem<P>(s) > kMaxDynamicSmem) {
+      set_error("stencil too large for the reconstruct tile: %zu bytes of shared memory", recon_smem<P>(s));
+      return AFAR_ERR_LIMIT;
+    }
+    if ((st = raise_smem_limit(k_reconstruct_tile<P, 3>, s->device, recon_smem<P>(s)))) return st;
+    return raise_smem_limit(k_reconstruct_tile<P, 4>, s->device, recon_smem<P>(s));
+  }
 }
 
 afar_status capture_graph(afar_solver* s) {
@@ -444,6 +456,21 @@ afar_status check_not_batched(afar_solver* s) {
   if (s->batch) {
     set_error("the solver belongs to a batch: step it with afar_batch_run or remove it first");
     return AFAR_ERR_STATE;
+  }
+  return AFAR_OK;
+}
+
+// Reads (and clears) the device error word after a wait: a bounded device wait that gave up marks
+// the step's results invalid.
+afar_status check_device_error(afar_solver* s) {
+  unsigned err = 0;
+  AFAR_CUDA(cudaMemcpyAsync(&err, &s->ctl->err, sizeof(err), cudaMemcpyDeviceToHost, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  if (err) {
+    AFAR_CUDA(cudaMemsetAsync(&s->ctl->err, 0, sizeof(err), s->stream));
+    AFAR_CUDA(cudaStreamSynchronize(s->stream));
+    set_error("a device-side wait for a bulk copy timed out (error word %u); the state is not valid", err);
+    return AFAR_ERR_CUDA;
   }
   return AFAR_OK;
 }
@@ -811,8 +838,8 @@ static afar_status run_impl(afar_solver* s, int nSteps, double dt, double CFL, d
   if ((st = ensure_graph(s, s->R, s->Cv))) return st;
   k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, tEnd);
   for (int i = 0; i < nSteps; ++i) AFAR_CUDA(cudaGraphLaunch(s->graph, s->stream));
-  if (wait) AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaGetLastError());
+  if (wait) return check_device_error(s);
   return AFAR_OK;
 }
 
@@ -870,7 +897,7 @@ extern "C" afar_status afar_run_timed(afar_solver* s, int nSteps, double dt, dou
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   AFAR_CUDA(cudaGetLastError());
-  return AFAR_OK;
+  return check_device_error(s);
 }
 
 extern "C" afar_status afar_profile_step(afar_solver* s, double dt, double CFL, float ms[5]) {
@@ -922,7 +949,7 @@ extern "C" afar_status afar_profile_step(afar_solver* s, double dt, double CFL, 
   }
   for (int i = 0; i < 32; ++i) cudaEventDestroy(ev[i]);
   AFAR_CUDA(cudaGetLastError());
-  return AFAR_OK;
+  return check_device_error(s);
 }
 
 extern "C" afar_status afar_synchronize(afar_solver* s) {
@@ -1207,8 +1234,13 @@ afar_status batch_build(afar_batch* b) {
   b->ncb = (int)cm.size();
   b->nfb = (int)fm.size();
   b->smem = smem;
+  int nfmax = 3;
+  for (afar_solver* s : b->members) nfmax = std::max(nfmax, s->maxM);
   if constexpr (P::id != PolicyMixed::id) {
     if ((st = raise_smem_limit(kb_reconstruct_staged<P>, b->device, smem))) return st;
+  } else {
+    if ((st = raise_smem_limit(kb_reconstruct_tile<P, 3>, b->device, smem))) return st;
+    if ((st = raise_smem_limit(kb_reconstruct_tile<P, 4>, b->device, smem))) return st;
   }
   // capture one step of the whole batch
   if (b->graph) {
@@ -1223,9 +1255,12 @@ afar_status batch_build(afar_batch* b) {
   cudaGraph_t g = nullptr;
   AFAR_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < 3; ++k) {
-    if constexpr (P::id == PolicyMixed::id)
-      kb_reconstruct<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap);
-    else
+    if constexpr (P::id == PolicyMixed::id) {
+      if (nfmax <= 3)
+        kb_reconstruct_tile<P, 3><<<b->ncb, kTile, b->smem, b->stream>>>(t, b->cmap);
+      else
+        kb_reconstruct_tile<P, 4><<<b->ncb, kTile, b->smem, b->stream>>>(t, b->cmap);
+    } else
       kb_reconstruct_staged<P><<<b->ncb, kCellBlock, b->smem, b->stream>>>(t, b->cmap);
     kb_bvd<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap);
     if (k == 0)
@@ -1327,6 +1362,8 @@ extern "C" afar_status afar_batch_run(afar_batch* b, int nSteps, float* ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   AFAR_CUDA(cudaGetLastError());
+  for (afar_solver* m : b->members)
+    if ((st = check_device_error(m))) return st;
   return AFAR_OK;
 }
 
