@@ -38,6 +38,15 @@ __device__ __forceinline__ double step_dt(const StepCtl* c) {
   return dt;
 }
 
+// The SSP-RK3 coefficients of one stage: U = b1 Un + b2 U + b3 dt R (truncated decimals, reference
+// GPUevolve.cu:222-225), their float-pair splits for the mixed policy (computed on the host so no
+// thread converts them), and the first/last-stage flags.
+struct StageCoef {
+  double b1, b2, b3;
+  float b1h, b1l, b2h, b2l;
+  int first, last;
+};
+
 template <class P>
 struct StageArgs {
   using S = typename P::S;
@@ -75,6 +84,8 @@ struct StageArgs {
   V4<double>* res_dbg;        // optional residual dump (parity hook)
   double R, Cv, invR, gamma;
   float gm1f, invRf;  // gamma - 1 and 1/R as floats (mixed)
+  float Rf, Cvf, gRf;  // R, Cv and gamma*R as floats (mixed)
+  const V2<float>* dtgf;  // Nf (delta r, fraction) as floats (mixed Courant estimate)
 };
 
 // limiterProcess (reference cudaLimiter.h:35-50)
@@ -815,8 +826,20 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
   using G = typename P::G;
   using D = typename P::D;
   using RC = typename P::RC;
+  constexpr bool kF32 = std::is_same<G, float>::value;  // mixed: no per-thread FP64 at all
   const int id = blk * blockDim.x + threadIdx.x;
+  // the Courant step: mixed estimates it in FP32 from block constants read once by thread 0
+  __shared__ float s_cfl;
+  __shared__ int s_cfl_step;
+  if constexpr (DT && kF32) {
+    if (threadIdx.x == 0) {
+      s_cfl_step = !(a.ctl->dt_fixed > 0.0);
+      s_cfl = (float)a.ctl->cfl;
+    }
+    __syncthreads();
+  }
   double dtf = 1e5;
+  float dtf32 = 1e5f;
   if (id < a.Nf) {
     const int2 on = a.on[id];
     const int own = on.x, nei = on.y;
@@ -827,7 +850,14 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
     const bool isShock = sL < 0 || sR < 0;
     const V4<G> fs = a.fs[id];
     const G Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
-    const G R = (G)a.R, Cv = (G)a.Cv;
+    G R, Cv;
+    if constexpr (kF32) {
+      R = a.Rf;
+      Cv = a.Cvf;
+    } else {
+      R = (G)a.R;
+      Cv = (G)a.Cv;
+    }
     const V4<typename P::W> Wo = a.W[own], Wn = a.W[nei];
     const V4<G> go0 = a.grad[2 * own], go1 = a.grad[2 * own + 1];
     const V4<G> gn0 = a.grad[2 * nei], gn1 = a.grad[2 * nei + 1];
@@ -867,7 +897,14 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
       pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
       pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
     }
-    const RC Rr = (RC)a.R, Cvr = (RC)a.Cv;
+    RC Rr, Cvr;
+    if constexpr (std::is_same<RC, float>::value && kF32) {
+      Rr = a.Rf;
+      Cvr = a.Cvf;
+    } else {
+      Rr = (RC)a.R;
+      Cvr = (RC)a.Cv;
+    }
     if (isShock)
       kfvs_flux<D, RC, G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
                           tRf, Rr, Cvr, (D)magSf, (D)Sfx, (D)Sfy);
@@ -876,27 +913,25 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
                          tRf, dP, dRho, Rr, Cvr, (D)magSf, (D)Sfx, (D)Sfy);
     a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)rhoUxFlux, (typename P::F)rhoUyFlux,
                                    (typename P::F)rhoEFlux};
-    if (DT) {
+    if constexpr (DT && kF32) {
+      if (s_cfl_step) {  // setDeltaT, cudaFieldOperation.h:140-157, as an FP32 estimate
+        const V2<float> g = a.dtgf[id];
+        const float deltaR = g.x, fraction = g.y;
+        dtf32 = s_cfl * deltaR * magSf /
+                ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
+                 sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+      }
+    } else if (DT) {
       const StepCtl* ctl = a.ctl;
       if (!(ctl->dt_fixed > 0.0)) {  // setDeltaT, cudaFieldOperation.h:140-157
         const V2<double> g = a.dtg[id];
-        if constexpr (P::id == PolicyMixed::id) {
-          // the mixed policy estimates the Courant step in FP32 (an estimate, not an accumulation;
-          // in FP64 its division and square root made this launch FP64-pipe bound)
-          const float deltaR = (float)g.x, fraction = (float)g.y;
-          const float cfl = (float)ctl->cfl, gR = (float)(a.gamma * a.R);
-          dtf = cfl * deltaR * magSf /
-                ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
-                 sqrtf(gR * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
-        } else {
-          const double deltaR = g.x, fraction = g.y;
-          const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
-          const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
-          dtf = CFL * deltaR * msf /
-                ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
-                 fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
-                 sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
-        }
+        const double deltaR = g.x, fraction = g.y;
+        const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
+        const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
+        dtf = CFL * deltaR * msf /
+              ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
+               fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
+               sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
       }
     }
   } else if (id < a.Nf + a.Nb) {  // boundary faces, reference :254-270
@@ -904,7 +939,14 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
     const V4<typename P::W> wb = a.W[a.Nc + b];
     const V4<G> fs = a.fs[id];
     const G Sfx = fs.x, Sfy = fs.y;
-    const G R = (G)a.R, Cv = (G)a.Cv;
+    G R, Cv;
+    if constexpr (kF32) {
+      R = a.Rf;
+      Cv = a.Cvf;
+    } else {
+      R = (G)a.R;
+      Cv = (G)a.Cv;
+    }
     const G bp = wb.x, bUx = wb.y, bUy = wb.z, bT = wb.w;
     const G rho = bp / (R * bT);
     const G rhoFlux = rho * (bUx * Sfx + bUy * Sfy);
@@ -912,7 +954,29 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
                                    (typename P::F)(rhoFlux * bUy + bp * Sfy),
                                    (typename P::F)(rhoFlux * (Cv * bT + G(0.5) * (bUx * bUx + bUy * bUy) + bp / rho))};
   }
-  if (DT) {
+  if constexpr (DT && kF32) {
+    // block min of the float estimates on their bit patterns (non-negative floats order like
+    // them; NaN sorts above +inf), then one atomicMin per block on the double's bits
+    unsigned v = (unsigned)__float_as_int(dtf32);
+    if (!(dtf32 >= 0.f)) v = 0x7F800000u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned u = __shfl_xor_sync(0xffffffffu, v, o);
+      v = u < v ? u : v;
+    }
+    __shared__ unsigned wmin32[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmin32[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned m = wmin32[0];
+      for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = wmin32[k] < m ? wmin32[k] : m;
+      const float mf = __int_as_float((int)m);
+      const unsigned long long bits =
+          m >= 0x7F800000u ? 0x7FF0000000000000ull : (unsigned long long)__double_as_longlong((double)mf);
+      atomicMin(&a.ctl->dt_bits, bits);
+    }
+  } else if (DT) {
     // block min (warp shuffles) then one atomicMin per block on the bit pattern; non-negative
     // doubles order like their bit patterns, and NaN patterns sort above +inf.
     unsigned long long v = (unsigned long long)__double_as_longlong(dtf);
@@ -968,13 +1032,14 @@ __device__ __forceinline__ void two_sum(float& s, float& e, const float a, const
 // the float-pair difference rhoE - |rhoU|^2/(2 rho) (the cancellation at high Mach costs no
 // precision), rounded once to float.  k = {beta3*dt, beta1 (hi, lo), beta2 (hi, lo)} of the stage.
 template <class P>
-__device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c, const float* k, const bool first,
-                                             const int last_stage) {
+__device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c, const StageCoef& k,
+                                             const int* s_go, const float* s_bdt) {
   const int ldc = a.ldc;
-  const int nM = a.nM[c];
+  const bool live = c < a.Nc;
+  const int nM = live ? a.nM[c] : 0;
   float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
   constexpr int MB = 4;
-  for (int f0 = 0; f0 < nM; f0 += MB) {
+  for (int f0 = 0; f0 < nM; f0 += MB) {  // the gather needs no step size: it overlaps thread 0's work
     int fid[MB];
 #pragma unroll
     for (int u = 0; u < MB; ++u) fid[u] = (f0 + u < nM) ? a.cf[(f0 + u) * ldc + c] : 1;
@@ -995,16 +1060,18 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
       }
     }
   }
+  __syncthreads();  // the block's step size (thread 0)
+  if (!live || !*s_go) return;
   if (a.res_dbg) a.res_dbg[c] = V4<double>{(double)hi[0] + lo[0], (double)hi[1] + lo[1], (double)hi[2] + lo[2],
                                           (double)hi[3] + lo[3]};
-  const float s3 = -k[0] * a.vinvf[c];
+  const float s3 = -*s_bdt * a.vinvf[c];
   DF4* const U = reinterpret_cast<DF4*>(a.U);
   DF4* const U0 = reinterpret_cast<DF4*>(a.U0);
   const DF4 o = U0[c];
   DF base[4] = {{o.hi.x, o.lo.x}, {o.hi.y, o.lo.y}, {o.hi.z, o.lo.z}, {o.hi.w, o.lo.w}};
-  if (!first) {  // stages 2, 3: beta1 Un + beta2 U (stage 1 is Un + increment, U not read)
+  if (!k.first) {  // stages 2, 3: beta1 Un + beta2 U (stage 1 is Un + increment, U not read)
     const DF4 u = U[c];
-    const DF b1{k[1], k[2]}, b2{k[3], k[4]};
+    const DF b1{k.b1h, k.b1l}, b2{k.b2h, k.b2l};
     const DF uu[4] = {{u.hi.x, u.lo.x}, {u.hi.y, u.lo.y}, {u.hi.z, u.lo.z}, {u.hi.w, u.lo.w}};
 #pragma unroll
     for (int q = 0; q < 4; ++q) base[q] = df_add(df_mul(b1, base[q]), df_mul(b2, uu[q]));
@@ -1014,8 +1081,9 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
   for (int q = 0; q < 4; ++q) un[q] = df_add(base[q], __fmul_rn(s3, __fadd_rn(hi[q], lo[q])));
   const DF4 st{{un[0].hi, un[1].hi, un[2].hi, un[3].hi}, {un[0].lo, un[1].lo, un[2].lo, un[3].lo}};
   U[c] = st;
-  if (last_stage) U0[c] = st;
-  const float irf = __frcp_rn(un[0].hi);
+  if (k.last) U0[c] = st;
+  float irf = __fdividef(1.f, un[0].hi);  // 1/rho: fast reciprocal + one Newton step (~1 ulp)
+  irf = __fmaf_rn(irf, __fmaf_rn(-un[0].hi, irf, 1.f), irf);
   const DF ke2 = df_div(df_add(df_sqr(un[1]), df_sqr(un[2])), un[0], irf);  // |rhoU|^2 / rho
   const DF e = df_add(un[3], DF{-0.5f * ke2.hi, -0.5f * ke2.lo});
   const float pf = a.gm1f * __fadd_rn(e.hi, e.lo);
@@ -1036,31 +1104,30 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
 // face fluxes in the cell's face order (no atomics), SSP-RK3 combine, conserved -> primitive, and
 // the ghost state of this cell's boundary faces from the new state.
 template <class P>
-__device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk, const double beta1,
-                                            const double beta2, const double beta3, const int last_stage) {
-  __shared__ double s_dt;  // the step size, read once per block (a block never spans two solves)
-  __shared__ float s_k[5];  // mixed: beta3*dt and the float-pair betas, split once per block
+__device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk, const StageCoef& k) {
+  // Block constants, computed once by thread 0 (a block never spans two solves): the step size,
+  // whether the step is live, and for mixed beta3*dt as a float.  Per-thread code then makes no
+  // FP64 operation in the mixed policy (on GB300 even an FP64 comparison costs FP64-pipe time).
+  __shared__ double s_dt;
+  __shared__ int s_go;
+  __shared__ float s_bdt;
   if (threadIdx.x == 0) {
     s_dt = step_dt(a.ctl);
-    if constexpr (P::id == PolicyMixed::id) {
-      s_k[0] = (float)(beta3 * s_dt);
-      s_k[1] = (float)beta1;
-      s_k[2] = (float)(beta1 - (double)s_k[1]);
-      s_k[3] = (float)beta2;
-      s_k[4] = (float)(beta2 - (double)s_k[3]);
-    }
+    s_go = s_dt > 0.0;  // past t_end: the step is a no-op
+    if constexpr (P::id == PolicyMixed::id) s_bdt = (float)(k.b3 * s_dt);
   }
-  __syncthreads();
-  const double deltaT = s_dt;
   const int c = blk * blockDim.x + threadIdx.x;
-  if (c >= a.Nc) return;
-  if (!(deltaT > 0.0)) return;  // past t_end: the step is a no-op
-  const int ldc = a.ldc;
-  const int nM = a.nM[c];
   if constexpr (P::id == PolicyMixed::id) {
-    update_mixed(a, c, s_k, beta2 == 0.0 && beta1 == 1.0, last_stage);
+    update_mixed(a, c, k, &s_go, &s_bdt);  // synchronises the block after its flux gather
     return;
   }
+  __syncthreads();
+  if (c >= a.Nc || !s_go) return;
+  const double beta1 = k.b1, beta2 = k.b2, beta3 = k.b3;
+  const int last_stage = k.last;
+  const double deltaT = s_dt;
+  const int ldc = a.ldc;
+  const int nM = a.nM[c];
   double Rrho = 0.0, RrhoUx = 0.0, RrhoUy = 0.0, RrhoE = 0.0;
   constexpr int MB = 4;  // face ids, then fluxes, four loads in flight; sums keep the face order
   for (int f0 = 0; f0 < nM; f0 += MB) {
@@ -1143,9 +1210,8 @@ __global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
   flux_body<P, DT>(a, blockIdx.x);
 }
 template <class P>
-__global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const double beta1, const double beta2,
-                                                const double beta3, const int last_stage) {
-  update_body<P>(a, blockIdx.x, beta1, beta2, beta3, last_stage);
+__global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const StageCoef k) {
+  update_body<P>(a, blockIdx.x, k);
 }
 
 // ------------------------------------------------------------------------- batch kernels
@@ -1180,10 +1246,9 @@ __global__ void __launch_bounds__(256) kb_flux(const StageArgs<P>* __restrict__ 
 }
 template <class P>
 __global__ void __launch_bounds__(128) kb_update(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map,
-                                                 const double beta1, const double beta2, const double beta3,
-                                                 const int last_stage) {
+                                                 const StageCoef k) {
   const int2 m = map[blockIdx.x];
-  update_body<P>(tab[m.x], m.y, beta1, beta2, beta3, last_stage);
+  update_body<P>(tab[m.x], m.y, k);
 }
 
 // Closes a step: advance time, record the step, re-arm the CFL minimum for the next step.

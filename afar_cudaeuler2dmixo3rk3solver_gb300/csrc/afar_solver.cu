@@ -131,12 +131,32 @@ __global__ void k_df_to_double(int n, const DF4* in, V4<double>* out) {
 }
 
 template <class A, class B>
+__global__ void k_convert2(int n, const V2<A>* in, V2<B>* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = V2<B>{(B)in[i].x, (B)in[i].y};
+}
+
+template <class A, class B>
 __global__ void k_convert4(int n, const V4<A>* in, V4<B>* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = V4<B>{(B)in[i].x, (B)in[i].y, (B)in[i].z, (B)in[i].w};
 }
 
 inline int grid_for(long long n, int block) { return (int)((n + block - 1) / block); }
+
+StageCoef stage_coef(int k) {
+  StageCoef c;
+  c.b1 = kBeta1[k];
+  c.b2 = kBeta2[k];
+  c.b3 = kBeta3[k];
+  c.b1h = (float)c.b1;
+  c.b1l = (float)(c.b1 - (double)c.b1h);
+  c.b2h = (float)c.b2;
+  c.b2l = (float)(c.b2 - (double)c.b2h);
+  c.first = k == 0;
+  c.last = k == 2;
+  return c;
+}
 
 }  // namespace
 
@@ -154,6 +174,7 @@ struct afar_solver {
   double* vol = nullptr;
   double* vinv = nullptr;
   float* vinvf = nullptr;  // mixed: 1/V as float
+  V2<float>* dtgf = nullptr;  // mixed: Courant geometry as float
   void* xfer = nullptr;    // mixed: staging for double <-> device-format copies, 32 B x (Nc + Nb)
   int2* on = nullptr;
   int* bnei = nullptr;
@@ -250,6 +271,10 @@ StageArgs<P> make_args(afar_solver* s) {
   a.gm1f = (float)(a.gamma - 1.0);
   a.invRf = (float)a.invR;
   a.vinvf = s->vinvf;
+  a.Rf = (float)s->R;
+  a.Cvf = (float)s->Cv;
+  a.gRf = (float)(a.gamma * s->R);
+  a.dtgf = s->dtgf;
   return a;
 }
 
@@ -317,7 +342,7 @@ struct Stage {
     }
   }
   void update(int k) const {
-    k_update<P><<<gc(), kCellBlock, 0, s->stream>>>(a, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+    k_update<P><<<gc(), kCellBlock, 0, s->stream>>>(a, stage_coef(k));
   }
 };
 
@@ -389,6 +414,10 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
   k_setup_lsm<P><<<gc, kCellBlock, 0, s->stream>>>(a, static_cast<V2<S>*>(s->lsm), nullptr, 0);
   k_setup_slot_geom<P><<<gc, kCellBlock, 0, s->stream>>>(a, fxy);
   k_setup_face_geom<P><<<gF, kFaceBlock, 0, s->stream>>>(a, fxy, fsr);
+  if constexpr (P::id == PolicyMixed::id) {
+    if ((st = dalloc_t(s, &s->dtgf, (size_t)Nf))) return st;
+    if (Nf > 0) k_convert2<double, float><<<grid_for(Nf, 256), 256, 0, s->stream>>>(Nf, s->dtg, s->dtgf);
+  }
   AFAR_CUDA(cudaGetLastError());
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaFree(fxy));
@@ -1267,7 +1296,7 @@ afar_status batch_build(afar_batch* b) {
       kb_flux<P, true><<<b->nfb, kFaceBlock, 0, b->stream>>>(t, b->fmap);
     else
       kb_flux<P, false><<<b->nfb, kFaceBlock, 0, b->stream>>>(t, b->fmap);
-    kb_update<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap, kBeta1[k], kBeta2[k], kBeta3[k], k == 2);
+    kb_update<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap, stage_coef(k));
   }
   kb_finish_step<P><<<grid_for((long long)tab.size(), 128), 128, 0, b->stream>>>(t, (int)tab.size());
   AFAR_CUDA(cudaStreamEndCapture(b->stream, &g));
