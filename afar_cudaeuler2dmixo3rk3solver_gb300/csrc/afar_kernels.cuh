@@ -102,6 +102,20 @@ __device__ __forceinline__ void limiter_process(S& limiter, S& phif, const S phi
   limiter = fmn(limiter, yy);
 }
 
+// limiterProcess for the mixed policy: the same ratio with selects and the fast float division
+// (2 ulp, MUFU reciprocal); the ratio feeds a min() with 2 and 1, so a rounding apart is all it
+// changes.
+__device__ __forceinline__ void limiter_process_fast(float& limiter, float& phif, const float phic, const float phiMax,
+                                                     const float phiMin, const float gx, const float gy,
+                                                     const float dx, const float dy) {
+  phif = phic;
+  phif += gx * dx + gy * dy;
+  const float d2 = phif - phic;
+  const float d1 = phif < phic ? phiMin - phic : phiMax - phic;
+  const float yy = fabsf(d2) >= 1e-5f ? fminf(2.f, __fdividef(0.5f * d1, d2 + (d2 >= 0.f ? 1e-10f : -1e-10f))) : 1.f;
+  limiter = fminf(limiter, yy);
+}
+
 // Faces per cell: triangles and quadrilaterals, the only cells the reference's quadrature accepts
 // (d2GaussQuadrature.C:65-148); the stencil upload rejects larger compact stencils.
 constexpr int kMaxFaces = 4;
@@ -238,10 +252,13 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   }
   const V4<WT> wc = s_w[t];
   const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  // O3 weights of boundary-face and missing slots are zero in the operator rows (setup), so only
+  // slots past this mesh's largest cell (a batch may stage fewer rows than NF) are skipped
+  const int nfm = a.maxM;
   G acc[NF][4];
 #pragma unroll
   for (int fi = 0; fi < NF; ++fi) {  // each face side's O3 sum starts with the cell's own term
-    const S w0 = inner[fi] ? s_wts[(fi * wrow) * kTile + t] : S(0);
+    const S w0 = fi < nfm ? s_wts[(fi * wrow) * kTile + t] : S(0);
     acc[fi][0] = w0 * pc;
     acc[fi][1] = w0 * uxc;
     acc[fi][2] = w0 * uyc;
@@ -256,7 +273,8 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   for (int ci0 = 0; ci0 < nS; ci0 += U) {
     V4<WT> wj[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) wj[u] = a.W[ci0 + u < nS ? s_sten[(ci0 + u) * kTile + t] : c];
+    for (int u = 0; u < U; ++u)
+      if (ci0 + u < nS) wj[u] = a.W[s_sten[(ci0 + u) * kTile + t]];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int ci = ci0 + u;
@@ -291,7 +309,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
         }
 #pragma unroll
         for (int fi = 0; fi < NF; ++fi) {
-          const S wv = inner[fi] ? s_wts[(fi * wrow + ci + 1) * kTile + t] : S(0);
+          const S wv = fi < nfm ? s_wts[(fi * wrow + ci + 1) * kTile + t] : S(0);
           acc[fi][0] += wv * vx;
           acc[fi][1] += wv * vy;
           acc[fi][2] += wv * vz;
@@ -339,16 +357,16 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
       const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
       S phif;
       V4<G> o;
-      limiter_process(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
+      limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
       o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
       notTrouble = phif > S(0);
-      smooth = fmx(smooth, fab((S(1) - fraction) * pc + fraction * pn[fi] - phif) / deltaR +
+      smooth = fmx(smooth, __fdividef(fab((S(1) - fraction) * pc + fraction * pn[fi] - phif), deltaR) +
                                (pf <= S(0)) * AFAR_LIT(S, 1e20) + (phif <= S(0)) * AFAR_LIT(S, 1e20));
-      limiter_process(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
+      limiter_process_fast(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
       o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
-      limiter_process(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
+      limiter_process_fast(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
       o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
-      limiter_process(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
+      limiter_process_fast(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
       o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
       notTrouble = phif > S(0);
       a.fv[2 * f + isNei] = o;
@@ -357,7 +375,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
     Lm.y = fmx(lux, S(0)) * notTrouble;
     Lm.z = fmx(luy, S(0)) * notTrouble;
     Lm.w = fmx(lt, S(0)) * notTrouble;
-    smooth = smooth / (S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
+    smooth = __fdividef(smooth, S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
     flag0 = (smooth > S(1));
   }
   a.lim[c] = Lm;
