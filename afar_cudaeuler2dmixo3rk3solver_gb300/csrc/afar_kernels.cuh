@@ -127,25 +127,14 @@ constexpr int kMaxFaces = 4;
 // one mbarrier) instead of per-thread loads: ~50 KB per tile in flight from a handful of lanes,
 // while registers stay free for the stencil gathers, which hit L2.
 constexpr int kTile = 128;
-#ifndef AFAR_RECON_GATHER
-#define AFAR_RECON_GATHER 8  // stencil gathers in flight per thread
-#endif
-#ifndef AFAR_RECON_MIN_CTAS
-#define AFAR_RECON_MIN_CTAS 4  // resident tiles per SM the register budget is sized for
-#endif
-// p4: the shared-memory pitch, in elements, of the 4-byte rows (face ids, stencil ids, weights).
-// The two-threads-per-cell variant reads two rows of the same cells at once, so it pads the pitch
-// to kTile + 16 words: the two half-warps then fall in disjoint banks.
 struct ReconTile {
-  unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_bar, bytes, p4;
+  unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_bar, bytes;
 };
-constexpr unsigned kPitchPair = kTile + 16;
-__host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int maxS, const unsigned p4 = kTile) {
+__host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int maxS) {
   ReconTile L;
-  L.p4 = p4;
   unsigned o = 0;
   L.off_cf = o;
-  o += maxM * p4 * 4;
+  o += maxM * kTile * 4;
   L.off_lsm = o;
   o += maxM * kTile * 8;
   L.off_sg = o;
@@ -153,9 +142,9 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
   L.off_sr = o;
   o += maxM * kTile * 8;
   L.off_sten = o;
-  o += maxS * p4 * 4;
+  o += maxS * kTile * 4;
   L.off_wts = o;
-  o += maxM * (maxS + 1) * p4 * 4;
+  o += maxM * (maxS + 1) * kTile * 4;
   L.off_w = o;
   o += kTile * 16;
   L.off_bar = o;
@@ -169,7 +158,7 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
 template <class P>
 __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const int blk, const ReconTile& L,
                                                  unsigned char* sm, unsigned long long* bar) {
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x;
   const int c0 = blk * kTile;
   const unsigned ne = (unsigned)min(kTile, a.ldc - c0);  // elements of a row slice
   const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
@@ -183,7 +172,7 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
     const void* src;
     unsigned bytes;
     if (r < M) {
-      dst = sm + L.off_cf + r * L.p4 * 4;
+      dst = sm + L.off_cf + r * kTile * 4;
       src = a.cf + (size_t)r * a.ldc + c0;
       bytes = ne * 4;
     } else if (r < 2 * M) {
@@ -203,12 +192,12 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
       bytes = ne * 8;
     } else if (r < 4 * M + S) {
       const int k = r - 4 * M;
-      dst = sm + L.off_sten + k * L.p4 * 4;
+      dst = sm + L.off_sten + k * kTile * 4;
       src = a.sten + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
     } else if (r < rows - 1) {
       const int k = r - 4 * M - S;
-      dst = sm + L.off_wts + k * L.p4 * 4;
+      dst = sm + L.off_wts + k * kTile * 4;
       src = a.wts + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
     } else {
@@ -280,7 +269,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   S pn[NF];  // pressure of the cell across each face
 #pragma unroll
   for (int fi = 0; fi < NF; ++fi) pn[fi] = S(0);
-  constexpr int U = AFAR_RECON_GATHER;
+  constexpr int U = 8;
   for (int ci0 = 0; ci0 < nS; ci0 += U) {
     V4<WT> wj[U];
 #pragma unroll
@@ -382,216 +371,6 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
       notTrouble = phif > S(0);
       a.fv[2 * f + isNei] = o;
     }
-    Lm.x = fmx(lp, S(0)) * notTrouble;
-    Lm.y = fmx(lux, S(0)) * notTrouble;
-    Lm.z = fmx(luy, S(0)) * notTrouble;
-    Lm.w = fmx(lt, S(0)) * notTrouble;
-    smooth = __fdividef(smooth, S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
-    flag0 = (smooth > S(1));
-  }
-  a.lim[c] = Lm;
-  a.si[2 * c] = flag0;
-}
-
-// The same reconstruct with two threads per cell (256 threads per 128-cell tile): the pair
-// (lanes 2k, 2k+1) splits the stencil by parity (thread h takes members h, h+2, ...), so each
-// thread waits on half as many gathers, and splits the faces the same way for the limiter.  Partial
-// sums, gradients and min/max are combined across the pair with shuffles (the O3 and gradient sums
-// are then added in two interleaved halves instead of stencil order: a rounding apart).  One
-// elected thread waits on the tile's mbarrier (bounded) and the block follows at a barrier.
-template <class P, int NF>
-__device__ __forceinline__ void recon_pair_body(const StageArgs<P>& a, const int blk, unsigned char* sm) {
-  using S = typename P::S;
-  using G = typename P::G;
-  using WT = typename P::W;
-  const ReconTile L = recon_tile_layout(a.maxM, a.maxS, kPitchPair);
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + L.off_bar);
-  __shared__ int s_ok;
-  const int t = threadIdx.x;
-  if (t == 0) mbar_init(bar, 1);
-  __syncthreads();
-  if (t < 32) recon_tile_fetch(a, blk, L, sm, bar);
-  const int ct = t >> 1, h = t & 1;
-  const int c = blk * kTile + ct;
-  const bool live = c < a.Nc;
-  const int nS = live ? a.nS[c] : 0, nM = live ? a.nM[c] : 0;
-  if (t == 0) s_ok = mbar_wait_bounded(bar, 0);
-  __syncthreads();
-  if (!s_ok) {  // the copies did not land: flag it, give them a last chance, leave
-    if (t == 0) {
-      atomicOr(&a.ctl->err, 1u);
-      mbar_wait_bounded(bar, 0);
-    }
-    return;
-  }
-  const unsigned P4 = L.p4;
-  const int* s_cf = reinterpret_cast<const int*>(sm + L.off_cf);
-  const V2<S>* s_lsm = reinterpret_cast<const V2<S>*>(sm + L.off_lsm);
-  const V2<G>* s_sg = reinterpret_cast<const V2<G>*>(sm + L.off_sg);
-  const V2<S>* s_sr = reinterpret_cast<const V2<S>*>(sm + L.off_sr);
-  const int* s_sten = reinterpret_cast<const int*>(sm + L.off_sten);
-  const S* s_wts = reinterpret_cast<const S*>(sm + L.off_wts);
-  const V4<WT>* s_w = reinterpret_cast<const V4<WT>*>(sm + L.off_w);
-  const int wrow = a.maxS + 1;
-  const int nfm = a.maxM;  // weight rows staged (zero weights cover boundary and missing slots)
-
-  int fid[NF];
-  bool inner[NF];
-#pragma unroll
-  for (int fi = 0; fi < NF; ++fi) {
-    fid[fi] = fi < nM ? s_cf[fi * P4 + ct] : 1;
-    inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
-  }
-  const V4<WT> wc = s_w[ct];
-  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
-  G acc[NF][4];
-#pragma unroll
-  for (int fi = 0; fi < NF; ++fi) {  // the cell's own term, once per pair
-    const S w0 = (h == 0 && fi < nfm) ? s_wts[(fi * wrow) * P4 + ct] : S(0);
-    acc[fi][0] = w0 * pc;
-    acc[fi][1] = w0 * uxc;
-    acc[fi][2] = w0 * uyc;
-    acc[fi][3] = w0 * tc;
-  }
-  G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
-  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
-  S pn[NF];
-#pragma unroll
-  for (int fi = 0; fi < NF; ++fi) pn[fi] = S(0);
-  constexpr int U = 4;
-  for (int ci0 = h; ci0 < nS; ci0 += 2 * U) {
-    V4<WT> wj[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (ci0 + 2 * u < nS) wj[u] = a.W[s_sten[(ci0 + 2 * u) * P4 + ct]];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int ci = ci0 + 2 * u;
-      if (ci < nS) {
-        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
-        if (ci < nM) {  // compact members: reference :148-169, :190-205
-          const V2<S> lm = s_lsm[ci * kTile + ct];
-          const S M1 = lm.x, M2 = lm.y;
-          S dphi = vx - pc;
-          gPx += M1 * dphi;
-          gPy += M2 * dphi;
-          dphi = vy - uxc;
-          gUxx += M1 * dphi;
-          gUyx += M2 * dphi;
-          dphi = vz - uyc;
-          gUxy += M1 * dphi;
-          gUyy += M2 * dphi;
-          dphi = vw - tc;
-          gTx += M1 * dphi;
-          gTy += M2 * dphi;
-          pMax = fmx(vx, pMax);
-          pMin = fmn(vx, pMin);
-          uxMax = fmx(vy, uxMax);
-          uxMin = fmn(vy, uxMin);
-          uyMax = fmx(vz, uyMax);
-          uyMin = fmn(vz, uyMin);
-          tMax = fmx(vw, tMax);
-          tMin = fmn(vw, tMin);
-#pragma unroll
-          for (int fi = 0; fi < NF; ++fi)
-            if (fi == ci) pn[fi] = vx;
-        }
-#pragma unroll
-        for (int fi = 0; fi < NF; ++fi) {
-          const S wv = fi < nfm ? s_wts[(fi * wrow + ci + 1) * P4 + ct] : S(0);
-          acc[fi][0] += wv * vx;
-          acc[fi][1] += wv * vy;
-          acc[fi][2] += wv * vz;
-          acc[fi][3] += wv * vw;
-        }
-      }
-    }
-  }
-  // combine the pair (every lane of the warp takes part)
-  constexpr unsigned FULL = 0xffffffffu;
-#pragma unroll
-  for (int fi = 0; fi < NF; ++fi)
-#pragma unroll
-    for (int q = 0; q < 4; ++q) acc[fi][q] += __shfl_xor_sync(FULL, acc[fi][q], 1);
-  gPx += __shfl_xor_sync(FULL, gPx, 1);
-  gPy += __shfl_xor_sync(FULL, gPy, 1);
-  gUxx += __shfl_xor_sync(FULL, gUxx, 1);
-  gUxy += __shfl_xor_sync(FULL, gUxy, 1);
-  gUyx += __shfl_xor_sync(FULL, gUyx, 1);
-  gUyy += __shfl_xor_sync(FULL, gUyy, 1);
-  gTx += __shfl_xor_sync(FULL, gTx, 1);
-  gTy += __shfl_xor_sync(FULL, gTy, 1);
-  pMax = fmx(pMax, __shfl_xor_sync(FULL, pMax, 1));
-  pMin = fmn(pMin, __shfl_xor_sync(FULL, pMin, 1));
-  uxMax = fmx(uxMax, __shfl_xor_sync(FULL, uxMax, 1));
-  uxMin = fmn(uxMin, __shfl_xor_sync(FULL, uxMin, 1));
-  uyMax = fmx(uyMax, __shfl_xor_sync(FULL, uyMax, 1));
-  uyMin = fmn(uyMin, __shfl_xor_sync(FULL, uyMin, 1));
-  tMax = fmx(tMax, __shfl_xor_sync(FULL, tMax, 1));
-  tMin = fmn(tMin, __shfl_xor_sync(FULL, tMin, 1));
-#pragma unroll
-  for (int fi = 0; fi < NF; ++fi) {
-    const S other = __shfl_xor_sync(FULL, pn[fi], 1);
-    pn[fi] = (fi & 1) == h ? pn[fi] : other;  // member fi was gathered by the thread of its parity
-  }
-
-  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
-  const bool flat = fab(tMax - tMin) < VSMALL;  // the same on both threads of the pair
-  S lp = S(2), lux = S(2), luy = S(2), lt = S(2);
-  S smooth = S(0);
-  int lastFace = -1;  // the last internal face this thread handled, and its T check
-  bool lastNotTrouble = true;
-#pragma unroll
-  for (int fi = 0; fi < NF; ++fi) {
-    if ((fi & 1) != h || !inner[fi]) continue;  // faces split by parity
-    const bool isNei = fid[fi] < 0;
-    const int f = abs(fid[fi]) - 1;
-    const V2<G> d = s_sg[fi * kTile + ct];
-    const G dx = d.x, dy = d.y;
-    V4<G> o;
-    if (flat) {  // reference :208-233
-      o.x = (G)(pc) + gPx * dx + gPy * dy;
-      o.y = (G)(uxc) + gUxx * dx + gUyx * dy;
-      o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
-      o.w = (G)(tc) + gTx * dx + gTy * dy;
-    } else {  // reference :235-314
-      const V2<S> rf = s_sr[fi * kTile + ct];
-      const S deltaR = rf.x, fraction = rf.y;
-      const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
-      S phif;
-      limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
-      o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
-      smooth = fmx(smooth, __fdividef(fab((S(1) - fraction) * pc + fraction * pn[fi] - phif), deltaR) +
-                               (pf <= S(0)) * AFAR_LIT(S, 1e20) + (phif <= S(0)) * AFAR_LIT(S, 1e20));
-      limiter_process_fast(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
-      o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
-      limiter_process_fast(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
-      o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
-      limiter_process_fast(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
-      o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
-      lastFace = fi;
-      lastNotTrouble = phif > S(0);
-    }
-    if (live) a.fv[2 * f + isNei] = o;
-  }
-  // combine the limiter pieces: min, max, and the T check of the pair's last internal face
-  lp = fmn(lp, __shfl_xor_sync(FULL, lp, 1));
-  lux = fmn(lux, __shfl_xor_sync(FULL, lux, 1));
-  luy = fmn(luy, __shfl_xor_sync(FULL, luy, 1));
-  lt = fmn(lt, __shfl_xor_sync(FULL, lt, 1));
-  smooth = fmx(smooth, __shfl_xor_sync(FULL, smooth, 1));
-  const int otherLast = __shfl_xor_sync(FULL, lastFace, 1);
-  const bool otherNT = __shfl_xor_sync(FULL, (int)lastNotTrouble, 1) != 0;
-  const bool notTrouble = otherLast > lastFace ? otherNT : lastNotTrouble;
-  if (!live || h != 0) return;
-  a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
-  a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
-  V4<S> Lm;
-  int8_t flag0;
-  if (flat) {
-    Lm = V4<S>{S(1), S(1), S(1), S(1)};
-    flag0 = 0;
-  } else {
     Lm.x = fmx(lp, S(0)) * notTrouble;
     Lm.y = fmx(lux, S(0)) * notTrouble;
     Lm.z = fmx(luy, S(0)) * notTrouble;
@@ -1432,12 +1211,7 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
 // ------------------------------------------------------------------------- single-solve kernels
 // One solve per launch, arguments by value (read from the parameter bank).
 template <class P, int NF>
-__global__ void __launch_bounds__(2 * kTile, 3) k_reconstruct_pair(StageArgs<P> a) {
-  extern __shared__ __align__(128) unsigned char sm[];
-  recon_pair_body<P, NF>(a, blockIdx.x, sm);
-}
-template <class P, int NF>
-__global__ void __launch_bounds__(kTile, AFAR_RECON_MIN_CTAS) k_reconstruct_tile(StageArgs<P> a) {
+__global__ void __launch_bounds__(kTile, 4) k_reconstruct_tile(StageArgs<P> a) {
   extern __shared__ __align__(128) unsigned char sm[];
   recon_tile_body<P, NF>(a, blockIdx.x, sm);
 }
@@ -1464,14 +1238,7 @@ __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const StageCoef 
 // reductions (the CFL minimum, the step size) stay within one solve, and a solve's result does not
 // depend on which other solves share the batch.
 template <class P, int NF>
-__global__ void __launch_bounds__(2 * kTile, 3) kb_reconstruct_pair(const StageArgs<P>* __restrict__ tab,
-                                                                   const int2* __restrict__ map) {
-  extern __shared__ __align__(128) unsigned char sm[];
-  const int2 m = map[blockIdx.x];
-  recon_pair_body<P, NF>(tab[m.x], m.y, sm);
-}
-template <class P, int NF>
-__global__ void __launch_bounds__(kTile, AFAR_RECON_MIN_CTAS) kb_reconstruct_tile(const StageArgs<P>* __restrict__ tab,
+__global__ void __launch_bounds__(kTile, 4) kb_reconstruct_tile(const StageArgs<P>* __restrict__ tab,
                                                                 const int2* __restrict__ map) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int2 m = map[blockIdx.x];

@@ -31,25 +31,6 @@ namespace {
 
 constexpr int kCellBlock = 128;
 constexpr size_t kMaxDynamicSmem = 227 * 1024;  // per CTA on sm_103a
-#ifndef AFAR_RECON_PAIR
-#define AFAR_RECON_PAIR 0  // mixed reconstruct: 1 = two threads per cell, 0 = one
-#endif
-constexpr unsigned kReconPitch = AFAR_RECON_PAIR ? kPitchPair : kTile;
-constexpr int kReconThreads = AFAR_RECON_PAIR ? 2 * kTile : kTile;
-template <class P, int NF>
-constexpr auto recon_kernel() {
-  if constexpr (AFAR_RECON_PAIR)
-    return k_reconstruct_pair<P, NF>;
-  else
-    return k_reconstruct_tile<P, NF>;
-}
-template <class P, int NF>
-constexpr auto recon_kernel_batch() {
-  if constexpr (AFAR_RECON_PAIR)
-    return kb_reconstruct_pair<P, NF>;
-  else
-    return kb_reconstruct_tile<P, NF>;
-}
 constexpr int kFaceBlock = 256;
 // GPUevolve.cu:223-225: the reference's truncated SSP-RK3 coefficients
 constexpr double kBeta1[3] = {1.0, 0.75, 0.333333};
@@ -316,7 +297,7 @@ afar_status raise_smem_limit(K kernel, int device, size_t bytes) {
 // operator rows (recon_tile_layout); the FP64-bound policies stage the stencil values.
 template <class P>
 size_t recon_smem(const afar_solver* s) {
-  if constexpr (P::id == PolicyMixed::id) return recon_tile_layout(s->maxM, s->maxS, kReconPitch).bytes;
+  if constexpr (P::id == PolicyMixed::id) return recon_tile_layout(s->maxM, s->maxS).bytes;
   return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
 }
 
@@ -331,9 +312,9 @@ struct Stage {
   void reconstruct() const {
     if constexpr (P::id == PolicyMixed::id) {
       if (s->maxM <= 3)
-        recon_kernel<P, 3>()<<<gc(), kReconThreads, recon_smem<P>(s), s->stream>>>(a);
+        k_reconstruct_tile<P, 3><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
       else
-        recon_kernel<P, 4>()<<<gc(), kReconThreads, recon_smem<P>(s), s->stream>>>(a);
+        k_reconstruct_tile<P, 4><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
     } else
       k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
   }
@@ -448,8 +429,8 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
       set_error("stencil too large for the reconstruct tile: %zu bytes of shared memory", recon_smem<P>(s));
       return AFAR_ERR_LIMIT;
     }
-    if ((st = raise_smem_limit(recon_kernel<P, 3>(), s->device, recon_smem<P>(s)))) return st;
-    return raise_smem_limit(recon_kernel<P, 4>(), s->device, recon_smem<P>(s));
+    if ((st = raise_smem_limit(k_reconstruct_tile<P, 3>, s->device, recon_smem<P>(s)))) return st;
+    return raise_smem_limit(k_reconstruct_tile<P, 4>, s->device, recon_smem<P>(s));
   }
 }
 
@@ -1287,8 +1268,8 @@ afar_status batch_build(afar_batch* b) {
   if constexpr (P::id != PolicyMixed::id) {
     if ((st = raise_smem_limit(kb_reconstruct_staged<P>, b->device, smem))) return st;
   } else {
-    if ((st = raise_smem_limit(recon_kernel_batch<P, 3>(), b->device, smem))) return st;
-    if ((st = raise_smem_limit(recon_kernel_batch<P, 4>(), b->device, smem))) return st;
+    if ((st = raise_smem_limit(kb_reconstruct_tile<P, 3>, b->device, smem))) return st;
+    if ((st = raise_smem_limit(kb_reconstruct_tile<P, 4>, b->device, smem))) return st;
   }
   // capture one step of the whole batch
   if (b->graph) {
@@ -1305,9 +1286,9 @@ afar_status batch_build(afar_batch* b) {
   for (int k = 0; k < 3; ++k) {
     if constexpr (P::id == PolicyMixed::id) {
       if (nfmax <= 3)
-        recon_kernel_batch<P, 3>()<<<b->ncb, kReconThreads, b->smem, b->stream>>>(t, b->cmap);
+        kb_reconstruct_tile<P, 3><<<b->ncb, kTile, b->smem, b->stream>>>(t, b->cmap);
       else
-        recon_kernel_batch<P, 4>()<<<b->ncb, kReconThreads, b->smem, b->stream>>>(t, b->cmap);
+        kb_reconstruct_tile<P, 4><<<b->ncb, kTile, b->smem, b->stream>>>(t, b->cmap);
     } else
       kb_reconstruct_staged<P><<<b->ncb, kCellBlock, b->smem, b->stream>>>(t, b->cmap);
     kb_bvd<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap);
