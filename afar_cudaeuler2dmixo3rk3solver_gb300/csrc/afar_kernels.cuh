@@ -1323,6 +1323,39 @@ __global__ void __launch_bounds__(256) k_delta_t(StageArgs<P> a, double CFL, uns
   if ((threadIdx.x & 31) == 0) atomicMin(bits, v);
 }
 
+// The Courant step of the mixed policy for afar_adjustTimeStep: the FP32 estimate of its fused
+// stage-1 flux (same expression), warp minimum on the float bits, one atomicMin per warp on the
+// double's bits.  No FP64 arithmetic per face.
+__global__ void __launch_bounds__(256) k_delta_t_mixed(StageArgs<PolicyMixed> a, const float cfl,
+                                                       unsigned long long* bits) {
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  float dtf = 1e5f;
+  if (id < a.Nf) {
+    const int2 on = a.on[id];
+    const V4<float> Wo = a.W[on.x], Wn = a.W[on.y];
+    const V4<float> fs = a.fs[id];
+    const float Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
+    const V2<float> g = a.dtgf[id];
+    const float deltaR = g.x, fraction = g.y;
+    dtf = cfl * deltaR * magSf /
+          ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
+           sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+  }
+  unsigned v = (unsigned)__float_as_int(dtf);
+  if (!(dtf >= 0.f)) v = 0x7F800000u;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned u = __shfl_xor_sync(0xffffffffu, v, o);
+    v = u < v ? u : v;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    const unsigned long long b = v >= 0x7F800000u
+                                     ? 0x7FF0000000000000ull
+                                     : (unsigned long long)__double_as_longlong((double)__int_as_float((int)v));
+    atomicMin(bits, b);
+  }
+}
+
 // ---------------------------------------------------------------------------------- setup kernels
 
 // calcLeastSquareMatrix (reference cudaFieldOperation.h:91-120) into the slot-major matrix, in

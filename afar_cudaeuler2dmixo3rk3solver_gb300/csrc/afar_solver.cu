@@ -837,11 +837,10 @@ extern "C" afar_status afar_adjustTimeStep(afar_solver* s, int facesNum, double 
         k_delta_t<PolicyFP64><<<gf, kFaceBlock, 0, s->stream>>>(a, CFL, s->dt_bits, nullptr);
         break;
       }
-      default: {
+      default: {  // the mixed policy's FP32 Courant estimate, as in its fused stage-1 flux
         StageArgs<PolicyMixed> a = make_args<PolicyMixed>(s);
-        a.R = R;
-        a.Cv = Cv;
-        k_delta_t<PolicyMixed><<<gf, kFaceBlock, 0, s->stream>>>(a, CFL, s->dt_bits, nullptr);
+        a.gRf = (float)((R / Cv + 1.0) * R);
+        k_delta_t_mixed<<<gf, kFaceBlock, 0, s->stream>>>(a, (float)CFL, s->dt_bits);
         break;
       }
     }

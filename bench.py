@@ -4,7 +4,7 @@
 Workload (one GPU): channel [0,3]x[0,1] with the step [0.6,3]x[0,0.2] removed, Delaunay
 triangulation of ~1M seeded jittered points (jitter 0.3h), RCM-renumbered: about 2.0M triangles,
 3.0M internal faces.  Inflow rho=1.4, p=1, u=3 (label 3), slip walls (label 2), outflow (label 4),
-edge-neighbour stencils, R = 1/1.4, Cv = R/0.4, CFL 0.3, device-side CFL step every step.
+edge-neighbour stencils, R = 1/1.4, Cv = R/0.4, CFL 0.2, device-side CFL step every step.
 Synthetic, seeded inputs; the working set (~1.5 GB) is larger than L2, so no L2 flush is needed.
 
 Our arm (default): K timed steps per precision policy, graph-replayed, CUDA events on the solver's
@@ -36,6 +36,11 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-RK3-steps/s"
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+PROFILE_STEPS = 10
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one mixed-policy reconstruct launch
+# per cell, from an ncu capture of the 500,094-cell version of this workload (traffic grows with
+# the cells of the tile stream); None when no capture matches the current kernels.
+RECON_TRAFFIC_BYTES_PER_CELL = 430.0
 
 
 def parse():
@@ -183,6 +188,25 @@ def algorithmic_bytes_per_step(hf, policy: str) -> float:
     return 3.0 * (cells + faces + bfaces) + hf.nc * (4 * wW + 16) + 48.0 * hf.nf
 
 
+def reconstruct_bytes_per_launch(hf, policy: str) -> float:
+    """Compulsory bytes of one reconstruct launch: its inputs read once and its outputs written once.
+      per cell: W (4 wW), LS rows (2 m wO), stencil ids (4 S), face ids (4 m), counts (2), face
+                geometry (2 x 2 words per face slot, 4 m wG), gradient out (8 wG), limiter out
+                (4 wS), troubled flag out (1)
+      per internal face: O3 weights of both sides ((S_own+1 + S_nei+1) wO), face values out (8 wG)
+    wG = gradient/face-value word, wS = limiter word (4 for mixed, else 8 and 4/8)."""
+    wW = 4 if policy == "mixed" else 8
+    wO = 8 if policy == "fp64" else 4
+    wG = 4 if policy == "mixed" else 8
+    wS = 8 if policy == "fp64" else 4
+    S = hf.stencilSize.astype(np.float64)
+    m = hf.compactStencilSize.astype(np.float64)
+    nb = hf.neighbour.reshape(-1, 2)
+    cells = np.sum(4 * wW + 2 * m * wO + 4 * S + 4 * m + 2 + 4 * m * wG + 8 * wG + 4 * wS + 1)
+    faces = np.sum((S[nb[:, 0]] + 1 + S[nb[:, 1]] + 1) * wO + 8 * wG)
+    return float(cells + faces)
+
+
 def peaks():
     try:
         with open(PEAKS_FILE) as f:
@@ -193,9 +217,10 @@ def peaks():
 
 
 # ------------------------------------------------------------------------------------ arms
-def cpu_oracle_rate(hf, cfg, target_s: float = 10.0, max_steps: int = 20, policy="ref"):
+def cpu_oracle_rate(hf, cfg, target_s: float = 10.0, max_steps: int = 100, policy="ref"):
     """The oracle (the reference's algorithm restated in C) on all host cores: cell-steps/s over a
-    bounded sample of about target_s seconds (whole RK3 steps of the full mesh)."""
+    bounded sample of about target_s seconds (whole RK3 steps of the full mesh; at most max_steps,
+    well inside the ~180 steps this start-up runs before its corner breaks down at CFL 0.2)."""
     from oracle.oracle import Oracle, max_threads
 
     o = Oracle(hf, cfg.R, cfg.Cv, policy)
@@ -220,7 +245,7 @@ def run_reference_arm(args, dist: Dist):
 
     b.build_all()
     m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl)
-    rate, cores, el, steps = cpu_oracle_rate(hf, cfg, target_s=20.0, max_steps=max(2, args.steps))
+    rate, cores, el, steps = cpu_oracle_rate(hf, cfg, target_s=20.0, max_steps=min(120, max(2, args.steps)))
     sample = (f"{steps} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle (ref policy), "
               f"{el:.1f} s")
     line = {
@@ -302,8 +327,13 @@ def run_ours(args, dist: Dist):
     for pol in policies:
         s = solvers[pol]
         s.restore()
-        prof = s.profile_step()
-        results[pol]["kernels_ms"] = prof
+        # per-kernel device time: CUDA events between the stage kernels on the solver's stream,
+        # averaged over PROFILE_STEPS steps from the post-warm-up state
+        acc = {}
+        for _ in range(PROFILE_STEPS):
+            for k, v in s.profile_step().items():
+                acc[k] = acc.get(k, 0.0) + v / PROFILE_STEPS
+        results[pol]["kernels_ms"] = acc
         results[pol]["device_bytes"] = s.device_bytes()
 
     # e2e through the reference-shaped C ABI with host buffers (mixed policy)
@@ -360,10 +390,16 @@ def run_ours(args, dist: Dist):
     ms_step = head["ms"] / K
     value = n * hf.nc * K / (head["ms"] * 1e-3)
     bstep = algorithmic_bytes_per_step(hf, pol0)
-    achieved = bstep / (ms_step * 1e-3) / 1e9
+    step_gbps = bstep / (ms_step * 1e-3) / 1e9
     prof = head["kernels_ms"]
     tot = sum(prof.values())
     dom = max(prof, key=prof.get)
+    # the dominant kernel (reconstruct, three launches per step)
+    b_launch = reconstruct_bytes_per_launch(hf, pol0)
+    t_launch = prof["reconstruct"] / 3.0
+    achieved = b_launch / (t_launch * 1e-3) / 1e9
+    traffic = (RECON_TRAFFIC_BYTES_PER_CELL * hf.nc
+               if RECON_TRAFFIC_BYTES_PER_CELL is not None and pol0 == "mixed" else None)
     by_policy = {}
     for pol in policies:
         r = results[pol]
@@ -386,9 +422,10 @@ def run_ours(args, dist: Dist):
                    "timed_chunks": chunks, "chunk_start": f"state after {Wm} warm-up steps (device snapshot)",
                    "setup_s": round(setup_s, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_kind": peak_kind,
-                     "granularity": "one RK3 step (one CUDA-graph launch of all stage kernels)",
-                     "dominant_kernel": dom, "dominant_share": prof[dom] / tot if tot else None},
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "reconstruct (mixed, tile-staged)",
+                     "algorithmic_bytes_per_launch": b_launch, "launch_ms": t_launch,
+                     "dominant_kernel": dom, "dominant_share": prof[dom] / tot if tot else None,
+                     "step": {"algorithmic_bytes": bstep, "achieved_GBps": step_gbps, "frac": step_gbps / hbm}},
         "clocks": clocks,
         "gpu_launches": K * head["launches"] + 1,
         "e2e": {"value": n * hf.nc * K / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": int(h2d),
