@@ -105,6 +105,7 @@ def lib():
             "afar_device_bytes": (S, [_p, C.POINTER(C.c_size_t)]),
             "afar_launches_per_step": (C.c_int, [_p]),
             "afar_set_step_params": (S, [_p, C.c_double, C.c_double, C.c_double]),
+            "afar_set_write_interval": (S, [_p, C.c_double]),
             "afar_batch_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),
             "afar_batch_add": (S, [_p, _p]),
             "afar_batch_remove": (S, [_p, _p]),
@@ -141,6 +142,6 @@ EXPORTED = [
     "afar_set_time", "afar_stage_debug", "afar_debug_limiter64", "afar_upload_state", "afar_download_state",
     "afar_download_ls_matrix", "afar_device_bytes", "afar_launches_per_step", "afar_run_timed",
     "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc", "afar_set_step_params",
-    "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
+    "afar_set_write_interval", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
     "afar_batch_destroy",
 ]

@@ -29,11 +29,24 @@ struct StepCtl {
   double last_dt;
   long long steps;
   unsigned err;  // bit 0: a bounded device wait gave up (the stage's results are not valid)
+  double write_interval;  // > 0: land on its multiples like OpenFOAM's adjustableRunTime
+  long long write_index;  // write times passed
 };
 
-// The step of the current RK step: fixed or CFL, clipped to t_end; <= 0 means "no step".
+// The step of the current RK step: fixed or CFL, spread over the steps left to the next write time
+// when write times are set, clipped to t_end; <= 0 means "no step".  The write-time rule is
+// OpenFOAM's Time::adjustDeltaT for writeControl adjustableRunTime (the reference application
+// sets each step with runTime.setDeltaT, cudaEuler2DmixO3RK3solver.cpp:44-48): with r the time to
+// the next write, n = floor(r/dt - small) + 1 steps of r/n, the change held within [dt/5, 2 dt].
 __device__ __forceinline__ double step_dt(const StepCtl* c) {
   double dt = c->dt_fixed > 0.0 ? c->dt_fixed : __longlong_as_double((long long)c->dt_bits);
+  if (c->write_interval > 0.0) {
+    const double r = (double)(c->write_index + 1) * c->write_interval - c->t;
+    if (r > 0.0) {
+      const double nd = r / (floor(r / dt - 1e-15) + 1.0);
+      dt = nd >= dt ? fmin(nd, 2.0 * dt) : fmax(nd, 0.2 * dt);
+    }
+  }
   if (c->t_end > 0.0) dt = fmin(dt, c->t_end - c->t);
   return dt;
 }
@@ -1276,6 +1289,9 @@ __device__ __forceinline__ void finish_one(StepCtl* ctl) {
     ctl->t += dt;
     ctl->steps += 1;
     ctl->last_dt = dt;
+    if (ctl->write_interval > 0.0)  // passed a write time (within rounding): aim at the next one
+      for (int k = 0; k < 4 && ctl->t >= (double)(ctl->write_index + 1) * ctl->write_interval * (1.0 - 1e-12); ++k)
+        ctl->write_index += 1;
   }
   ctl->dt_bits = (unsigned long long)__double_as_longlong(1e5);
 }

@@ -81,6 +81,13 @@ __global__ void k_setup_wts(int Nc, int Nf, int ldc, int maxS, const uint8_t* nS
   }
 }
 
+__global__ void k_set_write_interval(StepCtl* ctl, double interval) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    ctl->write_interval = interval;
+    ctl->write_index = interval > 0.0 ? (long long)floor(ctl->t / interval * (1.0 + 1e-12)) : 0;
+  }
+}
+
 __global__ void k_set_ctl(StepCtl* ctl, double dt_fixed, double cfl, double t_end) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     ctl->dt_fixed = dt_fixed;
@@ -99,6 +106,8 @@ __global__ void k_init_ctl(StepCtl* ctl) {
     ctl->last_dt = 0.0;
     ctl->steps = 0;
     ctl->err = 0;
+    ctl->write_interval = 0.0;
+    ctl->write_index = 0;
   }
 }
 
@@ -1201,6 +1210,16 @@ extern "C" afar_status afar_set_step_params(afar_solver* s, double dt, double CF
   if (st) return st;
   if (!(dt > 0.0) && !(CFL > 0.0)) return (set_error("afar_set_step_params: deltaT or CFL must be positive"), AFAR_ERR_ARGUMENT);
   k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, tEnd);
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_set_write_interval(afar_solver* s, double writeInterval) {
+  if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  if (!(writeInterval >= 0.0)) return (set_error("afar_set_write_interval: negative interval"), AFAR_ERR_ARGUMENT);
+  AFAR_CUDA(cudaSetDevice(s->device));
+  k_set_write_interval<<<1, 32, 0, s->stream>>>(s->ctl, writeInterval);
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaGetLastError());
   return AFAR_OK;

@@ -309,6 +309,10 @@ class CudaSolver:
         cfl = self.cfg.CFL if cfl is None else cfl
         check(lib().afar_set_step_params(self.h, dt, cfl, t_end))
 
+    def set_write_interval(self, interval: float):
+        """Land graph-replayed steps on multiples of ``interval`` (OpenFOAM adjustableRunTime); 0: off."""
+        check(lib().afar_set_write_interval(self.h, interval))
+
     def device_bytes(self) -> int:
         b = C.c_size_t()
         check(lib().afar_device_bytes(self.h, C.byref(b)))

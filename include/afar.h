@@ -285,6 +285,14 @@ afar_status afar_download_state(afar_solver* solver, afar_basicFieldData* FD,
  * the device CFL step, and an end time (<= 0: none). */
 afar_status afar_set_step_params(afar_solver* solver, double deltaT, double CFL, double tEnd);
 
+/* Write-time landing for graph-replayed steps (afar_run, afar_run_async, batches): with
+ * writeInterval > 0 the step size of each step is spread over the steps left to the next multiple
+ * of writeInterval, as OpenFOAM's Time does for writeControl adjustableRunTime after the reference
+ * application's runTime.setDeltaT (cudaEuler2DmixO3RK3solver.cpp:44-48; the rule: with r the time
+ * to the next write, n = floor(r/dt - 1e-15) + 1 steps of r/n, held within [dt/5, 2 dt]).  Run
+ * with tEnd at the write time to stop there.  0 switches it off. */
+afar_status afar_set_write_interval(afar_solver* solver, double writeInterval);
+
 /* ---- batches: many independent solves stepped by the same kernel launches ------------------- */
 /* A batch steps all of its member solvers with one launch per stage kernel (13 per RK3 step,
  * replayed as one CUDA graph): every block works on one member, so meshes of uneven size share the

@@ -1,0 +1,91 @@
+"""OpenFOAM case handling (no GPU): dictionary parsing, the 2-D blockMesh, the initial fields and
+the OpenFOAM ascii writers."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from foam_case import write_case
+
+
+def test_parse_dictionary_forms():
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    d = foam.parse_foam("""/* block */ a 1; b 2.5e-3; // line
+    c { d word; e (1 2 (3 4)); } f uniform (4.5 0 0); g [0 1 -1 0 0 0 0]; h "quoted text";""")
+    assert d["a"] == 1 and d["b"] == 2.5e-3
+    assert d["c"]["d"] == "word" and d["c"]["e"] == [1, 2, [3, 4]]
+    assert d["f"] == ["uniform", [4.5, 0, 0]]
+    assert d["g"] == [0, 1, -1, 0, 0, 0, 0] and d["h"] == "quoted text"
+    with pytest.raises(ValueError):
+        foam.parse_foam("#include \"other\"")
+
+
+def test_forward_step_case_mesh_and_fields(tmp_path):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam, precompute
+
+    case = foam.load_case(write_case(str(tmp_path), n=2))
+    m = case.mesh
+    assert m.n_cells == 6 * 2 + 6 * 8 + 24 * 8
+    names = [p[0] for p in m.patches]
+    labels = {p[0]: p[1] for p in m.patches}
+    sizes = {p[0]: p[3] for p in m.patches}
+    assert names == ["inflow", "outflow", "walls"] and labels == {"inflow": 3, "outflow": 4, "walls": 2}
+    assert sizes == {"inflow": 2 + 8, "outflow": 8, "walls": 6 + 2 + 24 + 6 + 24}
+    assert np.isclose(m.cell_areas().sum(), 3.0 - 2.4 * 0.2)
+    assert case.config.cOrder == 5 and case.config.fOrder == 4 and case.config.CFL == 0.2
+    assert case.adjust_time_step and case.end_time == 0.02 and case.write_interval == 0.005
+    assert np.allclose(case.W, [1.0, 3.0, 0.0, 1.0])
+    assert np.allclose(case.Wb, [1.0, 3.0, 0.0, 1.0])
+    hf = precompute(m, case.config, case.W, case.Wb)  # the native precompute accepts the mesh
+    assert hf.nc == m.n_cells
+
+
+def test_grading_and_orientation(tmp_path):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    x = foam._grading(4, 8.0)
+    d = np.diff(x)
+    assert np.isclose(x[-1], 1.0) and np.isclose(d[-1] / d[0], 8.0)
+    m = foam.load_case(write_case(str(tmp_path), n=1)).mesh
+    assert (m.cell_areas() > 0).all()
+
+
+def test_writers_round_trip(tmp_path):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    case = foam.load_case(write_case(str(tmp_path / "case"), n=2))
+    m = case.mesh
+    out = str(tmp_path / "out")
+    foam.write_poly_mesh(out, m)
+    rng = np.random.default_rng(2)
+    FD = rng.uniform(0.5, 2.0, (m.n_cells + m.n_boundary_faces, 4))
+    flags = np.zeros(2 * (m.n_cells + m.n_boundary_faces), dtype=np.int8)
+    flags[1::2] = rng.integers(-2, 2, flags[1::2].shape[0])
+    d = foam.write_fields(out, 0.005, m, FD, flags)
+    assert os.path.basename(d) == "0.005"
+    assert np.allclose(foam.read_field(os.path.join(d, "p")), FD[:m.n_cells, 0], rtol=1e-8)
+    U = foam.read_field(os.path.join(d, "U"))
+    assert np.allclose(U[:, :2], FD[:m.n_cells, 1:3], rtol=1e-8) and np.all(U[:, 2] == 0)
+    assert np.array_equal(foam.read_field(os.path.join(d, "shockIndicator")), flags[1:2 * m.n_cells:2])
+    faces = foam.read_foam(os.path.join(out, "constant", "polyMesh", "boundary"))
+    poly = os.path.join(out, "constant", "polyMesh")
+    owner = open(os.path.join(poly, "owner")).read()
+    assert f"\n{m.n_faces + 2 * m.n_cells}\n(" in owner
+    assert "defaultFaces" in open(os.path.join(poly, "boundary")).read() and faces is not None
+
+
+REF_CASE = "/root/reference/simulation/cornerFlow/cornerFlow_cuda"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="the reference's case files are not on this machine")
+def test_reference_corner_flow_case_loads():
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    case = foam.load_case(REF_CASE)
+    m = case.mesh
+    assert m.n_cells == 250000
+    assert [(p[0], p[1], p[3]) for p in m.patches] == [("inlet", 5, 250), ("obstacle", 2, 1250), ("outlet", 4, 500)]
+    assert case.config.cOrder == 7 and case.config.fOrder == 5 and case.config.stencilType == "edgeNeighbour"
+    assert case.end_time == 0.15 and case.write_interval == 0.01 and case.max_co == 0.3

@@ -1,0 +1,62 @@
+"""A reference-style OpenFOAM case run on the GPU (the reference application's time loop): the
+forward-step case written by the tests, stepped to endTime with the device CFL step, landing on
+every write time like OpenFOAM's adjustableRunTime, fields written in OpenFOAM format."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import gpu_available
+from foam_case import write_case
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def need_gpu():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+
+
+def test_run_case_writes_every_write_time(tmp_path):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    case_dir = write_case(str(tmp_path / "case"), n=4, end=0.02, wi=0.005)
+    out = str(tmp_path / "out")
+    res = foam.run_case(case_dir, out, policy="mixed")
+    assert res["write_times"] == pytest.approx([0.005, 0.01, 0.015, 0.02])
+    assert res["time"] == pytest.approx(0.02, rel=1e-12) and res["steps"] > 4
+    for t in ("0", "0.005", "0.01", "0.015", "0.02"):
+        p = foam.read_field(os.path.join(out, t, "p"))
+        assert p.shape == (res["cells"],) and np.isfinite(p).all() and (p > 0).all()
+    assert os.path.exists(os.path.join(out, "constant", "polyMesh", "faces"))
+
+
+def test_write_interval_spreads_the_steps_to_the_write_time(tmp_path):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver, foam, precompute
+
+    case = foam.load_case(write_case(str(tmp_path / "case"), n=4))
+    hf = precompute(case.mesh, case.config, case.W, case.Wb)
+    wi = 0.003
+    for landing in (False, True):
+        s = CudaSolver(hf, case.config, policy="fp64")
+        if landing:
+            s.set_write_interval(wi)
+        dts = []
+        t_prev = 0.0
+        for _ in range(500):
+            s.run(1, t_end=wi)
+            t, last, n = s.time()
+            if t <= t_prev:
+                break
+            dts.append(t - t_prev)
+            t_prev = t
+        s.close()
+        assert t == pytest.approx(wi, rel=1e-12)
+        if landing:
+            # OpenFOAM's rule spreads the remainder: no step is cut to a sliver at the write time
+            assert min(dts) >= 0.2 * max(dts)
+            assert dts[-1] == pytest.approx(dts[-2], rel=0.2)
+        else:
+            plain = dts
+    assert len(dts) <= len(plain) + 1
