@@ -6,6 +6,6 @@ generators used by the tests and the benchmark.
 """
 from . import mesh  # noqa: F401
 from ._ffi import AfarError, lib  # noqa: F401
-from .solver import Batch, CaseConfig, CudaSolver, HostFields, gauss_quadrature, precompute  # noqa: F401
+from .solver import Batch, CaseConfig, Server, CudaSolver, HostFields, gauss_quadrature, precompute  # noqa: F401
 
-__all__ = ["Batch", "mesh", "lib", "AfarError", "CaseConfig", "CudaSolver", "HostFields", "precompute", "gauss_quadrature"]
+__all__ = ["Batch", "Server", "mesh", "lib", "AfarError", "CaseConfig", "CudaSolver", "HostFields", "precompute", "gauss_quadrature"]

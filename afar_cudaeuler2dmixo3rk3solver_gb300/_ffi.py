@@ -53,6 +53,20 @@ class CaseConfig(C.Structure):
     ]
 
 
+class Request(C.Structure):
+    """afar_request: one solve for afar_server_submit."""
+    _fields_ = [("host", C.POINTER(FieldPointer)), ("sizes", FieldSizes), ("RBFbasis64", _p),
+                ("RBFbasis64Count", C.c_size_t), ("R", C.c_double), ("Cv", C.c_double), ("CFL", C.c_double),
+                ("tEnd", C.c_double), ("nSteps", C.c_int), ("outFD", _p), ("outShockIndicator", _p)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("submitted", "completed", "failed", "queued", "running",
+                                             "peakRunning")] + [
+        ("bytesInUse", C.c_size_t), ("peakBytes", C.c_size_t), ("budgetBytes", C.c_size_t),
+        ("batchSteps", C.c_longlong)]
+
+
 class AfarError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"afar status {status}: {msg}")
@@ -106,6 +120,12 @@ def lib():
             "afar_launches_per_step": (C.c_int, [_p]),
             "afar_set_step_params": (S, [_p, C.c_double, C.c_double, C.c_double]),
             "afar_set_write_interval": (S, [_p, C.c_double]),
+            "afar_server_create": (S, [C.POINTER(_p), C.c_int, C.c_int, C.c_size_t, C.c_int]),
+            "afar_server_submit": (S, [_p, C.POINTER(Request), C.POINTER(C.c_longlong)]),
+            "afar_server_wait": (S, [_p, C.c_longlong, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double)]),
+            "afar_server_get_stats": (S, [_p, C.POINTER(ServerStats)]),
+            "afar_server_destroy": (S, [_p]),
             "afar_batch_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),
             "afar_batch_add": (S, [_p, _p]),
             "afar_batch_remove": (S, [_p, _p]),
@@ -143,5 +163,6 @@ EXPORTED = [
     "afar_download_ls_matrix", "afar_device_bytes", "afar_launches_per_step", "afar_run_timed",
     "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc", "afar_set_step_params",
     "afar_set_write_interval", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
-    "afar_batch_destroy",
+    "afar_batch_destroy", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
+    "afar_server_destroy",
 ]

@@ -57,6 +57,7 @@ def build_lib(force=False, verbose=False) -> str:
         ("afar_noalloc.cu", "nvcc"),
         ("afar_precompute.cpp", "cxx"),
         ("afar_error.cpp", "cxx"),
+        ("afar_server.cpp", "cxx"),
     ]
     nvcc = _nvcc()
     jobs = []
@@ -77,7 +78,7 @@ def build_lib(force=False, verbose=False) -> str:
         for o in outs:
             sys.stdout.write(o)
     if force or jobs or _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs + ["-lgomp"])
+        _run([nvcc] + ARCH + ["-shared", "-Xcompiler", "-fopenmp", "-o", LIB] + objs + ["-lgomp", "-lpthread"])
     return LIB
 
 

@@ -371,3 +371,63 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class Server:
+    """A queue of solves served on one GPU under a device-memory budget (afar_server_*): requests
+    wait until their estimated memory fits beside the running ones, run together as one batch in
+    chunks of ``chunk_steps`` steps, and are retired (fields copied out, memory freed) when they
+    reach their end time or step count."""
+
+    def __init__(self, policy="mixed", device=0, hbm_budget_bytes=180 << 30, chunk_steps=50):
+        self.h = C.c_void_p()
+        self._keep = {}
+        check(lib().afar_server_create(C.byref(self.h), _ffi.POLICIES[policy], device, int(hbm_budget_bytes),
+                                       int(chunk_steps)))
+        self.policy = policy
+
+    def submit(self, fields: HostFields, cfg: CaseConfig, t_end: float = 0.0, n_steps: int = 0) -> int:
+        fp = fields.to_c()
+        out_FD = np.zeros((fields.nc + fields.nb, 4))
+        out_si = np.zeros(2 * (fields.nc + fields.nb), dtype=np.int8)
+        r = _ffi.Request()
+        r.host = C.pointer(fp)
+        for k, v in fields.sizes.items():
+            setattr(r.sizes, k, int(v))
+        r64 = fields.a.get("RBFbasis64") if self.policy == "fp64" else None
+        if r64 is not None:
+            r.RBFbasis64 = ptr(r64)
+            r.RBFbasis64Count = r64.shape[0]
+        r.R, r.Cv, r.CFL, r.tEnd, r.nSteps = cfg.R, cfg.Cv, cfg.CFL, t_end, n_steps
+        r.outFD = ptr(out_FD)
+        r.outShockIndicator = ptr(out_si)
+        rid = C.c_longlong()
+        check(lib().afar_server_submit(self.h, C.byref(r), C.byref(rid)))
+        self._keep[rid.value] = (fields, fp, r, out_FD, out_si)  # alive until the request is done
+        return rid.value
+
+    def wait(self, rid: int, timeout: float = -1.0):
+        """(FD, shock indicator, latency ms) once the request is done; None on timeout."""
+        done, status, lat = C.c_int(), C.c_int(), C.c_double()
+        check(lib().afar_server_wait(self.h, rid, timeout, C.byref(done), C.byref(status), C.byref(lat)))
+        if not done.value:
+            return None
+        check(status.value)
+        _, _, _, out_FD, out_si = self._keep.pop(rid)
+        return out_FD, out_si, lat.value
+
+    def stats(self) -> dict:
+        st = _ffi.ServerStats()
+        check(lib().afar_server_get_stats(self.h, C.byref(st)))
+        return {n: getattr(st, n) for n, _ in st._fields_}
+
+    def close(self):
+        if self.h:
+            lib().afar_server_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

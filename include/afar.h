@@ -314,6 +314,43 @@ afar_status afar_batch_size(afar_batch* batch, int* members);
 afar_status afar_batch_run(afar_batch* batch, int nSteps, float* ms);
 afar_status afar_batch_destroy(afar_batch* batch);
 
+/* ---- serving: a queue of solve requests on one GPU under a device-memory budget --------------- */
+/* No counterpart in the reference (it runs one case per process).  A server owns a worker thread
+ * that admits queued requests while their estimated device memory fits the budget (at least one
+ * at a time, whatever its size), builds a solver for each, steps all admitted solves together as
+ * one batch (afar_batch_*) in chunks of chunkSteps RK3 steps, and retires each solve when it
+ * reaches its end time or step count: its fields are copied into the request's output buffers and
+ * its device memory is freed.  Policies fp64 and mixed. */
+typedef struct afar_server afar_server;
+typedef struct {
+  const afar_fieldPointer* host; /* precomputed host fields (afar_precompute_fields); they and */
+  afar_fieldSizes sizes;         /* the output buffers must stay valid until the request is done */
+  const double* RBFbasis64;      /* fp64 policy: the FP64 O3 weights (may be NULL), count below */
+  size_t RBFbasis64Count;
+  double R, Cv, CFL;
+  double tEnd;                   /* > 0: step to this simulated time */
+  int nSteps;                    /* > 0: at most this many steps (both may be set) */
+  afar_basicFieldData* outFD;    /* cellsNum + totalBoundaryFacesNum states, written when done */
+  int8_t* outShockIndicator;     /* 2 (cellsNum + totalBoundaryFacesNum), may be NULL */
+} afar_request;
+typedef struct {
+  long long submitted, completed, failed, queued, running;
+  long long peakRunning;
+  size_t bytesInUse, peakBytes, budgetBytes;
+  long long batchSteps;          /* steps of the batch so far (each steps every running member) */
+} afar_server_stats;
+afar_status afar_server_create(afar_server** server, int policy, int device, size_t hbmBudgetBytes,
+                               int chunkSteps);
+afar_status afar_server_submit(afar_server* server, const afar_request* request, long long* requestId);
+/* Waits up to timeoutSeconds (< 0: no limit) for the request.  *done = 1 when it has finished;
+ * then *requestStatus is its afar_status (an error message is available from afar_last_error on
+ * the calling thread) and *latencyMs the time from submit to completion. */
+afar_status afar_server_wait(afar_server* server, long long requestId, double timeoutSeconds, int* done,
+                             int* requestStatus, double* latencyMs);
+afar_status afar_server_get_stats(afar_server* server, afar_server_stats* stats);
+/* Finishes the running and queued requests, then stops the worker. */
+afar_status afar_server_destroy(afar_server* server);
+
 /* In-device checkpoint of the whole solver state (primitive + conserved fields, RK stage start,
  * time and step count): op 0 saves, op 1 restores (bit-exact resume).  The snapshot lives in
  * device memory next to the state; restore without a prior save is an error. */

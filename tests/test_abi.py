@@ -119,3 +119,17 @@ def test_stencil_limit_is_enforced():
         precompute(m, CaseConfig(stencilType="edgeNeighbour"), W, Wb)
     hf = precompute(m, CaseConfig(stencilType="faceNeighbour"), W, Wb)
     assert hf.sizes["maxStencilSize"] <= 20
+
+
+def test_server_rejects_bad_arguments_without_a_gpu():
+    import ctypes as C
+
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import _ffi
+
+    L = _ffi.lib()
+    h = C.c_void_p()
+    assert L.afar_server_create(C.byref(h), 0, 0, 1 << 30, 50) == 1  # the ref policy is not served
+    assert L.afar_server_create(C.byref(h), 2, 0, 1 << 30, 0) == 1   # chunk of 0 steps
+    assert L.afar_server_submit(None, None, None) == 1
+    assert L.afar_server_get_stats(None, None) == 1
+    assert L.afar_server_destroy(None) == 0

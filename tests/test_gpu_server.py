@@ -1,0 +1,89 @@
+"""The serving queue (afar_server_*): requests of different meshes, end times and step counts,
+admitted under a device-memory budget and run together as one batch.  Each result must be bitwise
+the one the same solve reaches stepped in a batch of its own (a member's result does not depend on
+the other members), and the budget must bound how many run at once."""
+import numpy as np
+import pytest
+
+from conftest import gpu_available, small_cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cases():
+    if not gpu_available():
+        pytest.skip("no CUDA device")
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, precompute
+
+    out = {}
+    for name, (m, W, Wb, st) in small_cases().items():
+        if name == "corner_flow":
+            continue
+        cfg = CaseConfig(stencilType=st, CFL=0.2 if name == "ffs_tri" else 0.3)
+        out[name] = (precompute(m, cfg, W, Wb, want_rbf64=True), cfg)
+    return out
+
+
+def _alone(hf, cfg, policy, t_end, n_steps):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch, CudaSolver
+
+    s = CudaSolver(hf, cfg, policy=policy)
+    s.set_step_params(cfl=cfg.CFL, t_end=t_end)
+    b = Batch(policy)
+    b.add(s)
+    if n_steps:
+        b.run(n_steps)
+    else:
+        while s.time()[0] < t_end * (1 - 1e-12):
+            b.run(10)
+    b.close()
+    st = s.state()
+    s.close()
+    return st
+
+
+REQS = [("quad_riemann", 0.02, 0), ("ffs_tri", 0.0, 7), ("mixed_riemann", 0.0, 12), ("quad_riemann", 0.0, 3)]
+
+
+@pytest.mark.parametrize("policy", ["mixed", "fp64"])
+def test_server_results_match_alone(cases, policy):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Server
+
+    srv = Server(policy, chunk_steps=5)
+    ids = [srv.submit(*cases[n], t_end=t, n_steps=k) for n, t, k in REQS]
+    for rid, (n, t, k) in zip(ids, REQS):
+        FD, si, lat = srv.wait(rid, timeout=120.0)
+        ref = _alone(*cases[n], policy, t, k)
+        assert np.array_equal(FD, ref["FD"]), n
+        assert np.array_equal(si, ref["shockIndicator"]), n
+        assert lat > 0
+    st = srv.stats()
+    assert st["completed"] == len(REQS) and st["failed"] == 0 and st["running"] == 0
+    assert st["peakRunning"] >= 2 and st["bytesInUse"] == 0
+    srv.close()
+
+
+def test_budget_admits_one_at_a_time(cases):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Server
+
+    srv = Server("mixed", hbm_budget_bytes=1, chunk_steps=4)  # every request is over budget alone
+    ids = [srv.submit(*cases[n], t_end=t, n_steps=k) for n, t, k in REQS]
+    for rid in ids:
+        assert srv.wait(rid, timeout=120.0) is not None
+    st = srv.stats()
+    assert st["peakRunning"] == 1 and st["completed"] == len(REQS)
+    srv.close()
+
+
+def test_destroy_finishes_queued_requests(cases):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Server
+
+    srv = Server("mixed", chunk_steps=3)
+    hf, cfg = cases["quad_riemann"]
+    ids = [srv.submit(hf, cfg, n_steps=6) for _ in range(3)]
+    keep = srv._keep
+    srv.close()  # waits for the worker, which finishes everything queued
+    for rid in ids:
+        FD = keep[rid][3]
+        assert np.isfinite(FD).all() and (FD[:, 0] > 0).all()
