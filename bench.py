@@ -57,6 +57,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--serve", action="store_true",
+                    help="the serving workload instead: Poisson arrivals of solves through afar_server_*")
+    ap.add_argument("--serve-requests", type=int, default=60)
+    ap.add_argument("--serve-rate", type=float, default=50.0, help="arrivals per second")
     return ap.parse_args()
 
 
@@ -439,11 +443,73 @@ def run_ours(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args, dist: Dist):
+    """Serving workload: requests arrive as a Poisson process (rate --serve-rate) with meshes drawn
+    log-uniformly from a pool of quad Riemann problems of 10k-300k cells and step counts uniform in
+    [20, 200]; each is submitted to one afar_server (mixed policy, 180 GB budget, 25-step chunks)
+    from host buffers and its latency runs from submit to its fields being back on the host.
+    Prints served cell-steps/s and latency percentiles.  The pool's precompute is outside the
+    timed region; request inputs are resident host arrays."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, Server, mesh, precompute
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+
+    b.build_all()  # with several ranks, each serves its own queue on its own GPU (replicas)
+    rng = np.random.default_rng(args.seed + 17 * dist.rank)
+    pool = []
+    for n in (100, 175, 316, 550):
+        m = mesh.quad_grid(n, n, 0.0, 1.2, 0.0, 1.0)
+        W, Wb = mesh.riemann_fields(m)
+        cfg = CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+        pool.append((precompute(m, cfg, W, Wb), cfg))
+    sizes = np.array([hf.nc for hf, _ in pool], dtype=np.float64)
+    logp = np.log(sizes)
+    nreq = args.serve_requests
+    pick = [int(np.argmin(np.abs(logp - rng.uniform(logp[0], logp[-1])))) for _ in range(nreq)]
+    steps = rng.integers(20, 201, nreq)
+    gaps = rng.exponential(1.0 / args.serve_rate, nreq)
+    srv = Server("mixed", device=dist.local, hbm_budget_bytes=180 << 30, chunk_steps=25)
+    warm = srv.submit(*pool[0], n_steps=5)
+    srv.wait(warm)
+    dist.barrier()
+    t0 = time.perf_counter()
+    ids = []
+    t_next = t0
+    for i in range(nreq):
+        t_next += gaps[i]
+        while time.perf_counter() < t_next:
+            time.sleep(min(1e-3, max(0.0, t_next - time.perf_counter())))
+        ids.append(srv.submit(*pool[pick[i]], n_steps=int(steps[i])))
+    lat = []
+    ok = True
+    for rid in ids:
+        FD, si, ms = srv.wait(rid)
+        lat.append(ms)
+        ok = ok and bool(np.isfinite(FD).all())
+    wall = dist.max(time.perf_counter() - t0)
+    st = srv.stats()
+    srv.close()
+    work = dist.sum(float(sum(sizes[pick[i]] * steps[i] for i in range(nreq))))
+    if dist.rank != 0:
+        return
+    lat = np.array(lat)
+    print(json.dumps({
+        "metric": "served cell-RK3-steps/s", "value": work / wall, "unit": "cell-steps/s", "n_gpus": dist.world,
+        "higher_is_better": True, "data": "synthetic (quad Riemann meshes 10k-300k cells, seeded)",
+        "config": {"workload": "serve_poisson", "requests": nreq, "rate_per_s": args.serve_rate,
+                   "steps": "U[20,200]", "policy": "mixed", "chunk_steps": 25, "budget_bytes": 180 << 30},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max())},
+        "wall_s": wall, "peak_running": st["peakRunning"], "peak_bytes": st["peakBytes"], "finite": ok,
+    }), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.serve:
+            run_serve(args, dist)
+        elif args.impl == "reference":
             run_reference_arm(args, dist)
         else:
             run_ours(args, dist)
