@@ -729,12 +729,17 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
   h->compactExtendStencilSize = xalloc<uint16_t>(nblk);
   std::vector<std::vector<int>> ext(nblk);
   int maxLB = 0, maxCLB = 0;
+  // membership of a cell id in the current block's halo list, in O(1): seen[id] == blk, at where[id]
+  int max_id = nc;
+  for (size_t k = 0; k < (size_t)maxS * nc; ++k) max_id = std::max(max_id, gsten[k] + 1);
+  std::vector<int> seen(max_id, -1), where(max_id, 0);
   for (int blk = 0; blk < nblk; ++blk) {
     std::vector<int>& e = ext[blk];
     auto outside = [&](int id) { return id < blk * BD || id > BD - 1 + blk * BD || id >= nc; };
-    auto add = [&](int id) {
-      for (int v : e)
-        if (v == id) return;
+    auto add = [&](int id) {  // first occurrence order, as the reference's list
+      if (seen[id] == blk) return;
+      seen[id] = blk;
+      where[id] = (int)e.size();
       e.push_back(id);
     };
     for (int t = 0; t < BD; ++t) {
@@ -769,7 +774,10 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
   h->extendStencil = xalloc<int>((size_t)(maxLB - BD) * nblk);
   for (int blk = 0; blk < nblk; ++blk) {
     const std::vector<int>& e = ext[blk];
-    for (size_t i = 0; i < e.size(); ++i) h->extendStencil[(size_t)(maxLB - BD) * blk + i] = e[i];
+    for (size_t i = 0; i < e.size(); ++i) {
+      h->extendStencil[(size_t)(maxLB - BD) * blk + i] = e[i];
+      where[e[i]] = (int)i;
+    }
     for (int t = 0; t < BD; ++t) {
       const int c = t + blk * BD;
       if (c >= nc) break;
@@ -778,9 +786,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
         const bool out = sid < blk * BD || sid > BD - 1 + blk * BD || sid >= nc;
         int loc;
         if (out) {
-          int ex = 0;
-          while (e[ex] != sid) ex++;
-          loc = BD + ex;
+          loc = BD + where[sid];
         } else {
           loc = sid - blk * BD;
         }
