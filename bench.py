@@ -57,6 +57,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--mesh", default="step", choices=["step", "riemann_mixed"],
+                    help="step: the metric's workload; riemann_mixed: the 4M-cell mixed quad/triangle case")
+    ap.add_argument("--mixed-n", type=int, default=1766)
     ap.add_argument("--serve", action="store_true",
                     help="the serving workload instead: Poisson arrivals of solves through afar_server_*")
     ap.add_argument("--serve-requests", type=int, default=60)
@@ -162,12 +165,26 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------------------------ workload
-def make_workload(points: int, seed: int, cfl: float):
+WORKLOADS = {
+    "step": ("mach3_forward_step_tri", "synthetic (seeded Delaunay mesh, uniform Mach 3 inflow)"),
+    "riemann_mixed": ("riemann4_mixed_quad_tri", "synthetic (quads with a seeded triangulated disk, four-quadrant "
+                                                   "Riemann states)"),
+}
+
+
+def make_workload(points: int, seed: int, cfl: float, kind: str = "step", mixed_n: int = 1766):
+    """step: the Mach 3 forward step (about points/2 x 4 triangles); riemann_mixed: the unit square
+    of mixed_n^2 quads with the cells of a central disk (r = 0.3) split into seeded triangles (about
+    4.0M cells at 1766), four-quadrant Riemann states, outlets all round."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
 
     t0 = time.time()
-    m = mesh.forward_step_triangles(points, seed=seed)
-    W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
+    if kind == "riemann_mixed":
+        m = mesh.riemann_mixed(mixed_n, seed=seed)
+        W, Wb = mesh.riemann_fields(m)
+    else:
+        m = mesh.forward_step_triangles(points, seed=seed)
+        W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
     cfg = CaseConfig(stencilType="edgeNeighbour", CFL=cfl)
     hf = precompute(m, cfg, W, Wb, want_rbf64=True)
     return m, hf, cfg, time.time() - t0
@@ -248,16 +265,16 @@ def run_reference_arm(args, dist: Dist):
     from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
 
     b.build_all()
-    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl)
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n)
     rate, cores, el, steps = cpu_oracle_rate(hf, cfg, target_s=20.0, max_steps=min(120, max(2, args.steps)))
     sample = (f"{steps} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle (ref policy), "
               f"{el:.1f} s")
     line = {
         "metric": METRIC, "value": rate, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": steps,
         "warmup": 1, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded Delaunay mesh, uniform Mach 3 inflow)",
+        "vs_baseline": None, "dtype": "f32+f64", "data": WORKLOADS[args.mesh][1],
         "impl": "reference",
-        "config": {"workload": "mach3_forward_step_tri", "cells": hf.nc, "internal_faces": hf.nf,
+        "config": {"workload": WORKLOADS[args.mesh][0], "cells": hf.nc, "internal_faces": hf.nf,
                    "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
                    "parallelism": "replicas"},
         "cpu_baseline": {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port", "sample": sample},
@@ -299,7 +316,7 @@ def run_ours(args, dist: Dist):
 
     b.build_all()
     device = dist.local
-    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl)
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n)
     K, Wm = args.steps, max(3, args.warmup)
     hbm, peak_kind = peaks()
     policies = [p for p in args.policies.split(",") if p]
@@ -418,8 +435,8 @@ def run_ours(args, dist: Dist):
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": n, "steps": K, "warmup": Wm,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if pol0 == "mixed" else "f64",
-        "data": "synthetic (seeded Delaunay mesh, uniform Mach 3 inflow)",
-        "config": {"workload": "mach3_forward_step_tri", "policy": pol0, "cells": hf.nc, "internal_faces": hf.nf,
+        "data": WORKLOADS[args.mesh][1],
+        "config": {"workload": WORKLOADS[args.mesh][0], "policy": pol0, "cells": hf.nc, "internal_faces": hf.nf,
                    "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
                    "max_stencil": hf.sizes["maxStencilSize"], "dt": "device CFL step every step",
                    "l2": "working set > L2 (no flush needed)", "parallelism": "replicas" if n > 1 else "single",
