@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--mixed-n", type=int, default=1766)
     ap.add_argument("--serve", action="store_true",
                     help="the serving workload instead: Poisson arrivals of solves through afar_server_*")
+    ap.add_argument("--batch", action="store_true",
+                    help="the batched workload instead: many independent solves stepped by one graph")
+    ap.add_argument("--batch-solves", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--serve-requests", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="arrivals per second")
     return ap.parse_args()
@@ -520,12 +524,78 @@ def run_serve(args, dist: Dist):
     }), flush=True)
 
 
+def run_batch(args, dist: Dist):
+    """Batched workload: --batch-solves independent solves, cells log-uniform in [5k, 200k]
+    (square quad meshes), each a uniform flow at Mach U[1.5, 4] carrying an isentropic vortex of
+    strength U[0, 5] through a box with outlets, mixed policy, CFL 0.3; all stepped together
+    --batch-steps RK3 steps by one afar_batch (13 launches per step for the whole batch).  Compared
+    with stepping the same solves one after another (afar_run_timed, a sample of 40 steps each)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch, CaseConfig, CudaSolver, mesh, precompute
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+
+    b.build_all()
+    rng = np.random.default_rng(args.seed + 31 * dist.rank)
+    t0 = time.time()
+    solvers, cells = [], []
+    for k in range(args.batch_solves):
+        nc = float(np.exp(rng.uniform(np.log(5e3), np.log(2e5))))
+        n = max(8, int(round(np.sqrt(nc))))
+        m = mesh.quad_grid(n, n, -5.0, 5.0, -5.0, 5.0)
+        mach = rng.uniform(1.5, 4.0)
+        W = mesh.vortex_fields(m.cell_centres(), strength=rng.uniform(0.0, 5.0), xc=0.0, yc=0.0,
+                               u0=mach * np.sqrt(1.4), v0=0.0)
+        Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.0, yc=0.0, u0=mach * np.sqrt(1.4),
+                                v0=0.0)
+        cfg = CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+        s = CudaSolver(precompute(m, cfg, W, Wb), cfg, policy="mixed", device=dist.local)
+        solvers.append(s)
+        cells.append(m.n_cells)
+    setup_s = time.time() - t0
+    cells = np.array(cells, dtype=np.float64)
+    # one after another: device time of 40 graph-replayed steps each, from the initial state
+    solo_ms = 0.0
+    for s in solvers:
+        s.save()
+        s.run_timed(3)
+        s.restore()
+        solo_ms += s.run_timed(40) / 40.0
+        s.restore()
+    batch = Batch("mixed", device=dist.local)
+    for s in solvers:
+        s.set_step_params()
+        batch.add(s)
+    batch.run(3)
+    for s in solvers:  # restore the initial states before the timed run
+        s.restore()
+    dist.barrier()
+    ms = dist.max(batch.run(args.batch_steps))
+    finite = all(bool(np.isfinite(s.state()["FD"]).all()) for s in solvers)
+    batch.close()
+    for s in solvers:
+        s.close()
+    total = dist.sum(float(cells.sum()))
+    if dist.rank != 0:
+        return
+    print(json.dumps({
+        "metric": "batched cell-RK3-steps/s", "value": total * args.batch_steps / (ms * 1e-3), "unit": "cell-steps/s",
+        "n_gpus": dist.world, "higher_is_better": True, "ms_per_step": ms / args.batch_steps,
+        "data": "synthetic (square quad meshes 5k-200k cells, Mach 1.5-4 flow with an isentropic vortex, seeded)",
+        "config": {"workload": "batch_vortex_quads", "solves": args.batch_solves, "cells": int(cells.sum()),
+                   "steps": args.batch_steps, "policy": "mixed", "launches_per_step": 13, "setup_s": round(setup_s, 1)},
+        "one_after_another": {"value": float(cells.sum()) / (solo_ms * 1e-3), "ms_per_step": solo_ms,
+                              "launches_per_step": 13 * args.batch_solves},
+        "finite": finite,
+    }), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
         if args.serve:
             run_serve(args, dist)
+        elif args.batch:
+            run_batch(args, dist)
         elif args.impl == "reference":
             run_reference_arm(args, dist)
         else:
