@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import ctypes as C
 import dataclasses
+import hashlib
+import os
 
 import numpy as np
 
@@ -42,6 +44,10 @@ class CaseConfig:
         return c
 
 
+SIZE_KEYS = ["cellsNum", "facesNum", "patchesNum", "totalBoundaryFacesNum", "maxStencilSize",
+             "maxCompactStencilSize", "maxLocalBlockStencilSize", "maxCompactLocalBlockStencilSize"]
+
+
 class HostFields:
     """The reference's host field bundle as numpy arrays plus its integer sizes."""
 
@@ -58,6 +64,17 @@ class HostFields:
     @property
     def nc(self):
         return self.sizes["cellsNum"]
+
+    def save(self, path: str):
+        """The whole bundle (operators, RBF weights, initial fields) in one .npz file."""
+        np.savez(path, __sizes__=np.array([self.sizes[k] for k in SIZE_KEYS], dtype=np.int64),
+                 **{f"a_{k}": v for k, v in self.a.items()})
+
+    @classmethod
+    def load(cls, path: str) -> "HostFields":
+        z = np.load(path)
+        sizes = dict(zip(SIZE_KEYS, (int(v) for v in z["__sizes__"])))
+        return cls(sizes, {k[2:]: np.ascontiguousarray(z[k]) for k in z.files if k.startswith("a_")})
 
     @property
     def nf(self):
@@ -143,8 +160,33 @@ def poly_mesh_c(mesh: FoamMesh):
     return m, keep
 
 
-def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_rbf64=False):
-    """Mesh + initial fields -> the reference's host field bundle (native precompute)."""
+def _cache_key(mesh: FoamMesh, cfg: CaseConfig, Wc, Wb, want_rbf64) -> str:
+    h = hashlib.sha256()
+    for a in (mesh.points, mesh.cell_ptr, mesh.cell_pts, mesh.face_pts, mesh.owner, mesh.neighbour, Wc,
+              np.zeros(0) if Wb is None else Wb):
+        a = np.ascontiguousarray(a)
+        h.update(str(a.dtype).encode() + str(a.shape).encode() + a.tobytes())
+    h.update(repr((mesh.patches, mesh.depth, dataclasses.astuple(cfg), bool(want_rbf64))).encode())
+    return h.hexdigest()[:32]
+
+
+def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_rbf64=False, cache_dir=None):
+    """Mesh + initial fields -> the reference's host field bundle (native precompute).
+
+    With ``cache_dir`` the bundle is kept on disk under a hash of every input and read back on the
+    next call with the same inputs, instead of recomputing the RBF pseudo-inverses and weights (the
+    role of the reference's basisOwnList/basisNeiList files and its ``recalcBasis`` switch,
+    basicCUDAsolver.cpp:626-694)."""
+    if cache_dir is not None:
+        path = os.path.join(cache_dir, f"afar_bundle_{_cache_key(mesh, cfg, W_cells, W_boundary, want_rbf64)}.npz")
+        if os.path.exists(path):
+            return HostFields.load(path)
+        hf = precompute(mesh, cfg, W_cells, W_boundary, want_rbf64)
+        os.makedirs(cache_dir, exist_ok=True)
+        tmp = path + f".{os.getpid()}.tmp.npz"
+        hf.save(tmp)
+        os.replace(tmp, path)
+        return hf
     m, keep = poly_mesh_c(mesh)
     Wc = np.ascontiguousarray(W_cells, dtype=np.float64)
     Wb = None if W_boundary is None else np.ascontiguousarray(W_boundary, dtype=np.float64)
@@ -308,6 +350,23 @@ class CudaSolver:
         """Step control used when this solver is stepped inside a Batch (fixed dt, or CFL; t_end clamps)."""
         cfl = self.cfg.CFL if cfl is None else cfl
         check(lib().afar_set_step_params(self.h, dt, cfl, t_end))
+
+    def write_checkpoint(self, path: str):
+        """The state on disk for a bit-exact restart: primitive fields with ghosts, conserved fields and
+        the simulated time, read between steps.  (The shock flags and the step's intermediates are
+        recomputed from these by the next step.)"""
+        st = self.state()
+        t, last, n = self.time()
+        np.savez(path, FD=st["FD"], cFD=st["cFD"], t=np.float64(t), last_dt=np.float64(last), steps=np.int64(n),
+                 policy=self.policy, cells=np.int64(self.fields.nc), boundary_faces=np.int64(self.fields.nb))
+
+    def read_checkpoint(self, path: str):
+        z = np.load(path)
+        if str(z["policy"]) != self.policy or int(z["cells"]) != self.fields.nc or \
+                int(z["boundary_faces"]) != self.fields.nb:
+            raise ValueError("checkpoint of another mesh or policy")
+        self.upload_state(FD=z["FD"], cFD=z["cFD"], cFDold=z["cFD"])
+        self.set_time(float(z["t"]))
 
     def set_write_interval(self, interval: float):
         """Land graph-replayed steps on multiples of ``interval`` (OpenFOAM adjustableRunTime); 0: off."""

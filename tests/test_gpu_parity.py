@@ -233,3 +233,20 @@ def test_mixed_state_round_trip(cases):
     s.run(2, dt=1e-5)
     b = s.state()
     assert np.array_equal(a["cFD"], b["cFD"]) and np.array_equal(a["FD"], b["FD"])
+
+
+@pytest.mark.parametrize("policy", ["ref", "fp64", "mixed"])
+def test_checkpoint_file_resumes_bitwise(cases, policy, tmp_path):
+    """A checkpoint written between steps and read into a fresh solver continues bitwise."""
+    hf, cfg = cases["mixed_riemann"]
+    a = _solver(hf, cfg, policy)
+    a.run(4)
+    path = str(tmp_path / "ck.npz")
+    a.write_checkpoint(path)
+    a.run(5)
+    b = _solver(hf, cfg, policy)
+    b.read_checkpoint(path)
+    b.run(5)
+    sa, sb = a.state(), b.state()
+    assert np.array_equal(sa["FD"], sb["FD"]) and np.array_equal(sa["cFD"], sb["cFD"])
+    assert a.time()[0] == b.time()[0]

@@ -256,3 +256,21 @@ def test_ls_matrix_reproduces_linear_fields(cases, name):
         d = phi[g[c, :k]] - phi[c]
         grad = M[c, :k].T @ d
         np.testing.assert_allclose(grad, [2.0, -3.0], rtol=1e-9, atol=1e-9)
+
+
+def test_bundle_cache_round_trip(tmp_path):
+    """precompute(cache_dir=...) stores the bundle under a hash of its inputs and reads it back."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+
+    m = mesh.riemann_mixed(20, seed=4)
+    W, Wb = mesh.riemann_fields(m)
+    cfg = CaseConfig(stencilType="edgeNeighbour")
+    a = precompute(m, cfg, W, Wb, want_rbf64=True, cache_dir=str(tmp_path))
+    files = list(tmp_path.iterdir())
+    assert len(files) == 1
+    b = precompute(m, cfg, W, Wb, want_rbf64=True, cache_dir=str(tmp_path))
+    assert b.sizes == a.sizes and set(b.a) == set(a.a)
+    for k in a.a:
+        assert np.array_equal(a.a[k], b.a[k]), k
+    c = precompute(m, CaseConfig(stencilType="faceNeighbour"), W, Wb, cache_dir=str(tmp_path))
+    assert len(list(tmp_path.iterdir())) == 2 and c.sizes["maxStencilSize"] != a.sizes["maxStencilSize"]
