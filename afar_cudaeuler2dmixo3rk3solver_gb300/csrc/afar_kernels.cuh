@@ -98,6 +98,7 @@ struct StageArgs {
   double R, Cv, invR, gamma;
   float gm1f, invRf;  // gamma - 1 and 1/R as floats (mixed)
   float Rf, Cvf, gRf;  // R, Cv and gamma*R as floats (mixed)
+  double px, py;       // periods of a periodic mesh (0: none); setup kernels only
   const V2<float>* dtgf;  // Nf (delta r, fraction) as floats (mixed Courant estimate)
 };
 
@@ -1374,6 +1375,9 @@ __global__ void __launch_bounds__(256) k_delta_t_mixed(StageArgs<PolicyMixed> a,
 
 // ---------------------------------------------------------------------------------- setup kernels
 
+// A coordinate difference taken to the nearest periodic image (L > 0), else unchanged.
+__device__ __forceinline__ double wrapd(const double d, const double L) { return L > 0.0 ? d - L * rint(d / L) : d; }
+
 // calcLeastSquareMatrix (reference cudaFieldOperation.h:91-120) into the slot-major matrix, in
 // FP64 math, stored in the policy's operator type.
 template <class P>
@@ -1386,16 +1390,16 @@ __global__ void k_setup_lsm(StageArgs<P> a, V2<typename P::S>* lsm, float* lsm_r
   const double x0 = a.cellC[c].x, y0 = a.cellC[c].y;
   for (int i = 0; i < m; ++i) {
     const int j = a.sten[i * a.ldc + c];
-    const double xj = a.cellC[j].x, yj = a.cellC[j].y;
-    Sxx += (xj - x0) * (xj - x0);
-    Sxy += (xj - x0) * (yj - y0);
-    Syy += (yj - y0) * (yj - y0);
+    const double dx = wrapd(a.cellC[j].x - x0, a.px), dy = wrapd(a.cellC[j].y - y0, a.py);
+    Sxx += dx * dx;
+    Sxy += dx * dy;
+    Syy += dy * dy;
   }
   for (int i = 0; i < m; ++i) {
     const int j = a.sten[i * a.ldc + c];
-    const double xj = a.cellC[j].x, yj = a.cellC[j].y;
-    const S m1 = (Syy * (xj - x0) - Sxy * (yj - y0)) / (Sxx * Syy - Sxy * Sxy);
-    const S m2 = (-Sxy * (xj - x0) + Sxx * (yj - y0)) / (Sxx * Syy - Sxy * Sxy);
+    const double dx = wrapd(a.cellC[j].x - x0, a.px), dy = wrapd(a.cellC[j].y - y0, a.py);
+    const S m1 = (Syy * dx - Sxy * dy) / (Sxx * Syy - Sxy * Sxy);
+    const S m2 = (-Sxy * dx + Sxx * dy) / (Sxx * Syy - Sxy * Sxy);
     lsm[i * a.ldc + c] = V2<S>{m1, m2};
     if (lsm_ref_layout) {
       lsm_ref_layout[2 * (size_t)maxM_ref * c + 2 * i] = (float)m1;
@@ -1419,16 +1423,17 @@ __global__ void k_setup_slot_geom(StageArgs<P> a, const V4<double>* faceXY) {
   V2<S>* sr = const_cast<V2<S>*>(a.sr);
   for (int fi = 0; fi < m; ++fi) {
     const int f = abs(a.cf[fi * a.ldc + c]) - 1;
-    const double dx = faceXY[f].x - x0;
-    const double dy = faceXY[f].y - y0;
+    const double dx = wrapd(faceXY[f].x - x0, a.px);
+    const double dy = wrapd(faceXY[f].y - y0, a.py);
     sg[fi * a.ldc + c] = V2<G>{(G)dx, (G)dy};
     S dR = S(1), fr = S(0);
     if (f < a.Nf) {
       const int nb = a.sten[fi * a.ldc + c];
-      const float deltaR = hypot(a.cellC[nb].x - x0, a.cellC[nb].y - y0);
+      const double nx = wrapd(a.cellC[nb].x - x0, a.px), ny = wrapd(a.cellC[nb].y - y0, a.py);
+      const float deltaR = hypot(nx, ny);
       const float fraction = sqrt(dx * dx + dy * dy) / deltaR;
       if (P::id == PolicyFP64::id) {
-        const double dRd = hypot(a.cellC[nb].x - x0, a.cellC[nb].y - y0);
+        const double dRd = hypot(nx, ny);
         dR = (S)dRd;
         fr = (S)(sqrt(dx * dx + dy * dy) / dRd);
       } else {
@@ -1453,9 +1458,11 @@ __global__ void k_setup_face_geom(StageArgs<P> a, const V4<double>* faceXY, cons
   if (f < a.Nf) {
     const int2 on = a.on[f];
     const V2<double> co = a.cellC[on.x], cn = a.cellC[on.y];
-    const_cast<V4<G>*>(a.fd)[f] = V4<G>{(G)(xy.x - co.x), (G)(xy.y - co.y), (G)(xy.x - cn.x), (G)(xy.y - cn.y)};
-    const double deltaR = hypot(cn.x - co.x, cn.y - co.y);
-    const double fraction = hypot(xy.x - co.x, xy.y - co.y) / deltaR;
+    const double oxd = wrapd(xy.x - co.x, a.px), oyd = wrapd(xy.y - co.y, a.py);
+    const double nxd = wrapd(xy.x - cn.x, a.px), nyd = wrapd(xy.y - cn.y, a.py);
+    const_cast<V4<G>*>(a.fd)[f] = V4<G>{(G)oxd, (G)oyd, (G)nxd, (G)nyd};
+    const double deltaR = hypot(wrapd(cn.x - co.x, a.px), wrapd(cn.y - co.y, a.py));
+    const double fraction = hypot(oxd, oyd) / deltaR;
     const_cast<V2<double>*>(a.dtg)[f] = V2<double>{deltaR, fraction};
   } else {
     const int b = f - a.Nf;

@@ -133,6 +133,11 @@ void sort_quad(Pt* p) {
   for (int i = 0; i < 4; ++i) p[i] = q[i];
 }
 
+// A coordinate difference taken to the nearest periodic image (L > 0), else unchanged.
+inline double wrapd(const double d, const double L) { return L > 0.0 ? d - L * std::rint(d / L) : d; }
+// The point that stands for all periodic images of point p (topology only).
+inline int point_id(const afar_polyMesh* m, const int p) { return m->pointAlias ? m->pointAlias[p] : p; }
+
 struct Geom {
   std::vector<double> cx, cy, area;        // cells
   std::vector<double> fx, fy, sfx, sfy, magsf;  // all faces
@@ -398,6 +403,12 @@ static bool check_mesh(const afar_polyMesh* m) {
         return false;
       }
   }
+  if (m->pointAlias)
+    for (int p = 0; p < m->nPoints; ++p)
+      if (m->pointAlias[p] < 0 || m->pointAlias[p] >= m->nPoints) {
+        set_error("point %d: alias %d out of range", p, m->pointAlias[p]);
+        return false;
+      }
   int expect = m->nInternalFaces;
   for (int p = 0; p < m->nPatches; ++p) {
     if (m->patchSize[p] < 0 || (m->patchSize[p] > 0 && m->patchStart[p] != expect)) {
@@ -516,6 +527,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
       nb += m->patchSize[p];
     }
   const double R = cfg->R, Cv = cfg->Cv;
+  const double px = m->periodX > 0.0 ? m->periodX : 0.0, py = m->periodY > 0.0 ? m->periodY : 0.0;
 
   // ---- initFieldInfo (basicCUDAsolver.cpp:122-258)
   h->boundaryFacesNum = xalloc<int>(patches);
@@ -588,12 +600,13 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
   if (cfg->stencilType == AFAR_STENCIL_EDGE_NEIGHBOUR) {
     pc_off.assign(m->nPoints + 1, 0);
     for (int c = 0; c < nc; ++c)
-      for (int k = m->cellPointsOffset[c]; k < m->cellPointsOffset[c + 1]; ++k) pc_off[m->cellPoints[k] + 1]++;
+      for (int k = m->cellPointsOffset[c]; k < m->cellPointsOffset[c + 1]; ++k) pc_off[point_id(m, m->cellPoints[k]) + 1]++;
     for (int p = 0; p < m->nPoints; ++p) pc_off[p + 1] += pc_off[p];
     pc.resize(pc_off[m->nPoints]);
     std::vector<int> fill(pc_off.begin(), pc_off.end() - 1);
     for (int c = 0; c < nc; ++c)  // ascending cell order within each point
-      for (int k = m->cellPointsOffset[c]; k < m->cellPointsOffset[c + 1]; ++k) pc[fill[m->cellPoints[k]]++] = c;
+      for (int k = m->cellPointsOffset[c]; k < m->cellPointsOffset[c + 1]; ++k)
+        pc[fill[point_id(m, m->cellPoints[k])]++] = c;
   }
 
   // ---- stencils (basicCUDAsolver.cpp:303-398)
@@ -627,7 +640,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
       }
     } else {
       for (int k = m->cellPointsOffset[c]; k < m->cellPointsOffset[c + 1]; ++k) {
-        const int p = m->cellPoints[k];
+        const int p = point_id(m, m->cellPoints[k]);
         for (int l = pc_off[p]; l < pc_off[p + 1]; ++l)
           if (!added(pc[l])) push(pc[l]);
       }
@@ -687,7 +700,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
     const int* st = &gsten[(size_t)maxS * c];
     double rd = 0.0;
     for (int i = 0; i < S; ++i) {
-      const double dx = CELL[st[i]].x - CELL[c].x, dy = CELL[st[i]].y - CELL[c].y;
+      const double dx = wrapd(CELL[st[i]].x - CELL[c].x, px), dy = wrapd(CELL[st[i]].y - CELL[c].y, py);
       rd += std::sqrt(dx * dx + dy * dy);
     }
     rd /= double(S);
@@ -700,7 +713,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
         const double x0 = CELL[sj].x, y0 = CELL[sj].y;
         double acc = 0.0;
         for (int k = gq_off[si]; k < gq_off[si + 1]; ++k) {
-          const double ex = (gq_p[k].x - x0) / rd, ey = (gq_p[k].y - y0) / rd;
+          const double ex = wrapd(gq_p[k].x - x0, px) / rd, ey = wrapd(gq_p[k].y - y0, py) / rd;
           acc += gq_w[k] * std::sqrt(shape + (ex * ex + ey * ey));
         }
         P[i * n + j] = acc;
@@ -743,7 +756,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
       double bvec[AFAR_MAX_VALID_STENCIL_SIZE + 1], gtb[AFAR_MAX_VALID_STENCIL_SIZE + 1];
       for (int i = 0; i < n; ++i) {
         const int si = i == 0 ? c : st[i - 1];
-        const double ex = (x - CELL[si].x) / rd, ey = (y - CELL[si].y) / rd;
+        const double ex = wrapd(x - CELL[si].x, px) / rd, ey = wrapd(y - CELL[si].y, py) / rd;
         bvec[i] = std::sqrt(shape + (ex * ex + ey * ey));
       }
       const double* G = &Gall[(size_t)c * nmax * nmax];

@@ -184,6 +184,7 @@ struct afar_solver {
   double* vinv = nullptr;
   float* vinvf = nullptr;  // mixed: 1/V as float
   V2<float>* dtgf = nullptr;  // mixed: Courant geometry as float
+  double px = 0.0, py = 0.0;  // periods of a periodic mesh (afar_set_periodic)
   void* xfer = nullptr;    // mixed: staging for double <-> device-format copies, 32 B x (Nc + Nb)
   int2* on = nullptr;
   int* bnei = nullptr;
@@ -284,6 +285,8 @@ StageArgs<P> make_args(afar_solver* s) {
   a.Cvf = (float)s->Cv;
   a.gRf = (float)(a.gamma * s->R);
   a.dtgf = s->dtgf;
+  a.px = s->px;
+  a.py = s->py;
   return a;
 }
 
@@ -1212,6 +1215,18 @@ extern "C" afar_status afar_set_step_params(afar_solver* s, double dt, double CF
   k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, dt > 0.0 ? dt : 0.0, CFL, tEnd);
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaGetLastError());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_set_periodic(afar_solver* s, double px, double py) {
+  if (!s) return (set_error("null solver"), AFAR_ERR_ARGUMENT);
+  if (s->have_stencil) return (set_error("afar_set_periodic: call it before afar_setDeviceFieldDataStencil"), AFAR_ERR_STATE);
+  if (!(px >= 0.0) || !(py >= 0.0)) return (set_error("afar_set_periodic: negative period"), AFAR_ERR_ARGUMENT);
+  if (s->policy == AFAR_POLICY_REF && (px > 0.0 || py > 0.0))
+    return (set_error("afar_set_periodic: the ref policy takes raw cell centres in its flux (no periodic meshes)"),
+            AFAR_ERR_ARGUMENT);
+  s->px = px;
+  s->py = py;
   return AFAR_OK;
 }
 

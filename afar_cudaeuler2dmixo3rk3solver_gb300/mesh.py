@@ -46,6 +46,8 @@ class FoamMesh:
     neighbour: np.ndarray
     patches: list  # [(name, label, start, size)]
     depth: float = 1.0
+    period: tuple = (0.0, 0.0)  # periodic mesh: (Lx, Ly), 0 = not periodic in that direction
+    point_alias: np.ndarray | None = None  # periodic mesh: representative of each point's images
 
     @property
     def n_cells(self) -> int:
@@ -108,11 +110,15 @@ def _rcm_permutation(n_cells, own, nei):
     return np.asarray(reverse_cuthill_mckee(g, symmetric_mode=True), dtype=np.int64)
 
 
-def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=True, depth=1.0):
+def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=True, depth=1.0, alias=None,
+                    period=(0.0, 0.0)):
     """Assemble OpenFOAM-ordered face lists from cell polygons.
 
     ``classify(xm, ym) -> patch index`` assigns each boundary edge (by its midpoint) to one of
-    ``patch_defs = [(name, label), ...]``.  Polygons must be counter-clockwise.
+    ``patch_defs = [(name, label), ...]``.  Polygons must be counter-clockwise.  ``alias`` (periodic
+    meshes) maps every point to one representative of its periodic images: edges are matched on
+    representatives, so the two sides of a period meet in internal faces whose points (and so
+    coordinates) are the owner's.
     """
     points = np.ascontiguousarray(points, dtype=np.float64)
     cell_ptr = np.ascontiguousarray(cell_ptr, dtype=np.int64)
@@ -125,8 +131,9 @@ def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=T
     nxt[cell_ptr[1:] - 1] = cell_ptr[:-1]
     a = cell_pts
     b = cell_pts[nxt]
-    lo = np.minimum(a, b)
-    hi = np.maximum(a, b)
+    ka, kb = (a, b) if alias is None else (np.asarray(alias)[a], np.asarray(alias)[b])
+    lo = np.minimum(ka, kb)
+    hi = np.maximum(ka, kb)
     key = lo * points.shape[0] + hi
     order = np.argsort(key, kind="stable")
     ks = key[order]
@@ -169,7 +176,7 @@ def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=T
     bb = b[single]
     xm = 0.5 * (points[ba, 0] + points[bb, 0])
     ym = 0.5 * (points[ba, 1] + points[bb, 1])
-    pidx = np.asarray(classify(xm, ym), dtype=np.int64)
+    pidx = np.asarray(classify(xm, ym), dtype=np.int64) if xm.size else np.zeros(0, dtype=np.int64)
     bo = np.lexsort((bown, pidx))
     bown = bown[bo]
     pidx = pidx[bo]
@@ -200,6 +207,8 @@ def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=T
         neighbour=nei.astype(np.int32),
         patches=patches,
         depth=float(depth),
+        period=tuple(float(v) for v in period),
+        point_alias=None if alias is None else np.ascontiguousarray(alias, dtype=np.int32),
     )
 
 
@@ -274,6 +283,28 @@ def quad_grid(nx, ny, x0=0.0, x1=1.0, y0=0.0, y1=1.0, classify=None, patch_defs=
         patch_defs = patch_defs or [("bottom", BC_OUTLET), ("right", BC_OUTLET), ("top", BC_OUTLET),
                                     ("left", BC_OUTLET)]
     return build_foam_mesh(pts, cell_ptr, cell_pts, classify, patch_defs, renumber=renumber)
+
+
+def periodic_quad_grid(nx, ny, x0=0.0, x1=1.0, y0=0.0, y1=1.0, renumber=True):
+    """nx x ny quads on [x0,x1] x [y0,y1], periodic in both directions (no boundary faces).  The
+    points of the last column and row are duplicates of the first, tied to them by the alias."""
+    xs = np.linspace(x0, x1, nx + 1)
+    ys = np.linspace(y0, y1, ny + 1)
+    X, Y = np.meshgrid(xs, ys, indexing="ij")
+    pts = np.stack([X.ravel(), Y.ravel()], axis=1)
+    I, J = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), indexing="ij")
+    alias = ((I % nx) * (ny + 1) + (J % ny)).ravel()
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    I = I.ravel()
+    J = J.ravel()
+    quads = np.stack([I * (ny + 1) + J, (I + 1) * (ny + 1) + J, (I + 1) * (ny + 1) + J + 1, I * (ny + 1) + J + 1],
+                     axis=1)
+
+    def classify(xm, ym):
+        raise ValueError("a doubly periodic mesh has no boundary faces")
+
+    return build_foam_mesh(pts, np.arange(0, 4 * quads.shape[0] + 1, 4), quads.ravel(), classify, [],
+                           renumber=renumber, alias=alias, period=(x1 - x0, y1 - y0))
 
 
 def corner_flow(n=500):
@@ -432,13 +463,20 @@ def primitive_from_conserved(U, R=R_GAS, Cv=CV_GAS):
     return np.stack([rho * R * T, u, v, T], axis=1)
 
 
-def vortex_cell_averages(mesh: FoamMesh, quadrature, t, strength=5.0, R=R_GAS, gamma=GAMMA):
+def vortex_cell_averages(mesh: FoamMesh, quadrature, t, strength=5.0, R=R_GAS, gamma=GAMMA, centre=(0.0, 0.0)):
     """Cell averages of the conserved variables of the exact solution at time t (the vortex centre
-    at (t, t)), from Gauss points/weights (offsets, points, weights over cells first)."""
+    at centre + (t, t)), from Gauss points/weights (offsets, points, weights over cells first).  On a
+    periodic mesh each point takes its nearest image of the vortex."""
     off, pts, w = quadrature
     nc = mesh.n_cells
     npts = int(off[nc])
-    W = vortex_fields(pts[:npts], strength=strength, xc=t, yc=t, R=R, gamma=gamma)
+    xc, yc = centre[0] + t, centre[1] + t
+    p = pts[:npts].copy()
+    for k, L in enumerate(mesh.period):
+        if L > 0:
+            c = (xc, yc)[k]
+            p[:, k] = c + (p[:, k] - c - L * np.rint((p[:, k] - c) / L))
+    W = vortex_fields(p, strength=strength, xc=xc, yc=yc, R=R, gamma=gamma)
     U = conserved_from_primitive(W, R=R, Cv=R / (gamma - 1.0)) * w[:npts, None]
     sums = np.add.reduceat(U, off[:nc], axis=0)
     wsum = np.add.reduceat(w[:npts], off[:nc])

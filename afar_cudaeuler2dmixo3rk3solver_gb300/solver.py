@@ -51,9 +51,10 @@ SIZE_KEYS = ["cellsNum", "facesNum", "patchesNum", "totalBoundaryFacesNum", "max
 class HostFields:
     """The reference's host field bundle as numpy arrays plus its integer sizes."""
 
-    def __init__(self, sizes: dict, arrays: dict):
+    def __init__(self, sizes: dict, arrays: dict, period=(0.0, 0.0)):
         self.sizes = dict(sizes)
         self.a = dict(arrays)
+        self.period = tuple(float(v) for v in period)  # of a periodic mesh
 
     def __getattr__(self, k):
         a = self.__dict__.get("a", {})
@@ -68,13 +69,15 @@ class HostFields:
     def save(self, path: str):
         """The whole bundle (operators, RBF weights, initial fields) in one .npz file."""
         np.savez(path, __sizes__=np.array([self.sizes[k] for k in SIZE_KEYS], dtype=np.int64),
+                 __period__=np.array(self.period, dtype=np.float64),
                  **{f"a_{k}": v for k, v in self.a.items()})
 
     @classmethod
     def load(cls, path: str) -> "HostFields":
         z = np.load(path)
         sizes = dict(zip(SIZE_KEYS, (int(v) for v in z["__sizes__"])))
-        return cls(sizes, {k[2:]: np.ascontiguousarray(z[k]) for k in z.files if k.startswith("a_")})
+        period = tuple(z["__period__"]) if "__period__" in z.files else (0.0, 0.0)
+        return cls(sizes, {k[2:]: np.ascontiguousarray(z[k]) for k in z.files if k.startswith("a_")}, period)
 
     @property
     def nf(self):
@@ -157,16 +160,20 @@ def poly_mesh_c(mesh: FoamMesh):
     m.patchSize = ptr(keep[7])
     m.patchLabel = ptr(keep[8])
     m.depth = mesh.depth
+    m.periodX, m.periodY = (float(v) for v in mesh.period)
+    if mesh.point_alias is not None:
+        keep.append(np.ascontiguousarray(mesh.point_alias, dtype=np.int32))
+        m.pointAlias = ptr(keep[-1])
     return m, keep
 
 
 def _cache_key(mesh: FoamMesh, cfg: CaseConfig, Wc, Wb, want_rbf64) -> str:
     h = hashlib.sha256()
     for a in (mesh.points, mesh.cell_ptr, mesh.cell_pts, mesh.face_pts, mesh.owner, mesh.neighbour, Wc,
-              np.zeros(0) if Wb is None else Wb):
+              np.zeros(0) if Wb is None else Wb, np.zeros(0) if mesh.point_alias is None else mesh.point_alias):
         a = np.ascontiguousarray(a)
         h.update(str(a.dtype).encode() + str(a.shape).encode() + a.tobytes())
-    h.update(repr((mesh.patches, mesh.depth, dataclasses.astuple(cfg), bool(want_rbf64))).encode())
+    h.update(repr((mesh.patches, mesh.depth, tuple(mesh.period), dataclasses.astuple(cfg), bool(want_rbf64))).encode())
     return h.hexdigest()[:32]
 
 
@@ -202,6 +209,7 @@ def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_r
     check(st)
     try:
         hf = HostFields.from_c(fp, sz)
+        hf.period = tuple(float(v) for v in mesh.period)
         if want_rbf64:
             n = hf.a["RBFbasis"].shape[0]
             buf = (C.c_double * n).from_address(r64.value) if n else None
@@ -232,7 +240,7 @@ def gauss_quadrature(mesh: FoamMesh, cfg: CaseConfig):
 class CudaSolver:
     """The reference's basicCUDAsolver on libafar (one mesh, one GPU)."""
 
-    def __init__(self, fields: HostFields, cfg: CaseConfig, policy="ref", device=0):
+    def __init__(self, fields: HostFields, cfg: CaseConfig, policy="ref", device=0, period=None):
         self.cfg = cfg
         self.fields = fields
         self.policy = policy
@@ -242,6 +250,9 @@ class CudaSolver:
         self._fp = fields.to_c()
         check(lib().afar_setDeviceFieldData(self.h, C.byref(self._fp), s["cellsNum"], s["facesNum"],
                                             s["totalBoundaryFacesNum"]))
+        period = fields.period if period is None else period
+        if any(v > 0 for v in period):
+            check(lib().afar_set_periodic(self.h, float(period[0]), float(period[1])))
         if policy == "fp64" and "RBFbasis64" in fields.a:
             r = fields.a["RBFbasis64"]
             check(lib().afar_set_rbf_basis64(self.h, ptr(r), r.shape[0]))

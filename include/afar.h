@@ -141,6 +141,13 @@ typedef struct {
   const int* patchSize;           /* [nPatches] */
   const int* patchLabel;          /* [nPatches] cudaEulerBCs label (cudaEulerBCs.h:56-61) */
   double depth;                   /* extrusion depth (cell volume = area*depth) */
+  /* Periodic meshes (no counterpart in the reference, which has no periodic patch type): faces
+   * that join the two sides of a period are internal faces whose points are the owner's; seam
+   * points are duplicated so that every polygon has its true coordinates.  periodX/periodY > 0
+   * are the periods (0: not periodic in that direction); pointAlias (may be NULL) maps each point
+   * to one representative of its periodic images, for the point-based (edge-neighbour) stencils. */
+  double periodX, periodY;
+  const int* pointAlias;          /* [nPoints] or NULL */
 } afar_polyMesh;
 
 #define AFAR_STENCIL_FACE_NEIGHBOUR 0  /* basicCUDAsolver.cpp:333-355 */
@@ -292,6 +299,12 @@ afar_status afar_set_step_params(afar_solver* solver, double deltaT, double CFL,
  * to the next write, n = floor(r/dt - 1e-15) + 1 steps of r/n, held within [dt/5, 2 dt]).  Run
  * with tEnd at the write time to stop there.  0 switches it off. */
 afar_status afar_set_write_interval(afar_solver* solver, double writeInterval);
+
+/* Periods of a periodic mesh (as in its afar_polyMesh), before afar_setDeviceFieldDataStencil: the
+ * device geometry (least-squares rows, face offsets, Courant distances) then takes differences
+ * between cell and face centres to the nearest periodic image.  Policies fp64 and mixed (the ref
+ * policy's flux recomputes geometry from the raw centres, as the reference's kernel does). */
+afar_status afar_set_periodic(afar_solver* solver, double periodX, double periodY);
 
 /* ---- batches: many independent solves stepped by the same kernel launches ------------------- */
 /* A batch steps all of its member solvers with one launch per stage kernel (13 per RK3 step,
