@@ -1125,6 +1125,7 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
     const int f = abs(a.cf[fi * ldc + c]) - 1;
     if (f < a.Nf) continue;
     const int b = f - a.Nf;
+    if (a.btype[b] == AFAR_BC_FIXED_INITIAL) continue;  // the ghost keeps its uploaded state
     const V4<double> g = boundary_value(a.btype[b], V4<double>{(double)wn.x, (double)wn.y, (double)wn.z, (double)wn.w},
                                         a.bn[b]);
     reinterpret_cast<V4<float>*>(a.W)[a.Nc + b] = V4<float>{(float)g.x, (float)g.y, (float)g.z, (float)g.w};
@@ -1216,6 +1217,7 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
     const int f = abs(a.cf[fi * ldc + c]) - 1;
     if (f < a.Nf) continue;
     const int b = f - a.Nf;
+    if (a.btype[b] == AFAR_BC_FIXED_INITIAL) continue;  // the ghost keeps its uploaded state
     const V4<double> g =
         boundary_value(a.btype[b], V4<double>{(double)wn.x, (double)wn.y, (double)wn.z, (double)wn.w}, a.bn[b]);
     a.W[a.Nc + b] = V4<WT>{(WT)g.x, (WT)g.y, (WT)g.z, (WT)g.w};

@@ -749,8 +749,8 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
       set_error("boundary face %d: owner out of range", b);
       return AFAR_ERR_ARGUMENT;
     }
-    if (h->boundaryFacesType[b] > 5) {
-      set_error("boundary face %d: unknown cudaEulerBCs label %d (0-5)", b, h->boundaryFacesType[b]);
+    if (h->boundaryFacesType[b] > AFAR_BC_FIXED_INITIAL) {
+      set_error("boundary face %d: unknown boundary label %d (cudaEulerBCs 0-5, or 6)", b, h->boundaryFacesType[b]);
       return AFAR_ERR_ARGUMENT;
     }
   }

@@ -34,6 +34,7 @@ BC_SLIP = 2
 BC_FIXED_VALUE = 3
 BC_OUTLET = 4
 BC_FIXED_VALUE2 = 5
+BC_FIXED_INITIAL = 6  # the ghost keeps the state given for it at set-up (an inflow of any value)
 
 
 @dataclasses.dataclass
@@ -305,6 +306,37 @@ def periodic_quad_grid(nx, ny, x0=0.0, x1=1.0, y0=0.0, y1=1.0, renumber=True):
 
     return build_foam_mesh(pts, np.arange(0, 4 * quads.shape[0] + 1, 4), quads.ravel(), classify, [],
                            renumber=renumber, alias=alias, period=(x1 - x0, y1 - y0))
+
+
+def wedge_quads(nx, ny, angle_deg, x_ramp=0.5, length=2.0, height=1.0, renumber=True):
+    """Supersonic compression ramp: the channel [0, length] x [0, height] whose floor turns up by
+    ``angle_deg`` at x = x_ramp; nx x ny quads, each column spanning floor to ceiling.  Patches:
+    inflow x = 0 (label 6: its ghost keeps the inflow state given at set-up), outflow x = length
+    (label 4), slip walls on floor and ceiling (label 2)."""
+    xs = np.linspace(0.0, length, nx + 1)
+    yb = np.where(xs > x_ramp, (xs - x_ramp) * np.tan(np.radians(angle_deg)), 0.0)
+    if yb.max() >= 0.8 * height:
+        raise ValueError("the ramp leaves less than a fifth of the channel height")
+    eta = np.linspace(0.0, 1.0, ny + 1)
+    X = np.repeat(xs[:, None], ny + 1, axis=1)
+    Y = yb[:, None] + (height - yb[:, None]) * eta[None, :]
+    pts = np.stack([X.ravel(), Y.ravel()], axis=1)
+    I, J = np.meshgrid(np.arange(nx), np.arange(ny), indexing="ij")
+    I = I.ravel()
+    J = J.ravel()
+    quads = np.stack([I * (ny + 1) + J, (I + 1) * (ny + 1) + J, (I + 1) * (ny + 1) + J + 1, I * (ny + 1) + J + 1],
+                     axis=1)
+    eps = 1e-9 * length
+
+    def classify(xm, ym):
+        out = np.full(xm.shape[0], 2, dtype=np.int64)  # walls
+        out[np.abs(xm) < eps] = 0
+        out[np.abs(xm - length) < eps] = 1
+        return out
+
+    return build_foam_mesh(pts, np.arange(0, 4 * quads.shape[0] + 1, 4), quads.ravel(), classify,
+                           [("inflow", BC_FIXED_INITIAL), ("outflow", BC_OUTLET), ("walls", BC_SLIP)],
+                           renumber=renumber)
 
 
 def corner_flow(n=500):

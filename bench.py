@@ -525,11 +525,12 @@ def run_serve(args, dist: Dist):
 
 
 def run_batch(args, dist: Dist):
-    """Batched workload: --batch-solves independent solves, cells log-uniform in [5k, 200k]
-    (square quad meshes), each a uniform flow at Mach U[1.5, 4] carrying an isentropic vortex of
-    strength U[0, 5] through a box with outlets, mixed policy, CFL 0.3; all stepped together
-    --batch-steps RK3 steps by one afar_batch (13 launches per step for the whole batch).  Compared
-    with stepping the same solves one after another (afar_run_timed, a sample of 40 steps each)."""
+    """Batched workload (the shape of the batched config): --batch-solves independent supersonic
+    compression ramps, cells log-uniform in [5k, 200k] (quads, 2:1 channel), inflow Mach U[1.5, 4]
+    through a label-6 inflow patch, ramp angle U[5, 20] degrees, an isentropic vortex of strength
+    U[0, 5] carried in the stream; mixed policy, CFL 0.3; all stepped together --batch-steps RK3
+    steps by one afar_batch (13 launches per step for the whole batch).  Compared with stepping
+    the same solves one after another (afar_run_timed, 40 steps each)."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch, CaseConfig, CudaSolver, mesh, precompute
     from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
 
@@ -539,13 +540,12 @@ def run_batch(args, dist: Dist):
     solvers, cells = [], []
     for k in range(args.batch_solves):
         nc = float(np.exp(rng.uniform(np.log(5e3), np.log(2e5))))
-        n = max(8, int(round(np.sqrt(nc))))
-        m = mesh.quad_grid(n, n, -5.0, 5.0, -5.0, 5.0)
-        mach = rng.uniform(1.5, 4.0)
-        W = mesh.vortex_fields(m.cell_centres(), strength=rng.uniform(0.0, 5.0), xc=0.0, yc=0.0,
-                               u0=mach * np.sqrt(1.4), v0=0.0)
-        Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.0, yc=0.0, u0=mach * np.sqrt(1.4),
-                                v0=0.0)
+        ny = max(8, int(round(np.sqrt(nc / 2.0))))
+        m = mesh.wedge_quads(2 * ny, ny, rng.uniform(5.0, 20.0))
+        u0 = rng.uniform(1.5, 4.0) * np.sqrt(1.4)  # rho = p = 1: sound speed sqrt(1.4)
+        strength = rng.uniform(0.0, 5.0)
+        W = mesh.vortex_fields(m.cell_centres(), strength=strength, xc=0.5, yc=0.6, u0=u0, v0=0.0)
+        Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.5, yc=0.6, u0=u0, v0=0.0)
         cfg = CaseConfig(stencilType="faceNeighbour", CFL=0.3)
         s = CudaSolver(precompute(m, cfg, W, Wb), cfg, policy="mixed", device=dist.local)
         solvers.append(s)
@@ -579,8 +579,8 @@ def run_batch(args, dist: Dist):
     print(json.dumps({
         "metric": "batched cell-RK3-steps/s", "value": total * args.batch_steps / (ms * 1e-3), "unit": "cell-steps/s",
         "n_gpus": dist.world, "higher_is_better": True, "ms_per_step": ms / args.batch_steps,
-        "data": "synthetic (square quad meshes 5k-200k cells, Mach 1.5-4 flow with an isentropic vortex, seeded)",
-        "config": {"workload": "batch_vortex_quads", "solves": args.batch_solves, "cells": int(cells.sum()),
+        "data": "synthetic (compression ramps 5k-200k quads, Mach 1.5-4, 5-20 deg, vortex 0-5, seeded)",
+        "config": {"workload": "batch_wedges", "solves": args.batch_solves, "cells": int(cells.sum()),
                    "steps": args.batch_steps, "policy": "mixed", "launches_per_step": 13, "setup_s": round(setup_s, 1)},
         "one_after_another": {"value": float(cells.sum()) / (solo_ms * 1e-3), "ms_per_step": solo_ms,
                               "launches_per_step": 13 * args.batch_solves},

@@ -125,6 +125,13 @@ typedef struct {
 /* OpenFOAM-style 2-D polyMesh: the x-y cross-section of a one-cell-deep mesh.  Face f joins
  * facePoints[2f] -> facePoints[2f+1]; its normal (Sf) points out of owner[f].  Internal faces
  * come first (owner < neighbour), then the boundary faces patch by patch. */
+/* Boundary labels: the reference's cudaEulerBCs labels 0-5 (cudaEulerBCs.h:56-61: constant-
+ * temperature wall, adiabatic wall, slip, fixed value (1, 3, 0, 1), outlet, fixed value of the
+ * cornerFlow inlet), and one more with no counterpart in the reference: the ghost state stays at
+ * the value given for it at upload (afar_fieldPointer FD[cellsNum + b]), a fixed-value patch whose
+ * value comes from the case's initial fields, e.g. an inflow of any Mach number. */
+#define AFAR_BC_FIXED_INITIAL 6
+
 typedef struct {
   int nPoints;
   const double* points;           /* [2*nPoints] x, y */

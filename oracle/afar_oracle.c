@@ -159,7 +159,7 @@ void oracle_boundary(const oracle_mesh* m, double* FD, double R, double Cv) {
       case 5: /* fixedValue2Boundary */
         Wg[0] = 30.05945; Wg[1] = 4.07795; Wg[2] = 0.0; Wg[3] = 5.97677;
         break;
-      default:
+      default: /* 6: the ghost keeps its initial state (a fixed value from the case's fields) */
         break;
     }
   }

@@ -30,3 +30,16 @@ def test_periodic_cell_averages_wrap():
     a = mesh.vortex_cell_averages(m, q, 0.0, centre=(5.0, 5.0))
     b = mesh.vortex_cell_averages(m, q, 10.0, centre=(5.0, 5.0))  # one full period later: same field
     assert np.abs(a - b).max() < 1e-12
+
+
+def test_wedge_mesh_patches():
+    """The compression ramp of the batched workload: label-6 inflow, outlet, slip walls."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+
+    m = mesh.wedge_quads(40, 20, 15.0)
+    assert [(p[0], p[1], p[3]) for p in m.patches] == [("inflow", 6, 20), ("outflow", 4, 20), ("walls", 2, 80)]
+    assert (m.cell_areas() > 0).all()
+    W = mesh.vortex_fields(m.cell_centres(), strength=2.0, xc=0.5, yc=0.6, u0=3.0, v0=0.0)
+    Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.5, yc=0.6, u0=3.0, v0=0.0)
+    hf = precompute(m, CaseConfig(stencilType="faceNeighbour"), W, Wb)
+    assert set(np.unique(hf.boundaryFacesType)) == {2, 4, 6}
