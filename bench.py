@@ -465,32 +465,34 @@ def run_ours(args, dist: Dist):
 
 
 def run_serve(args, dist: Dist):
-    """Serving workload: requests arrive as a Poisson process (rate --serve-rate) with meshes drawn
-    log-uniformly from a pool of quad Riemann problems of 10k-300k cells and step counts uniform in
-    [20, 200]; each is submitted to one afar_server (mixed policy, 180 GB budget, 25-step chunks)
-    from host buffers and its latency runs from submit to its fields being back on the host.
-    Prints served cell-steps/s and latency percentiles.  The pool's precompute is outside the
-    timed region; request inputs are resident host arrays."""
+    """Serving workload: requests arrive as a Poisson process (rate --serve-rate); each takes a mesh
+    drawn log-uniformly from a pool of quad Riemann problems of 10k-2M cells and a step count
+    uniform in [100, 2000]; 5% of them are solved in the fp64 policy, the rest in mixed.  Each
+    policy has its own afar_server (180 GB budget, 50-step chunks); a request's latency runs from
+    submit to its fields being back in its host buffers.  The pool's precompute is outside the
+    timed region (request inputs are resident host arrays).  Prints served cell-steps/s and the
+    latency percentiles."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, Server, mesh, precompute
     from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
 
     b.build_all()  # with several ranks, each serves its own queue on its own GPU (replicas)
     rng = np.random.default_rng(args.seed + 17 * dist.rank)
     pool = []
-    for n in (100, 175, 316, 550):
+    for n in (100, 224, 500, 1000, 1414):
         m = mesh.quad_grid(n, n, 0.0, 1.2, 0.0, 1.0)
         W, Wb = mesh.riemann_fields(m)
         cfg = CaseConfig(stencilType="faceNeighbour", CFL=0.3)
-        pool.append((precompute(m, cfg, W, Wb), cfg))
+        pool.append((precompute(m, cfg, W, Wb, want_rbf64=True), cfg))
     sizes = np.array([hf.nc for hf, _ in pool], dtype=np.float64)
     logp = np.log(sizes)
     nreq = args.serve_requests
     pick = [int(np.argmin(np.abs(logp - rng.uniform(logp[0], logp[-1])))) for _ in range(nreq)]
-    steps = rng.integers(20, 201, nreq)
+    steps = rng.integers(100, 2001, nreq)
+    fp64 = rng.uniform(size=nreq) < 0.05
     gaps = rng.exponential(1.0 / args.serve_rate, nreq)
-    srv = Server("mixed", device=dist.local, hbm_budget_bytes=180 << 30, chunk_steps=25)
-    warm = srv.submit(*pool[0], n_steps=5)
-    srv.wait(warm)
+    servers = {p: Server(p, device=dist.local, hbm_budget_bytes=180 << 30, chunk_steps=50) for p in ("mixed", "fp64")}
+    for srv in servers.values():
+        srv.wait(srv.submit(*pool[0], n_steps=5))
     dist.barrier()
     t0 = time.perf_counter()
     ids = []
@@ -499,28 +501,32 @@ def run_serve(args, dist: Dist):
         t_next += gaps[i]
         while time.perf_counter() < t_next:
             time.sleep(min(1e-3, max(0.0, t_next - time.perf_counter())))
-        ids.append(srv.submit(*pool[pick[i]], n_steps=int(steps[i])))
+        srv = servers["fp64" if fp64[i] else "mixed"]
+        ids.append((srv, srv.submit(*pool[pick[i]], n_steps=int(steps[i]))))
     lat = []
     ok = True
-    for rid in ids:
+    for srv, rid in ids:
         FD, si, ms = srv.wait(rid)
         lat.append(ms)
         ok = ok and bool(np.isfinite(FD).all())
     wall = dist.max(time.perf_counter() - t0)
-    st = srv.stats()
-    srv.close()
+    st = {p: srv.stats() for p, srv in servers.items()}
+    for srv in servers.values():
+        srv.close()
     work = dist.sum(float(sum(sizes[pick[i]] * steps[i] for i in range(nreq))))
     if dist.rank != 0:
         return
     lat = np.array(lat)
     print(json.dumps({
         "metric": "served cell-RK3-steps/s", "value": work / wall, "unit": "cell-steps/s", "n_gpus": dist.world,
-        "higher_is_better": True, "data": "synthetic (quad Riemann meshes 10k-300k cells, seeded)",
+        "higher_is_better": True, "data": "synthetic (quad Riemann meshes 10k-2M cells, seeded)",
         "config": {"workload": "serve_poisson", "requests": nreq, "rate_per_s": args.serve_rate,
-                   "steps": "U[20,200]", "policy": "mixed", "chunk_steps": 25, "budget_bytes": 180 << 30},
+                   "steps": "U[100,2000]", "policies": "mixed, 5% fp64", "chunk_steps": 50,
+                   "budget_bytes": 180 << 30, "fp64_requests": int(fp64.sum())},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(lat.max())},
-        "wall_s": wall, "peak_running": st["peakRunning"], "peak_bytes": st["peakBytes"], "finite": ok,
+        "wall_s": wall, "peak_running": {p: v["peakRunning"] for p, v in st.items()},
+        "peak_bytes": {p: v["peakBytes"] for p, v in st.items()}, "finite": ok,
     }), flush=True)
 
 
