@@ -125,7 +125,7 @@ def lib():
             "afar_server_create": (S, [C.POINTER(_p), C.c_int, C.c_int, C.c_size_t, C.c_int]),
             "afar_server_submit": (S, [_p, C.POINTER(Request), C.POINTER(C.c_longlong)]),
             "afar_server_wait": (S, [_p, C.c_longlong, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
-                                     C.POINTER(C.c_double)]),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
             "afar_server_get_stats": (S, [_p, C.POINTER(ServerStats)]),
             "afar_server_destroy": (S, [_p]),
             "afar_batch_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),

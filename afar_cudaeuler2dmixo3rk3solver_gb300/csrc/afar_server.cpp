@@ -6,6 +6,7 @@
 // memory of the running solves plus the next one fits the budget (the first always runs), steps
 // the batch by one chunk, and retires the solves that reached their end time or step count.
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -32,6 +33,7 @@ struct Request {
   afar_solver* solver = nullptr;
   size_t bytes = 0;
   long long steps0 = 0;
+  long long steps_done = 0;
 };
 
 // Device memory of a solve before it is built: a per-cell, per-face model of the allocations
@@ -182,9 +184,20 @@ struct afar_server {
           }
         }
         if (fin) {
+          r->steps_done = steps - r->steps0;
           if (r->status == AFAR_OK &&
               (e = afar_download_state(r->solver, r->req.outFD, nullptr, r->req.outShockIndicator)))
             fail(r, e, "download");
+          if (r->status == AFAR_OK) {  // a state that broke down still advanced: report it
+            const size_t n = 4 * (size_t)(r->req.sizes.cellsNum + r->req.sizes.totalBoundaryFacesNum);
+            const double* v = reinterpret_cast<const double*>(r->req.outFD);
+            for (size_t i = 0; i < n; ++i)
+              if (!std::isfinite(v[i])) {
+                r->status = AFAR_ERR_NOT_FINITE;
+                r->message = "the solve's state is not finite";
+                break;
+              }
+          }
           {
             std::lock_guard<std::mutex> lock(mu);
             st.bytesInUse -= r->bytes;
@@ -253,7 +266,7 @@ extern "C" afar_status afar_server_submit(afar_server* s, const afar_request* q,
 }
 
 extern "C" afar_status afar_server_wait(afar_server* s, long long id, double timeout, int* done, int* status,
-                                        double* latency_ms) {
+                                        double* latency_ms, long long* steps) {
   using afar::set_error;
   if (!s || !done) return (set_error("afar_server_wait: null argument"), AFAR_ERR_ARGUMENT);
   std::unique_lock<std::mutex> lock(s->mu);
@@ -269,6 +282,7 @@ extern "C" afar_status afar_server_wait(afar_server* s, long long id, double tim
   if (r->done) {
     if (status) *status = r->status;
     if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+    if (steps) *steps = r->steps_done;
     if (r->status != AFAR_OK) set_error("%s", r->message.c_str());
   }
   return AFAR_OK;

@@ -476,15 +476,17 @@ class Server:
         self._keep[rid.value] = (fields, fp, r, out_FD, out_si)  # alive until the request is done
         return rid.value
 
-    def wait(self, rid: int, timeout: float = -1.0):
-        """(FD, shock indicator, latency ms) once the request is done; None on timeout."""
-        done, status, lat = C.c_int(), C.c_int(), C.c_double()
-        check(lib().afar_server_wait(self.h, rid, timeout, C.byref(done), C.byref(status), C.byref(lat)))
+    def wait(self, rid: int, timeout: float = -1.0, with_steps: bool = False):
+        """(FD, shock indicator, latency ms[, steps]) once the request is done; None on timeout.
+        Raises AfarError for a failed request (AFAR_ERR_NOT_FINITE: its state broke down)."""
+        done, status, lat, steps = C.c_int(), C.c_int(), C.c_double(), C.c_longlong()
+        check(lib().afar_server_wait(self.h, rid, timeout, C.byref(done), C.byref(status), C.byref(lat),
+                                     C.byref(steps)))
         if not done.value:
             return None
-        check(status.value)
         _, _, _, out_FD, out_si = self._keep.pop(rid)
-        return out_FD, out_si, lat.value
+        check(status.value)
+        return (out_FD, out_si, lat.value, steps.value) if with_steps else (out_FD, out_si, lat.value)
 
     def stats(self) -> dict:
         st = _ffi.ServerStats()

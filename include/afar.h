@@ -363,10 +363,11 @@ afar_status afar_server_create(afar_server** server, int policy, int device, siz
                                int chunkSteps);
 afar_status afar_server_submit(afar_server* server, const afar_request* request, long long* requestId);
 /* Waits up to timeoutSeconds (< 0: no limit) for the request.  *done = 1 when it has finished;
- * then *requestStatus is its afar_status (an error message is available from afar_last_error on
- * the calling thread) and *latencyMs the time from submit to completion. */
+ * then *requestStatus is its afar_status (AFAR_ERR_NOT_FINITE for a solve whose state broke down;
+ * the message is available from afar_last_error on the calling thread), *latencyMs the time from
+ * submit to completion and *steps the RK3 steps it took (any of the three may be NULL). */
 afar_status afar_server_wait(afar_server* server, long long requestId, double timeoutSeconds, int* done,
-                             int* requestStatus, double* latencyMs);
+                             int* requestStatus, double* latencyMs, long long* steps);
 afar_status afar_server_get_stats(afar_server* server, afar_server_stats* stats);
 /* Finishes the running and queued requests, then stops the worker. */
 afar_status afar_server_destroy(afar_server* server);
