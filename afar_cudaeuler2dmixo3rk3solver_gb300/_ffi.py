@@ -122,6 +122,8 @@ def lib():
             "afar_set_step_params": (S, [_p, C.c_double, C.c_double, C.c_double]),
             "afar_set_write_interval": (S, [_p, C.c_double]),
             "afar_set_periodic": (S, [_p, C.c_double, C.c_double]),
+            "afar_set_tuning": (S, [_p, C.c_int]),
+            "afar_get_tuning": (S, [_p, C.POINTER(C.c_int), C.POINTER(C.c_float), C.POINTER(C.c_float)]),
             "afar_server_create": (S, [C.POINTER(_p), C.c_int, C.c_int, C.c_size_t, C.c_int]),
             "afar_server_submit": (S, [_p, C.POINTER(Request), C.POINTER(C.c_longlong)]),
             "afar_server_wait": (S, [_p, C.c_longlong, C.c_double, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -164,7 +166,7 @@ EXPORTED = [
     "afar_set_time", "afar_stage_debug", "afar_debug_limiter64", "afar_upload_state", "afar_download_state",
     "afar_download_ls_matrix", "afar_device_bytes", "afar_launches_per_step", "afar_run_timed",
     "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc", "afar_set_step_params",
-    "afar_set_write_interval", "afar_set_periodic", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
+    "afar_set_write_interval", "afar_set_periodic", "afar_set_tuning", "afar_get_tuning", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
     "afar_batch_destroy", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
     "afar_server_destroy",
 ]

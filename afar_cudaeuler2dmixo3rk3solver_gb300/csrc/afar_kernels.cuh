@@ -134,6 +134,190 @@ __device__ __forceinline__ void limiter_process_fast(float& limiter, float& phif
 // (d2GaussQuadrature.C:65-148); the stencil upload rejects larger compact stencils.
 constexpr int kMaxFaces = 4;
 
+// reconstruct, register-pass variant for the mixed policy (the autotuner's alternative to the
+// tile-staged kernel): LS gradient, stencil min/max, raw limiter, O3 RBF face values of this
+// cell's side of each internal face, troubled-cell flag.
+// One pass over the stencil: each member's state is gathered once and feeds the gradient and
+// min/max (compact members) and the O3 sums of every face side at once, all in registers.  The
+// loads of a batch of members (indices, gathers, weights) are issued together, so several are in
+// flight per thread; no shared memory, so occupancy is set by registers alone.  Every sum is
+// still accumulated in stencil order, as in the reference.
+template <class P>
+__device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int blk) {
+  using S = typename P::S;
+  using G = typename P::G;
+  using WT = typename P::W;
+  const int c = blk * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int ldc = a.ldc;
+  const int nS = a.nS[c], nM = a.nM[c];
+  const int wrow = a.maxS + 1;
+  int fid[kMaxFaces];
+  bool inner[kMaxFaces];
+  V2<S> lm[kMaxFaces];
+#pragma unroll
+  for (int fi = 0; fi < kMaxFaces; ++fi) {
+    fid[fi] = fi < nM ? a.cf[fi * ldc + c] : 1;
+    inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
+    lm[fi] = fi < nM ? a.lsm[fi * ldc + c] : V2<S>{S(0), S(0)};
+  }
+  const V4<WT> wc = a.W[c];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  G acc[kMaxFaces][4];
+#pragma unroll
+  for (int fi = 0; fi < kMaxFaces; ++fi) {  // each face side's O3 sum starts with the cell's own term
+    const S w0 = inner[fi] ? a.wts[(size_t)(fi * wrow) * ldc + c] : S(0);
+    acc[fi][0] = w0 * pc;
+    acc[fi][1] = w0 * uxc;
+    acc[fi][2] = w0 * uyc;
+    acc[fi][3] = w0 * tc;
+  }
+  G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
+  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
+  S pn[kMaxFaces];  // pressure of the cell across each face
+  {  // members 0..3: the face neighbours (compact stencil) come first
+    int j[kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) j[u] = u < nS ? a.sten[u * ldc + c] : c;
+    V4<WT> wj[kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) wj[u] = a.W[j[u]];
+    S wv[kMaxFaces][kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u)
+#pragma unroll
+      for (int fi = 0; fi < kMaxFaces; ++fi)
+        wv[u][fi] = (u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + u + 1) * ldc + c] : S(0);
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) {
+      if (u < nS) {
+        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        if (u < nM) {  // reference :148-169 and :190-205
+          const S M1 = lm[u].x, M2 = lm[u].y;
+          S dphi = vx - pc;
+          gPx += M1 * dphi;
+          gPy += M2 * dphi;
+          dphi = vy - uxc;
+          gUxx += M1 * dphi;
+          gUyx += M2 * dphi;
+          dphi = vz - uyc;
+          gUxy += M1 * dphi;
+          gUyy += M2 * dphi;
+          dphi = vw - tc;
+          gTx += M1 * dphi;
+          gTy += M2 * dphi;
+          pMax = fmx(vx, pMax);
+          pMin = fmn(vx, pMin);
+          uxMax = fmx(vy, uxMax);
+          uxMin = fmn(vy, uxMin);
+          uyMax = fmx(vz, uyMax);
+          uyMin = fmn(vz, uyMin);
+          tMax = fmx(vw, tMax);
+          tMin = fmn(vw, tMin);
+          pn[u] = vx;
+        }
+#pragma unroll
+        for (int fi = 0; fi < kMaxFaces; ++fi) {
+          acc[fi][0] += wv[u][fi] * vx;
+          acc[fi][1] += wv[u][fi] * vy;
+          acc[fi][2] += wv[u][fi] * vz;
+          acc[fi][3] += wv[u][fi] * vw;
+        }
+      }
+    }
+  }
+  constexpr int U = sizeof(WT) == 4 ? 4 : 2;
+  for (int ci0 = kMaxFaces; ci0 < nS; ci0 += U) {  // the rest of the stencil: O3 sums only
+    int j[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) j[u] = (ci0 + u < nS) ? a.sten[(ci0 + u) * ldc + c] : c;
+    V4<WT> wj[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) wj[u] = a.W[j[u]];
+    S wv[U][kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int fi = 0; fi < kMaxFaces; ++fi)
+        wv[u][fi] = (ci0 + u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + ci0 + u + 1) * ldc + c] : S(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (ci0 + u < nS) {
+        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+#pragma unroll
+        for (int fi = 0; fi < kMaxFaces; ++fi) {
+          acc[fi][0] += wv[u][fi] * vx;
+          acc[fi][1] += wv[u][fi] * vy;
+          acc[fi][2] += wv[u][fi] * vz;
+          acc[fi][3] += wv[u][fi] * vw;
+        }
+      }
+    }
+  }
+  a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
+  a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
+
+  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
+  V4<S> L;
+  int8_t flag0;
+  if (fab(tMax - tMin) < VSMALL) {  // reference :208-233
+    L = V4<S>{S(1), S(1), S(1), S(1)};
+#pragma unroll
+    for (int fi = 0; fi < kMaxFaces; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      V4<G> o;
+      o.x = (G)(pc) + gPx * dx + gPy * dy;
+      o.y = (G)(uxc) + gUxx * dx + gUyx * dy;
+      o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
+      o.w = (G)(tc) + gTx * dx + gTy * dy;
+      a.fv[2 * f + isNei] = o;
+    }
+    flag0 = 0;
+  } else {  // reference :235-314
+    S lp = S(2), lux = S(2), luy = S(2), lt = S(2);
+    S smooth = S(0);
+    bool notTrouble = true;
+#pragma unroll
+    for (int fi = 0; fi < kMaxFaces; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      const V2<S> rf = a.sr[fi * ldc + c];
+      const S deltaR = rf.x, fraction = rf.y;
+      const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
+      S phif;
+      V4<G> o;
+      limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
+      o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
+      notTrouble = phif > S(0);
+      smooth = fmx(smooth, __fdividef(fab((S(1) - fraction) * pc + fraction * pn[fi] - phif), deltaR) +
+                               (pf <= S(0)) * AFAR_LIT(S, 1e20) + (phif <= S(0)) * AFAR_LIT(S, 1e20));
+      limiter_process_fast(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
+      o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
+      limiter_process_fast(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
+      o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
+      limiter_process_fast(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
+      o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
+      notTrouble = phif > S(0);
+      a.fv[2 * f + isNei] = o;
+    }
+    L.x = fmx(lp, S(0)) * notTrouble;
+    L.y = fmx(lux, S(0)) * notTrouble;
+    L.z = fmx(luy, S(0)) * notTrouble;
+    L.w = fmx(lt, S(0)) * notTrouble;
+    smooth = __fdividef(smooth, S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
+    flag0 = (smooth > S(1));
+  }
+  a.lim[c] = L;
+  a.si[2 * c] = flag0;
+}
+
 // ---------------------------------------------------------------- mixed reconstruct, tile-staged
 // One CTA per 128-cell tile.  The tile's slice of every per-cell operator row (face ids, LS rows,
 // face offsets, (dr, fraction), stencil ids, O3 weights) and the cells' own states are contiguous
@@ -1226,6 +1410,10 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
 
 // ------------------------------------------------------------------------- single-solve kernels
 // One solve per launch, arguments by value (read from the parameter bank).
+template <class P>
+__global__ void __launch_bounds__(128, 5) k_reconstruct_reg(StageArgs<P> a) {
+  recon_reg_body<P>(a, blockIdx.x);
+}
 template <class P, int NF>
 __global__ void __launch_bounds__(kTile, 4) k_reconstruct_tile(StageArgs<P> a) {
   extern __shared__ __align__(128) unsigned char sm[];

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "afar_internal.h"
@@ -185,6 +186,9 @@ struct afar_solver {
   float* vinvf = nullptr;  // mixed: 1/V as float
   V2<float>* dtgf = nullptr;  // mixed: Courant geometry as float
   double px = 0.0, py = 0.0;  // periods of a periodic mesh (afar_set_periodic)
+  int recon_variant = 0;      // mixed reconstruct: 0 tile-staged, 1 register pass (autotuned)
+  int recon_request = -1;     // afar_set_tuning: -1 autotune, else the variant to use
+  float tune_ms[2] = {0.f, 0.f};  // the autotuner's measured launch times (0: decision from the cache)
   void* xfer = nullptr;    // mixed: staging for double <-> device-format copies, 32 B x (Nc + Nb)
   int2* on = nullptr;
   int* bnei = nullptr;
@@ -323,7 +327,9 @@ struct Stage {
 
   void reconstruct() const {
     if constexpr (P::id == PolicyMixed::id) {
-      if (s->maxM <= 3)
+      if (s->recon_variant == 1)
+        k_reconstruct_reg<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
+      else if (s->maxM <= 3)
         k_reconstruct_tile<P, 3><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
       else
         k_reconstruct_tile<P, 4><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
@@ -602,6 +608,83 @@ static afar_status get_state(afar_solver* s, afar_basicFieldData* FD, afar_conse
   return AFAR_OK;
 }
 
+// The project autotuner: the mixed reconstruct has two implementations whose speed depends on the
+// mesh (stencil size, faces per cell, size): the tile-staged kernel (bulk copies of each 128-cell
+// tile's operator rows into shared memory) and the register pass (no shared memory, more tiles per
+// SM).  At the stencil upload each is timed on the solver's own data (one warm-up, best of three
+// launches, CUDA events on its stream; the launches only write the stage's intermediates) and the
+// faster kept.  Decisions are cached per device and mesh class (faces per cell, stencil size, cell
+// count to a factor of two), so later solvers of the same class skip the timing.
+static afar_status tune_reconstruct(afar_solver* s) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int>, int> cache;
+  if (s->recon_request >= 0) {
+    s->recon_variant = s->recon_request;
+    return AFAR_OK;
+  }
+  int lg = 0;
+  while ((1 << (lg + 1)) <= s->Nc) ++lg;
+  const auto key = std::make_tuple(s->device, s->maxM, s->maxS, lg);
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      s->recon_variant = it->second;
+      s->tune_ms[0] = s->tune_ms[1] = 0.f;
+      return AFAR_OK;
+    }
+  }
+  Stage<PolicyMixed> sg;
+  afar_status st = make_stage<PolicyMixed>(s, false, &sg);
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  AFAR_CUDA(cudaEventCreate(&e0));
+  AFAR_CUDA(cudaEventCreate(&e1));
+  float best[2];
+  for (int v = 0; v < 2; ++v) {
+    s->recon_variant = v;
+    sg.reconstruct();  // warm-up
+    best[v] = 1e30f;
+    for (int k = 0; k < 3; ++k) {
+      AFAR_CUDA(cudaEventRecord(e0, s->stream));
+      sg.reconstruct();
+      AFAR_CUDA(cudaEventRecord(e1, s->stream));
+      AFAR_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      AFAR_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      best[v] = std::min(best[v], ms);
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  AFAR_CUDA(cudaGetLastError());
+  if ((st = check_device_error(s))) return st;
+  s->recon_variant = best[1] < best[0] ? 1 : 0;
+  s->tune_ms[0] = best[0];
+  s->tune_ms[1] = best[1];
+  std::lock_guard<std::mutex> lock(mu);
+  cache[key] = s->recon_variant;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_set_tuning(afar_solver* s, int reconVariant) {
+  if (!s || reconVariant < -1 || reconVariant > 1) return (set_error("afar_set_tuning: variant -1, 0 or 1"), AFAR_ERR_ARGUMENT);
+  s->recon_request = reconVariant;
+  if (!s->have_stencil || s->policy != AFAR_POLICY_MIXED) return AFAR_OK;
+  AFAR_CUDA(cudaSetDevice(s->device));
+  afar_status st = tune_reconstruct(s);
+  if (st) return st;
+  return s->graph ? capture_graph(s) : AFAR_OK;
+}
+
+extern "C" afar_status afar_get_tuning(afar_solver* s, int* reconVariant, float* msTile, float* msRegister) {
+  if (!s || !reconVariant) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
+  *reconVariant = s->recon_variant;
+  if (msTile) *msTile = s->tune_ms[0];
+  if (msRegister) *msRegister = s->tune_ms[1];
+  return AFAR_OK;
+}
+
 extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldPointer* h, int cellsNum, int facesNum,
                                                int totalBoundaryFacesNum) {
   if (!s || !h || !h->CELL || !h->FACE || !h->cellVolume || !h->FD || !h->cFD || cellsNum <= 0 || facesNum < 0 ||
@@ -805,6 +888,7 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
   if (st) return st;
   if ((st = dalloc_t(s, &s->res_dbg, (size_t)Nc))) return st;
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  if (s->policy == AFAR_POLICY_MIXED && (st = tune_reconstruct(s))) return st;
   s->have_stencil = true;
   return AFAR_OK;
 }

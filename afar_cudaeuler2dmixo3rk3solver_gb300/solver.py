@@ -379,6 +379,15 @@ class CudaSolver:
         self.upload_state(FD=z["FD"], cFD=z["cFD"], cFDold=z["cFD"])
         self.set_time(float(z["t"]))
 
+    def set_tuning(self, recon_variant: int = -1):
+        """Mixed reconstruct: -1 autotune, 0 tile-staged, 1 register pass."""
+        check(lib().afar_set_tuning(self.h, recon_variant))
+
+    def tuning(self) -> dict:
+        v, a, b = C.c_int(), C.c_float(), C.c_float()
+        check(lib().afar_get_tuning(self.h, C.byref(v), C.byref(a), C.byref(b)))
+        return {"recon_variant": v.value, "ms_tile": a.value, "ms_register": b.value}
+
     def set_write_interval(self, interval: float):
         """Land graph-replayed steps on multiples of ``interval`` (OpenFOAM adjustableRunTime); 0: off."""
         check(lib().afar_set_write_interval(self.h, interval))

@@ -405,6 +405,15 @@ afar_status afar_adjustTimeStep_noalloc(const afar_basicFieldData* FD, const afa
 /* Device memory held by the solver, in bytes. */
 afar_status afar_device_bytes(afar_solver* solver, size_t* bytes);
 
+/* The autotuner (no counterpart in the reference).  The mixed policy's reconstruct has two
+ * implementations, tile-staged (0) and register pass (1); at the stencil upload each is timed on
+ * the solver's own data and the faster kept, the decision cached per device and mesh class (faces
+ * per cell, stencil size, cell count to a factor of two).  afar_set_tuning picks one instead
+ * (-1: autotune, the default); afar_get_tuning reports the choice and the measured launch times
+ * (0 when the decision came from the cache). */
+afar_status afar_set_tuning(afar_solver* solver, int reconVariant);
+afar_status afar_get_tuning(afar_solver* solver, int* reconVariant, float* msTile, float* msRegister);
+
 /* Number of kernel launches one afar_run step issues on this solver (for accounting). */
 int afar_launches_per_step(afar_solver* solver);
 

@@ -250,3 +250,26 @@ def test_checkpoint_file_resumes_bitwise(cases, policy, tmp_path):
     sa, sb = a.state(), b.state()
     assert np.array_equal(sa["FD"], sb["FD"]) and np.array_equal(sa["cFD"], sb["cFD"])
     assert a.time()[0] == b.time()[0]
+
+
+def test_autotuner_picks_a_reconstruct_and_caches_it(cases):
+    """The mixed reconstruct's two implementations agree, the autotuner times both on the first
+    solver of a mesh class and takes the cached decision for the next one."""
+    hf, cfg = cases["ffs_tri"]
+    a = _solver(hf, cfg, "mixed")
+    ta = a.tuning()
+    assert ta["recon_variant"] in (0, 1)
+    b = _solver(hf, cfg, "mixed")
+    tb = b.tuning()
+    assert tb["recon_variant"] == ta["recon_variant"] and tb["ms_tile"] == 0.0
+    if ta["ms_tile"] > 0.0:  # this process timed the class first
+        assert ta["ms_register"] > 0.0
+    outs = []
+    for v in (0, 1):
+        s = _solver(hf, cfg, "mixed")
+        s.set_tuning(v)
+        assert s.tuning()["recon_variant"] == v
+        s.run(5, dt=1e-4)
+        outs.append(s.state())
+    scale = np.abs(outs[0]["cFD"]).max(axis=0)
+    assert (np.abs(outs[0]["cFD"] - outs[1]["cFD"]) <= 1e-5 * scale).all()
