@@ -912,6 +912,97 @@ __device__ __forceinline__ void roe_flux(G& rhoFlux, G& rhoUxFlux, G& rhoUyFlux,
               magSf;
 }
 
+// ---------------------------------------------------------------- dissipation, fp64 and mixed
+// The same Roe and KFVS dissipation for the policies without bit parity, with their divisions
+// folded: p/rho as R T (the state's own equation of state), one reciprocal of magSf (precomputed
+// per face), of c^2 and of lambda, gamma and K computed once on the host, and the entropy fix's
+// division only on the faces that need it.  Equal to the reference's expressions up to rounding.
+__device__ __forceinline__ double fdiv(const double a, const double b) { return a / b; }
+__device__ __forceinline__ float fdiv(const float a, const float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double rsqrt_(const double a) { return rsqrt(a); }
+__device__ __forceinline__ float rsqrt_(const float a) { return rsqrtf(a); }
+
+template <class D>
+__device__ __forceinline__ void entropy_fix(D& l, const D eps) {
+  if (l < eps) l = fdiv(l * l + eps * eps, D(2) * eps + AFAR_LIT(D, 1e-30));
+}
+
+template <class D>
+__device__ __forceinline__ void roe_flux_fast(D& rhoFlux, D& rhoUxFlux, D& rhoUyFlux, D& rhoEFlux, const D rhoL,
+                                              const D rhoR, const D uxL, const D uxR, const D uyL, const D uyR,
+                                              const D tL, const D tR, const D deltaP, const D deltaRho, const D R,
+                                              const D Cv, const D gamma, const D magSf, const D nfx, const D nfy) {
+  const D cvL = uxL * nfx + uyL * nfy;
+  const D cvR = uxR * nfx + uyR * nfy;
+  const D kL = D(0.5) * (uxL * uxL + uyL * uyL), kR = D(0.5) * (uxR * uxR + uyR * uyR);
+  const D hL = Cv * tL + kL + R * tL;
+  const D hR = Cv * tR + kR + R * tR;
+  const D tiny = AFAR_LIT(D, 1e-20);
+  const D rhoT = sqr_(fmx(rhoL * rhoR, tiny));
+  const D sL = sqr_(fmx(rhoL, tiny)), sR = sqr_(fmx(rhoR, tiny));
+  const D wL = fdiv(sL, sL + sR);
+  const D wR = D(1) - wL;
+  const D uxT = uxL * wL + uxR * wR;
+  const D uyT = uyL * wL + uyR * wR;
+  const D hT = hL * wL + hR * wR;
+  const D q2 = uxT * uxT + uyT * uyT;
+  const D cT = sqr_(fmx((gamma - D(1)) * (hT - D(0.5) * q2), tiny));
+  const D ic2 = fdiv(D(1), cT * cT);
+  const D cvT = uxT * nfx + uyT * nfy;
+  const D dUx = uxR - uxL;
+  const D dUy = uyR - uyL;
+  const D dCv = dUx * nfx + dUy * nfy;
+  const D r1 = (deltaP - rhoT * cT * dCv) * (D(0.5) * ic2);
+  const D r2 = deltaRho - deltaP * ic2;
+  const D r3 = (deltaP + rhoT * cT * dCv) * (D(0.5) * ic2);
+  const D cL = sqr_(fmx((gamma - D(1)) * (hL - kL), tiny));
+  const D cR = sqr_(fmx((gamma - D(1)) * (hR - kR), tiny));
+  D l1 = fab(cvT - cT), l2 = fab(cvT), l3 = fab(cvT + cT);
+  entropy_fix(l1, D(2) * fmx(D(0), (cvR - cR) - (cvL - cL)));
+  entropy_fix(l2, D(2) * fmx(D(0), cvR - cvL));
+  entropy_fix(l3, D(2) * fmx(D(0), (cvR + cR) - (cvL + cL)));
+  rhoFlux -= D(0.5) * (l1 * r1 + l2 * r2 + l3 * r3) * magSf;
+  rhoUxFlux -= D(0.5) * (l1 * r1 * (uxT - cT * nfx) + l2 * (r2 * uxT + rhoT * (dUx - dCv * nfx)) + l3 * r3 * (uxT + cT * nfx)) * magSf;
+  rhoUyFlux -= D(0.5) * (l1 * r1 * (uyT - cT * nfy) + l2 * (r2 * uyT + rhoT * (dUy - dCv * nfy)) + l3 * r3 * (uyT + cT * nfy)) * magSf;
+  rhoEFlux -= D(0.5) *
+              (l1 * r1 * (hT - cT * cvT) + l2 * (r2 * D(0.5) * q2 + rhoT * (uxT * dUx + uyT * dUy - cvT * dCv)) +
+               l3 * r3 * (hT + cT * cvT)) *
+              magSf;
+}
+
+template <class D>
+__device__ __forceinline__ void kfvs_flux_fast(D& rhoFlux, D& rhoUxFlux, D& rhoUyFlux, D& rhoEFlux, const D rhoL,
+                                               const D rhoR, const D pL, const D pR, const D uxL, const D uxR,
+                                               const D uyL, const D uyR, const D tL, const D tR, const D R, const D Cv,
+                                               const D K, const D magSf, const D nfx, const D nfy) {
+  const D Sfx = nfx * magSf, Sfy = nfy * magSf;
+  const D uLl = uxL * nfx + uyL * nfy;
+  const D vLl = uyL * nfx - uxL * nfy;
+  const D uRl = uxR * nfx + uyR * nfy;
+  const D vRl = uyR * nfx - uxR * nfy;
+  const D ilamL = D(2) * R * tL, ilamR = D(2) * R * tR;  // 1/lambda = 2 p / rho
+  const D lamL = fdiv(D(1), ilamL), lamR = fdiv(D(1), ilamR);
+  const D PI = std::is_same<D, float>::value ? (D)3.141593f : (D)3.14159265358979323846;
+  const D m0p = D(0.5) * erfc_(-sqr_(lamL) * uLl);
+  const D m1p = uLl * m0p + D(0.5) * exp_(-lamL * uLl * uLl) * rsqrt_(PI * lamL);
+  const D m2p = uLl * m1p + D(0.5) * m0p * ilamL;
+  const D m3p = uLl * m2p + m1p * ilamL;
+  const D m0n = D(0.5) * erfc_(sqr_(lamR) * uRl);
+  const D m1n = uRl * m0n - D(0.5) * exp_(-lamR * uRl * uRl) * rsqrt_(PI * lamR);
+  const D m2n = uRl * m1n + D(0.5) * m0n * ilamR;
+  const D m3n = uRl * m2n + m1n * ilamR;
+  const D trho = rhoL * m1p + rhoR * m1n;
+  const D trhoUx = rhoL * m2p + rhoR * m2n;
+  const D trhoUy = rhoL * m1p * vLl + rhoR * m1n * vRl;
+  const D trhoE = D(0.5) * rhoL * (m3p + m1p * (vLl * vLl + D(0.5) * ilamL) + m1p * K * D(0.5) * ilamL) +
+                  D(0.5) * rhoR * (m3n + m1n * (vRl * vRl + D(0.5) * ilamR) + m1n * K * D(0.5) * ilamR);
+  rhoUxFlux += trhoUx * Sfx - trhoUy * Sfy - D(0.5) * (rhoFlux * uxL + pL * Sfx) - D(0.5) * (rhoFlux * uxR + pR * Sfx);
+  rhoUyFlux += trhoUx * Sfy + trhoUy * Sfx - D(0.5) * (rhoFlux * uyL + pL * Sfy) - D(0.5) * (rhoFlux * uyR + pR * Sfy);
+  rhoEFlux += trhoE * magSf - D(0.5) * rhoFlux * (Cv * tL + D(0.5) * (uxL * uxL + uyL * uyL) + R * tL) -
+              D(0.5) * rhoFlux * (Cv * tR + D(0.5) * (uxR * uxR + uyR * uyR) + R * tR);
+  rhoFlux += trho * magSf - D(0.5) * rhoL * (uxL * Sfx + uyL * Sfy) - D(0.5) * rhoR * (uxR * Sfx + uyR * Sfy);
+}
+
 // Out-of-line dissipation with the reference's parameter passing (outputs by reference, float
 // states by const reference) behind a device function-pointer table like the reference's
 // calcFlux[] (cudaRiemannSolver.h:139-152); used by the ref policy's k_flux_ref_layout.
@@ -1066,13 +1157,17 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
     const bool isShock = sL < 0 || sR < 0;
     const V4<G> fs = a.fs[id];
     const G Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
-    G R, Cv;
+    G R, Cv, iR, gam;
     if constexpr (kF32) {
       R = a.Rf;
       Cv = a.Cvf;
+      iR = a.invRf;
+      gam = a.gm1f + 1.f;
     } else {
       R = (G)a.R;
       Cv = (G)a.Cv;
+      iR = (G)a.invR;
+      gam = (G)a.gamma;
     }
     const V4<typename P::W> Wo = a.W[own], Wn = a.W[nei];
     const V4<G> go0 = a.grad[2 * own], go1 = a.grad[2 * own + 1];
@@ -1086,47 +1181,41 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
       const G uxLT = (G)Wo.y + lo.y * (go0.z * dxL + go1.x * dyL);
       const G uyLT = (G)Wo.z + lo.z * (go0.w * dxL + go1.y * dyL);
       const G tLT = (G)Wo.w + lo.w * (go1.z * dxL + go1.w * dyL);
-      const G rhoLT = pLT / (R * tLT);
+      const G rhoLT = fdiv(pLT * iR, tLT);
       const G pRT = (G)Wn.x + ln.x * (gn0.x * dxR + gn0.y * dyR);
       const G uxRT = (G)Wn.y + ln.y * (gn0.z * dxR + gn1.x * dyR);
       const G uyRT = (G)Wn.z + ln.z * (gn0.w * dxR + gn1.y * dyR);
       const G tRT = (G)Wn.w + ln.w * (gn1.z * dxR + gn1.w * dyR);
-      const G rhoRT = pRT / (R * tRT);
+      const G rhoRT = fdiv(pRT * iR, tRT);
       const G pL = pick<P>(!tvdL, tvdL, fo.x, pLT);
       const G uxL = pick<P>(!tvdL, tvdL, fo.y, uxLT);
       const G uyL = pick<P>(!tvdL, tvdL, fo.z, uyLT);
       const G tL = pick<P>(!tvdL, tvdL, fo.w, tLT);
-      const G rhoL = pL / (R * tL);
+      const G rhoL = fdiv(pL * iR, tL);
       const G pR = pick<P>(!tvdR, tvdR, fn.x, pRT);
       const G uxR = pick<P>(!tvdR, tvdR, fn.y, uxRT);
       const G uyR = pick<P>(!tvdR, tvdR, fn.z, uyRT);
       const G tR = pick<P>(!tvdR, tvdR, fn.w, tRT);
-      const G rhoR = pR / (R * tR);
+      const G rhoR = fdiv(pR * iR, tR);
       dP = min_delta<D, G>(pL, pR, pLT, pRT);
       dRho = min_delta<D, G>(rhoL, rhoR, rhoLT, rhoRT);
       const G h = G(0.5);
       rhoFlux = h * rhoL * (uxL * Sfx + uyL * Sfy) + h * rhoR * (uxR * Sfx + uyR * Sfy);
       rhoUxFlux = h * (rhoFlux * uxL + pL * Sfx) + h * (rhoFlux * uxR + pR * Sfx);
       rhoUyFlux = h * (rhoFlux * uyL + pL * Sfy) + h * (rhoFlux * uyR + pR * Sfy);
-      rhoEFlux = h * rhoFlux * (Cv * tL + h * (uxL * uxL + uyL * uyL) + pL / rhoL) +
-                 h * rhoFlux * (Cv * tR + h * (uxR * uxR + uyR * uyR) + pR / rhoR);
+      rhoEFlux = h * rhoFlux * (Cv * tL + h * (uxL * uxL + uyL * uyL) + R * tL) +  // p/rho = R T
+                 h * rhoFlux * (Cv * tR + h * (uxR * uxR + uyR * uyR) + R * tR);
       pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
       pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
     }
-    RC Rr, Cvr;
-    if constexpr (std::is_same<RC, float>::value && kF32) {
-      Rr = a.Rf;
-      Cvr = a.Cvf;
-    } else {
-      Rr = (RC)a.R;
-      Cvr = (RC)a.Cv;
-    }
+    static_assert(std::is_same<D, G>::value, "fp64 and mixed run the dissipation in their face-value type");
+    const G nfx = Sfx * fs.w, nfy = Sfy * fs.w;  // fs.w = 1/|Sf| (setup)
     if (isShock)
-      kfvs_flux<D, RC, G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
-                          tRf, Rr, Cvr, (D)magSf, (D)Sfx, (D)Sfy);
+      kfvs_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
+                        tRf, R, Cv, G(2) * Cv * iR - G(2), magSf, nfx, nfy);
     else
-      roe_flux<D, RC, G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
-                         tRf, dP, dRho, Rr, Cvr, (D)magSf, (D)Sfx, (D)Sfy);
+      roe_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, uxLf, uxRf, uyLf, uyRf, tLf, tRf, dP,
+                       dRho, R, Cv, gam, magSf, nfx, nfy);
     a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)rhoUxFlux, (typename P::F)rhoUyFlux,
                                    (typename P::F)rhoEFlux};
     if constexpr (DT && kF32) {
@@ -1644,7 +1733,9 @@ __global__ void k_setup_face_geom(StageArgs<P> a, const V4<double>* faceXY, cons
   if (f >= a.Nf + a.Nb) return;
   const V4<double> xy = faceXY[f];  // x, y
   const V4<double> s = faceS[f];    // Sfx, Sfy, magSf
-  const_cast<V4<G>*>(a.fs)[f] = V4<G>{(G)s.x, (G)s.y, (G)s.z, G(0)};
+  // fs.w: 1/|Sf| for the dissipation of the policies without bit parity (the ref policy's flux
+  // divides like the reference)
+  const_cast<V4<G>*>(a.fs)[f] = V4<G>{(G)s.x, (G)s.y, (G)s.z, P::id == PolicyRef::id ? G(0) : (G)(1.0 / s.z)};
   if (f < a.Nf) {
     const int2 on = a.on[f];
     const V2<double> co = a.cellC[on.x], cn = a.cellC[on.y];
