@@ -232,6 +232,7 @@ class FoamCase:
     delta_t: float
     adjust_time_step: bool
     max_co: float
+    recalc_basis: bool = True  # fvSchemes CUDA recalcBasis: false reads system/basis{Own,Nei}List
 
 
 def _uniform(v):
@@ -288,7 +289,11 @@ def load_case(case_dir: str, renumber: bool = True) -> FoamCase:
                     write_interval=float(control.get("writeInterval", control["endTime"])),
                     delta_t=float(control.get("deltaT", 0.0)),
                     adjust_time_step=str(control.get("adjustTimeStep", "no")) in ("true", "yes", "on", "1"),
-                    max_co=max_co)
+                    max_co=max_co, recalc_basis=_truth(cuda.get("recalcBasis", "true")))
+
+
+def _truth(v) -> bool:
+    return str(v) in ("true", "yes", "on", "1")
 
 
 # ----------------------------------------------------------------------------------- writing
@@ -403,6 +408,87 @@ def read_field(path: str) -> np.ndarray:
     return np.array([float(x) for x in body.split()])[:n]
 
 
+# ----------------------------------------------------------------------------------- RBF basis files
+BASIS_FILES = ("basisOwnList", "basisNeiList")
+
+
+def _basis_layout(hf):
+    """Per internal face and side: the stencil length (the cell itself first) and the offset of the
+    face's row in the bundle's ``RBFbasis`` (2*(maxStencilSize+1) values per face, owner side then
+    neighbour side)."""
+    nf, maxS = hf.sizes["facesNum"], hf.sizes["maxStencilSize"]
+    nb = hf.a["neighbour"].reshape(nf, 2)
+    ss = hf.a["stencilSize"].astype(np.int64)
+    lens = np.stack([ss[nb[:, 0]] + 1, ss[nb[:, 1]] + 1])  # (2, nf)
+    base = np.arange(nf, dtype=np.int64) * 2 * (maxS + 1)
+    return lens, np.stack([base, base + maxS + 1])
+
+
+def write_basis_lists(system_dir: str, hf, precision: int = 17):
+    """``basisOwnList`` and ``basisNeiList``: the O3 RBF weights of every internal face as OpenFOAM
+    ascii ``IOList<List<scalar>>`` files, one list per face with the owner's (neighbour's) stencil
+    length, the cell itself first -- the files the reference writes beside its case dictionaries
+    after computing the weights (basicCUDAsolver.cpp:538-651).  The values are the double weights
+    when the bundle carries them (``RBFbasis64``), else its float weights; ``precision`` significant
+    digits (17 reads back bit-exact)."""
+    os.makedirs(system_dir, exist_ok=True)
+    w = hf.a.get("RBFbasis64")
+    if w is None or w.shape[0] != hf.a["RBFbasis"].shape[0]:
+        w = hf.a["RBFbasis"].astype(np.float64)
+    lens, starts = _basis_layout(hf)
+    fmt = f"{{:.{precision}g}}"
+    for side, name in enumerate(BASIS_FILES):
+        with open(os.path.join(system_dir, name), "w") as f:
+            f.write(_header("scalarListList", name, "system"))
+            f.write(f"{lens.shape[1]}\n(\n")
+            for n, o in zip(lens[side].tolist(), starts[side].tolist()):
+                f.write(f"{n}(" + " ".join(fmt.format(v) for v in w[o:o + n].tolist()) + ")\n")
+            f.write(")\n")
+
+
+def _read_list_list(path: str, lens: np.ndarray) -> np.ndarray:
+    """The values of an ascii ``List<List<scalar>>`` whose inner lengths must equal ``lens``,
+    concatenated.  Inner lists may be written on one line (``n(a b c)``) or one value per line,
+    as OpenFOAM writes lists longer than ten."""
+    txt = _strip_comments(open(path).read())
+    m = re.search(r"FoamFile\s*\{(.*?)\}", txt, re.S)
+    if m and re.search(r"format\s+binary", m.group(1)):
+        raise ValueError(f"{path}: binary lists are not supported; write the case in ascii")
+    body = txt[m.end():] if m else txt
+    if "{" in body:
+        raise ValueError(f"{path}: uniform list notation n{{v}} is not supported")
+    a = np.fromstring(body.replace("(", " ").replace(")", " "), dtype=np.float64, sep=" ")
+    n = lens.shape[0]
+    if a.shape[0] < 1 or a[0] != n:
+        raise ValueError(f"{path}: {int(a[0]) if a.shape[0] else 0} lists, the mesh has {n} internal faces")
+    heads = 1 + np.concatenate([[0], np.cumsum(lens + 1)[:-1]])
+    if a.shape[0] != 1 + int((lens + 1).sum()) or not np.array_equal(a[heads], lens):
+        bad = np.nonzero(a[heads[heads < a.shape[0]]] != lens[heads < a.shape[0]])[0]
+        face = int(bad[0]) if bad.shape[0] else int(np.searchsorted(heads, a.shape[0]))
+        raise ValueError(f"{path}: the list of face {face} does not have the stencil's length "
+                         f"{int(lens[min(face, n - 1)])}")
+    idx = np.repeat(heads + 1, lens) + (np.arange(int(lens.sum())) - np.repeat(np.cumsum(lens) - lens, lens))
+    return a[idx]
+
+
+def read_basis_lists(system_dir: str, hf):
+    """Replaces the bundle's O3 weights by those in ``basisOwnList``/``basisNeiList`` (the
+    reference's ``recalcBasis false`` path, basicCUDAsolver.cpp:653-694): each face's double values
+    go to ``RBFbasis64`` and, rounded to float, to ``RBFbasis``; entries past a stencil's length are
+    zero.  The lists must match the mesh's stencils (count and length), else ValueError."""
+    lens, starts = _basis_layout(hf)
+    n = hf.a["RBFbasis"].shape[0]
+    w64 = np.zeros(n, dtype=np.float64)
+    for side, name in enumerate(BASIS_FILES):
+        vals = _read_list_list(os.path.join(system_dir, name), lens[side])
+        dst = np.repeat(starts[side], lens[side]) + (
+            np.arange(vals.shape[0]) - np.repeat(np.cumsum(lens[side]) - lens[side], lens[side]))
+        w64[dst] = vals
+    hf.a["RBFbasis64"] = w64
+    hf.a["RBFbasis"] = w64.astype(np.float32)
+    return hf
+
+
 # ----------------------------------------------------------------------------------- running a case
 def run_case(case_dir: str, out_dir: str | None = None, policy: str = "mixed", device: int = 0, chunk: int = 50,
              write: bool = True):
@@ -410,13 +496,21 @@ def run_case(case_dir: str, out_dir: str | None = None, policy: str = "mixed", d
     the case, mesh it, precompute, then step to ``endTime`` with the device CFL step (or the fixed
     ``deltaT`` when ``adjustTimeStep`` is off), landing on every write time like OpenFOAM's
     adjustableRunTime and writing ``p``, ``U``, ``T``, ``shockIndicator`` there (and the initial
-    fields and ``constant/polyMesh``) under ``out_dir``.  Returns the write times, the steps taken
+    fields and ``constant/polyMesh``) under ``out_dir``.  With ``recalcBasis false`` in the case's
+    fvSchemes the O3 weights come from ``system/basisOwnList``/``basisNeiList`` of ``case_dir``
+    (which must exist); otherwise they are computed and, when writing, saved to
+    ``out_dir/system`` (basicCUDAsolver.cpp:59,626-694).  Returns the write times, the steps taken
     and the solver's final time."""
     from .solver import CudaSolver, precompute
 
     case = load_case(case_dir)
     m = case.mesh
-    hf = precompute(m, case.config, case.W, case.Wb, want_rbf64=policy == "fp64")
+    save_basis = case.recalc_basis and write and out_dir
+    hf = precompute(m, case.config, case.W, case.Wb, want_rbf64=policy == "fp64" or bool(save_basis))
+    if not case.recalc_basis:
+        read_basis_lists(os.path.join(case_dir, "system"), hf)
+    elif save_basis:
+        write_basis_lists(os.path.join(out_dir, "system"), hf)
     s = CudaSolver(hf, case.config, policy=policy, device=device)
     try:
         if write and out_dir:

@@ -35,7 +35,7 @@ CUDA
     R 0.714285714285714;
     Cv 1.785714285714286;
     stencilType edgeNeighbour;
-    boundary { patch0 3; patch1 4; patch2 2; }   // inflow, outflow, walls
+%(recalc)s    boundary { patch0 3; patch1 4; patch2 2; }   // inflow, outflow, walls
 }
 ddtSchemes { default Euler; }
 """
@@ -63,7 +63,7 @@ boundaryField
 """
 
 
-def write_case(root, n=4, end=0.02, wi=0.005):
+def write_case(root, n=4, end=0.02, wi=0.005, recalc_basis=None):
     """Blocks of (3n x n), (3n x 4n), (12n x 4n) cells."""
     for d in ("system", "0", "constant"):
         os.makedirs(os.path.join(root, d), exist_ok=True)
@@ -73,7 +73,8 @@ def write_case(root, n=4, end=0.02, wi=0.005):
             f.write(HEADER % obj + "\n" + body)
 
     put("system/blockMeshDict", "blockMeshDict", BLOCK_MESH % {"na": 3 * n, "nb": n, "nc": 4 * n, "nd": 12 * n})
-    put("system/fvSchemes", "fvSchemes", SCHEMES)
+    recalc = "" if recalc_basis is None else f"    recalcBasis {'true' if recalc_basis else 'false'};\n"
+    put("system/fvSchemes", "fvSchemes", SCHEMES % {"recalc": recalc})
     put("system/controlDict", "controlDict", CONTROL % {"end": end, "wi": wi})
     put("0/p", "p", FIELD % {"dims": "[1 -1 -2 0 0 0 0]", "val": "1", "wall": "zeroGradient"})
     put("0/U", "U", FIELD % {"dims": "[0 1 -1 0 0 0 0]", "val": "(3 0 0)", "wall": "slip"})

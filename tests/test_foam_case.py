@@ -89,3 +89,72 @@ def test_reference_corner_flow_case_loads():
     assert [(p[0], p[1], p[3]) for p in m.patches] == [("inlet", 5, 250), ("obstacle", 2, 1250), ("outlet", 4, 500)]
     assert case.config.cOrder == 7 and case.config.fOrder == 5 and case.config.stencilType == "edgeNeighbour"
     assert case.end_time == 0.15 and case.write_interval == 0.01 and case.max_co == 0.3
+
+
+def test_basis_lists_round_trip(tmp_path):
+    """basisOwnList/basisNeiList (basicCUDAsolver.cpp:538-694): written with 17 digits and read
+    back, the weights are bit-identical in double and float; one list per internal face with the
+    stencil's length."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam, precompute
+    from afar_cudaeuler2dmixo3rk3solver_gb300.solver import HostFields
+
+    case = foam.load_case(write_case(str(tmp_path / "case"), n=2))
+    hf = precompute(case.mesh, case.config, case.W, case.Wb, want_rbf64=True)
+    sysd = str(tmp_path / "system")
+    foam.write_basis_lists(sysd, hf)
+    nf = hf.sizes["facesNum"]
+    own = open(os.path.join(sysd, "basisOwnList")).read()
+    assert "class       scalarListList;" in own and f"\n{nf}\n(\n" in own
+    back = HostFields(hf.sizes, {k: (v.copy() if k != "RBFbasis" else np.zeros_like(v)) for k, v in hf.a.items()})
+    del back.a["RBFbasis64"]
+    foam.read_basis_lists(sysd, back)
+    assert np.array_equal(back.a["RBFbasis64"], hf.a["RBFbasis64"])
+    assert np.array_equal(back.a["RBFbasis"], hf.a["RBFbasis"])
+    assert back.a["RBFbasis"].dtype == np.float32
+
+
+def test_basis_lists_openfoam_long_list_form_and_errors(tmp_path):
+    """OpenFOAM writes inner lists longer than ten one value per line; both forms read the same.
+    A list count or a list length that does not match the mesh's stencils is an error."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam, precompute
+
+    case = foam.load_case(write_case(str(tmp_path / "case"), n=2))
+    hf = precompute(case.mesh, case.config, case.W, case.Wb, want_rbf64=True)
+    sysd = str(tmp_path / "system")
+    foam.write_basis_lists(sysd, hf)
+    ref = hf.a["RBFbasis64"].copy()
+    path = os.path.join(sysd, "basisNeiList")
+    lines = open(path).read().split("\n")
+    long = []
+    for ln in lines:
+        m = __import__("re").match(r"^(\d+)\((.*)\)$", ln)
+        if m:
+            long += [m.group(1), "("] + m.group(2).split() + [")"]
+        else:
+            long.append(ln)
+    open(path, "w").write("\n".join(long))
+    foam.read_basis_lists(sysd, hf)
+    assert np.array_equal(hf.a["RBFbasis64"], ref)
+    txt = open(os.path.join(sysd, "basisOwnList")).read()
+    n0 = int(__import__("re").search(r"\n(\d+)\(", txt).group(1))
+    bad = txt.replace(f"\n{n0}(", f"\n{n0 + 1}(0 ", 1)
+    open(os.path.join(sysd, "basisOwnList"), "w").write(bad)
+    with pytest.raises(ValueError, match="face 0"):
+        foam.read_basis_lists(sysd, hf)
+    nf = hf.sizes["facesNum"]
+    open(os.path.join(sysd, "basisOwnList"), "w").write(txt.replace(f"\n{nf}\n(", f"\n{nf - 1}\n(", 1))
+    with pytest.raises(ValueError, match="internal faces"):
+        foam.read_basis_lists(sysd, hf)
+
+
+def test_recalc_basis_switch(tmp_path):
+    """fvSchemes CUDA recalcBasis: absent or true computes the weights; false reads them from the
+    case's system directory and fails without the files."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam, precompute
+
+    assert foam.load_case(write_case(str(tmp_path / "a"), n=1)).recalc_basis
+    case = foam.load_case(write_case(str(tmp_path / "b"), n=1, recalc_basis=False))
+    assert not case.recalc_basis
+    hf = precompute(case.mesh, case.config, case.W, case.Wb)
+    with pytest.raises(FileNotFoundError):
+        foam.read_basis_lists(str(tmp_path / "b" / "system"), hf)

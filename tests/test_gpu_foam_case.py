@@ -60,3 +60,25 @@ def test_write_interval_spreads_the_steps_to_the_write_time(tmp_path):
         else:
             plain = dts
     assert len(dts) <= len(plain) + 1
+
+
+def test_recalc_basis_false_reuses_the_written_weights(tmp_path):
+    """A first run computes the O3 weights and writes system/basisOwnList/basisNeiList; a case with
+    recalcBasis false reads them and steps to bit-identical fields (the weights read back exactly)."""
+    import shutil
+
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    first = write_case(str(tmp_path / "a"), n=2, end=0.004, wi=0.002)
+    foam.run_case(first, first, policy="fp64")
+    assert os.path.exists(os.path.join(first, "system", "basisOwnList"))
+    second = write_case(str(tmp_path / "b"), n=2, end=0.004, wi=0.002, recalc_basis=False)
+    for name in foam.BASIS_FILES:
+        shutil.copy(os.path.join(first, "system", name), os.path.join(second, "system", name))
+    res = foam.run_case(second, second, policy="fp64")
+    assert res["time"] == pytest.approx(0.004, rel=1e-12)
+    for t in ("0.002", "0.004"):
+        for f in ("p", "U", "T"):
+            a = foam.read_field(os.path.join(first, t, f))
+            b = foam.read_field(os.path.join(second, t, f))
+            assert np.array_equal(a, b), (t, f)
