@@ -220,6 +220,155 @@ def block_mesh_2d(bmd: FoamDict, labels: dict, renumber: bool = True) -> M.FoamM
                              depth=depth if depth > 0 else 1.0)
 
 
+# ----------------------------------------------------------------------------------- polyMesh (2-D)
+def _body(path: str) -> str:
+    """A file's text after its FoamFile header, comments removed; ascii only."""
+    txt = _strip_comments(open(path).read())
+    m = re.search(r"FoamFile\s*\{(.*?)\}", txt, re.S)
+    if m and re.search(r"format\s+binary", m.group(1)):
+        raise ValueError(f"{path}: binary files are not supported; write the case in ascii")
+    return txt[m.end():] if m else txt
+
+
+def _read_numbers(path: str, per_item: int, dtype) -> np.ndarray:
+    """``N ( item ... )`` with items of ``per_item`` numbers (``(x y z)`` or a bare label)."""
+    a = np.fromstring(_body(path).replace("(", " ").replace(")", " "), dtype=np.float64, sep=" ")
+    n = int(a[0]) if a.shape[0] else -1
+    if n < 0 or a.shape[0] != 1 + n * per_item:
+        raise ValueError(f"{path}: malformed list ({a.shape[0] - 1} numbers for {n} items of {per_item})")
+    out = a[1:].reshape(n, per_item) if per_item > 1 else a[1:]
+    return out.astype(dtype)
+
+
+def _read_label_lists(path: str):
+    """A ``List<labelList>`` (the polyMesh ``faces``) as CSR: offsets (N+1,), labels."""
+    a = np.fromstring(_body(path).replace("(", " -1 ").replace(")", " -2 "), dtype=np.float64, sep=" ")
+    if a.shape[0] < 3 or a[1] != -1 or a[-1] != -2:
+        raise ValueError(f"{path}: malformed list of lists")
+    n = int(a[0])
+    opens = np.nonzero(a == -1)[0][1:]
+    counts = a[opens - 1].astype(np.int64)
+    if opens.shape[0] != n or np.any(counts < 0) or np.any(a[opens + 1 + counts] != -2):
+        raise ValueError(f"{path}: malformed list of lists ({opens.shape[0]} lists for {n})")
+    off = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=off[1:])
+    idx = np.repeat(opens + 1, counts) + (np.arange(off[-1]) - np.repeat(off[:-1], counts))
+    return off, a[idx].astype(np.int64)
+
+
+def _read_boundary(path: str):
+    """The polyMesh ``boundary`` file: [(name, type, nFaces, startFace)] in file order."""
+    out = []
+    for name, body in re.findall(r'([^\s{}()";]+)\s*\{([^{}]*)\}', _body(path)):
+        e = parse_foam(body)
+        out.append((name, str(e.get("type", "patch")), int(e["nFaces"]), int(e["startFace"])))
+    return out
+
+
+def read_poly_mesh(case_dir: str, labels: dict | None = None, renumber: bool = False) -> M.FoamMesh:
+    """The 2-D cross-section of the one-cell-deep polyMesh in ``case_dir/constant/polyMesh`` (what the
+    reference's solver reads through OpenFOAM, basicCUDAsolver.cpp:122-258).
+
+    The mesh must be extruded along z between two planes: every face with two points on each plane
+    is a face of the 2-D mesh (internal, or of a boundary patch), every face on one plane lies in the
+    ``empty`` patch, and each cell's face on the lower plane gives its polygon.  ``labels`` maps a
+    patch's index in the boundary file (empty patches included, as fvSchemes ``CUDA { boundary {
+    patch<k> ...; } }`` counts them) to its cudaEulerBCs label; a missing label is an error, like the
+    reference's lookup.  Face order, owners and neighbours are kept as the file has them (the
+    reference runs on the mesh as renumberMesh left it); ``renumber`` applies reverse Cuthill-McKee."""
+    d = os.path.join(case_dir, "constant", "polyMesh")
+    P3 = _read_numbers(os.path.join(d, "points"), 3, np.float64)
+    foff, flab = _read_label_lists(os.path.join(d, "faces"))
+    owner = _read_numbers(os.path.join(d, "owner"), 1, np.int64)
+    neigh = _read_numbers(os.path.join(d, "neighbour"), 1, np.int64)
+    bnd = _read_boundary(os.path.join(d, "boundary"))
+    nF, nI = foff.shape[0] - 1, neigh.shape[0]
+    if owner.shape[0] != nF or (flab.size and (flab.min() < 0 or flab.max() >= P3.shape[0])):
+        raise ValueError("polyMesh: faces, owner and points do not agree")
+    nc = int(max(owner.max(initial=-1), neigh.max(initial=-1))) + 1
+    z = P3[:, 2]
+    z0, z1 = float(z.min()), float(z.max())
+    depth = z1 - z0
+    tol = 1e-9 * max(depth, np.abs(P3[:, :2]).max(initial=0.0), 1e-300)
+    lo, hi = np.abs(z - z0) <= tol, np.abs(z - z1) <= tol
+    if depth <= 0 or not np.all(lo | hi):
+        raise ValueError("polyMesh: not a one-cell-deep mesh between two planes of constant z")
+    cnt = np.diff(foff)
+    face_of = np.repeat(np.arange(nF), cnt)
+    nlo = np.bincount(face_of, weights=lo[flab], minlength=nF).astype(np.int64)
+    side = (cnt == 4) & (nlo == 2)
+    front = nlo == cnt
+    plane = front | (nlo == 0)
+    if not np.all(side | plane):
+        raise ValueError("polyMesh: a face is neither a side face nor on a z plane")
+    if not np.all(side[:nI]):
+        raise ValueError("polyMesh: an internal face is not a side face (not a 2-D mesh)")
+
+    # patches: empty ones hold exactly the plane faces
+    patches, keep = [], [np.arange(nI)]
+    start = nI
+    for k, (name, ptype, size, pstart) in enumerate(bnd):
+        f = np.arange(pstart, pstart + size)
+        if ptype == "empty":
+            if not np.all(plane[f]):
+                raise ValueError(f"polyMesh: the empty patch {name} holds side faces")
+            continue
+        if not np.all(side[f]):
+            raise ValueError(f"polyMesh: the patch {name} holds faces on a z plane; make it empty")
+        if size == 0:
+            continue
+        if labels is None or k not in labels:
+            raise ValueError(f"no cudaEulerBCs label for patch{k} ({name}) in fvSchemes CUDA boundary")
+        patches.append((name, int(labels[k]), start, size))
+        keep.append(f)
+        start += size
+    keep = np.concatenate(keep)
+    if keep.shape[0] != int(side.sum()):
+        raise ValueError("polyMesh: side faces outside the internal faces and the patches")
+
+    # 2-D points: those of the lower plane, in file order
+    pid = np.full(P3.shape[0], -1, dtype=np.int64)
+    pid[lo] = np.arange(int(lo.sum()))
+    pts = P3[lo, :2].copy()
+
+    # cell polygons: each cell's lower-plane face, counter-clockwise
+    fr = np.nonzero(front)[0]
+    cell = owner[fr]
+    if fr.shape[0] != nc or np.unique(cell).shape[0] != nc:
+        raise ValueError("polyMesh: every cell needs exactly one face on the lower plane")
+    fr = fr[np.argsort(cell)]
+    ccnt = cnt[fr]
+    cptr = np.zeros(nc + 1, dtype=np.int64)
+    np.cumsum(ccnt, out=cptr[1:])
+    cpts = pid[flab[np.repeat(foff[fr], ccnt) + (np.arange(cptr[-1]) - np.repeat(cptr[:-1], ccnt))]]
+    _, area = M._polygon_centroids(pts, cptr, cpts)
+    for c in np.nonzero(area < 0)[0]:
+        cpts[cptr[c]:cptr[c + 1]] = cpts[cptr[c]:cptr[c + 1]][::-1].copy()
+
+    # 2-D faces: the lower-plane edge of each side face, ordered so (dy, -dx) points out of the owner
+    sl = flab[foff[keep][:, None] + np.arange(4)[None, :]]
+    on = lo[sl]
+    first = np.argmax(on, axis=1)
+    second = 3 - np.argmax(on[:, ::-1], axis=1)
+    a, b = sl[np.arange(keep.shape[0]), first], sl[np.arange(keep.shape[0]), second]
+    Q = P3[sl]  # (F, 4, 3): the face's area vector (sum of edge cross products) in x-y
+    nx = np.zeros(keep.shape[0])
+    ny = np.zeros(keep.shape[0])
+    for i in range(4):
+        p, q = Q[:, i], Q[:, (i + 1) % 4]
+        nx += p[:, 1] * q[:, 2] - p[:, 2] * q[:, 1]
+        ny += p[:, 2] * q[:, 0] - p[:, 0] * q[:, 2]
+    pa, pb = P3[a], P3[b]
+    flip = (pb[:, 1] - pa[:, 1]) * nx - (pb[:, 0] - pa[:, 0]) * ny < 0
+    a, b = np.where(flip, b, a), np.where(flip, a, b)
+    fpts = np.stack([pid[a], pid[b]], axis=1)
+    fown = owner[keep]
+    mesh = M.FoamMesh(points=pts, cell_ptr=cptr.astype(np.int32), cell_pts=cpts.astype(np.int32),
+                      face_pts=fpts.astype(np.int32), owner=fown.astype(np.int32),
+                      neighbour=neigh.astype(np.int32), patches=patches, depth=depth)
+    return M.renumber_mesh(mesh) if renumber else mesh
+
+
 # ----------------------------------------------------------------------------------- the case
 @dataclasses.dataclass
 class FoamCase:
@@ -235,54 +384,126 @@ class FoamCase:
     recalc_basis: bool = True  # fvSchemes CUDA recalcBasis: false reads system/basis{Own,Nei}List
 
 
-def _uniform(v):
+_NONUNIFORM = re.compile(r"nonuniform\s+List<(scalar|vector)>\s*(\d+)\s*\(")
+_VECTOR_BODY = re.compile(r"(?:\s*\([^()]*\))*\s*\)")
+_SLIP = ("slip", "symmetryPlane", "symmetry")
+
+
+def read_field_dict(path: str):
+    """A volField file as a FoamDict, its ``nonuniform List<...>`` values read by numpy into arrays
+    ((N,) for scalars, (N, 3) for vectors) instead of being tokenised."""
+    txt = _strip_comments(open(path).read())
+    arrays, parts, i = [], [], 0
+    while True:
+        m = _NONUNIFORM.search(txt, i)
+        if not m:
+            break
+        kind, n = m.group(1), int(m.group(2))
+        if kind == "scalar":
+            end = txt.index(")", m.end()) + 1
+        else:
+            e = _VECTOR_BODY.match(txt, m.end())
+            if not e:
+                raise ValueError(f"{path}: malformed vector list")
+            end = e.end()
+        a = np.fromstring(txt[m.end():end - 1].replace("(", " ").replace(")", " "), dtype=np.float64, sep=" ")
+        k = 3 if kind == "vector" else 1
+        if a.shape[0] != n * k:
+            raise ValueError(f"{path}: a list of {n} {kind}s holds {a.shape[0]} numbers")
+        arrays.append(a.reshape(n, 3) if k == 3 else a)
+        parts += [txt[i:m.start()], f" __afar_list_{len(arrays) - 1}__ "]
+        i = end
+    parts.append(txt[i:])
+    d = parse_foam("".join(parts))
+
+    def resolve(v):
+        if isinstance(v, str) and v.startswith("__afar_list_"):
+            return arrays[int(v[12:-2])]
+        if isinstance(v, list):
+            return [resolve(x) for x in v]
+        if isinstance(v, dict):
+            for key in v:
+                v[key] = resolve(v[key])
+        return v
+
+    return resolve(d)
+
+
+def _values(v, n, is_vector, what):
+    """An entry's value as (n, 2) velocities (x, y) or (n, 1) scalars."""
     if isinstance(v, list) and len(v) == 2 and v[0] == "uniform":
-        return v[1]
-    raise ValueError(f"only uniform values are supported, got {v!r}")
+        a = np.asarray(v[1], dtype=np.float64)
+        return np.tile(a[:2] if is_vector else np.array([float(a)]), (n, 1))
+    if isinstance(v, np.ndarray):
+        if v.shape[0] != n:
+            raise ValueError(f"{what}: {v.shape[0]} values for {n}")
+        return v[:, :2].copy() if is_vector else v[:, None].copy()
+    raise ValueError(f"{what}: expected uniform or nonuniform values, got {v!r}")
 
 
-def _field_values(fdict, patches, n_cells, is_vector):
-    internal = _uniform(fdict["internalField"])
-    nb = sum(p[3] for p in patches)
-    cells = np.tile(np.asarray(internal, dtype=np.float64)[:2] if is_vector else [float(internal)], (n_cells, 1))
-    ghosts = np.tile(cells[0], (nb, 1))
+def _field_values(fdict, m: M.FoamMesh, is_vector):
+    """Cell values and the initial ghost value of every boundary face, the patch values OpenFOAM
+    gives the reference at construction (basicCUDAsolver.cpp:161-192): ``value`` where the patch
+    type stores one, the owner cell's value for zeroGradient and other value-less types, the
+    owner's tangential velocity for slip/symmetry (scalars: the owner's value), zero velocity for
+    noSlip."""
+    nc = m.n_cells
+    cells = _values(fdict["internalField"], nc, is_vector, "internalField")
     bf = fdict.get("boundaryField", {})
-    off = 0
-    for name, _, _, size in patches:
+    out = []
+    for name, _, start, size in m.patches:
         spec = bf.get(name, {})
-        if spec.get("type") == "fixedValue":
-            v = _uniform(spec["value"])
-            ghosts[off:off + size] = np.asarray(v, dtype=np.float64)[:2] if is_vector else float(v)
-        off += size
+        ptype = str(spec.get("type", "zeroGradient"))
+        own = m.owner[start:start + size]
+        if ptype in _SLIP and is_vector:
+            pa, pb = m.points[m.face_pts[start:start + size, 0]], m.points[m.face_pts[start:start + size, 1]]
+            nrm = np.stack([pb[:, 1] - pa[:, 1], pa[:, 0] - pb[:, 0]], axis=1)
+            nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+            u = cells[own]
+            out.append(u - nrm * np.sum(u * nrm, axis=1, keepdims=True))
+        elif ptype == "noSlip" and is_vector:
+            out.append(np.zeros((size, 2)))
+        elif "value" in spec and ptype not in ("zeroGradient",) + _SLIP:
+            out.append(_values(spec["value"], size, is_vector, f"{name} value"))
+        else:
+            out.append(cells[own])
+    ghosts = np.concatenate(out) if out else np.zeros((0, cells.shape[1]))
     return cells, ghosts
 
 
 def load_case(case_dir: str, renumber: bool = True) -> FoamCase:
     """The reference case in ``case_dir`` as solver inputs: the meshed cross-section, the case
     configuration (fvSchemes ``CUDA`` and ``gaussQuadrature``, controlDict ``maxCo``), the initial
-    cell states and ghost states, and the time controls."""
+    cell states and ghost states, and the time controls.  The mesh is ``constant/polyMesh`` when the
+    case has one (as the reference reads it), else ``system/blockMeshDict`` meshed here and, with
+    ``renumber``, reverse Cuthill-McKee ordered (the blockMesh + renumberMesh steps).  Initial
+    fields may be uniform or nonuniform."""
     from .solver import CaseConfig
 
     sysd = os.path.join(case_dir, "system")
     schemes = read_foam(os.path.join(sysd, "fvSchemes"))
     control = read_foam(os.path.join(sysd, "controlDict"))
-    bmd = read_foam(os.path.join(sysd, "blockMeshDict"))
     cuda = schemes["CUDA"]
     gq = schemes.get("gaussQuadrature", {})
-    bnd = bmd.get("boundary", [])
-    names = [bnd[k] for k in range(0, len(bnd), 2)]
     blabels = cuda.get("boundary", {})
-    labels = {name: int(blabels[f"patch{k}"]) for k, name in enumerate(names) if f"patch{k}" in blabels}
-    m = block_mesh_2d(bmd, labels, renumber=renumber)
+    if os.path.exists(os.path.join(case_dir, "constant", "polyMesh", "faces")):
+        by_index = {int(k[5:]): int(v) for k, v in blabels.items() if re.fullmatch(r"patch\d+", str(k))}
+        m = read_poly_mesh(case_dir, by_index)
+    else:
+        bmd = read_foam(os.path.join(sysd, "blockMeshDict"))
+        bnd = bmd.get("boundary", [])
+        names = [bnd[k] for k in range(0, len(bnd), 2)]
+        labels = {name: int(blabels[f"patch{k}"]) for k, name in enumerate(names) if f"patch{k}" in blabels}
+        m = block_mesh_2d(bmd, labels, renumber=renumber)
     max_co = float(control.get("maxCo", 0.5))
     cfg = CaseConfig(R=float(cuda["R"]), Cv=float(cuda["Cv"]), CFL=max_co,
                      stencilType=str(cuda.get("stencilType", "edgeNeighbour")),
                      shapeFactor=float(schemes.get("shapeFactor", 10.0)),
                      cOrder=int(gq.get("cOrder", 5)), fOrder=int(gq.get("fOrder", 4)))
     zero = os.path.join(case_dir, "0")
-    p, pb = _field_values(read_foam(os.path.join(zero, "p")), m.patches, m.n_cells, False)
-    U, Ub = _field_values(read_foam(os.path.join(zero, "U")), m.patches, m.n_cells, True)
-    T, Tb = _field_values(read_foam(os.path.join(zero, "T")), m.patches, m.n_cells, False)
+    p, pb = _field_values(read_field_dict(os.path.join(zero, "p")), m, False)
+    U, Ub = _field_values(read_field_dict(os.path.join(zero, "U")), m, True)
+    T, Tb = _field_values(read_field_dict(os.path.join(zero, "T")), m, False)
     W = np.concatenate([p, U, T], axis=1)
     Wb = np.concatenate([pb, Ub, Tb], axis=1)
     return FoamCase(mesh=m, config=cfg, W=W, Wb=Wb, end_time=float(control["endTime"]),
@@ -318,7 +539,7 @@ def write_poly_mesh(out_dir: str, m: M.FoamMesh):
     with open(os.path.join(d, "points"), "w") as f:
         f.write(_header("vectorField", "points", "constant/polyMesh"))
         f.write(f"{P3.shape[0]}\n(\n")
-        f.writelines(f"({_fmt(x)} {_fmt(y)} {_fmt(z)})\n" for x, y, z in P3)
+        f.writelines(f"({x!r} {y!r} {z!r})\n" for x, y, z in P3.tolist())  # shortest exact form
         f.write(")\n")
     fp = m.face_pts.astype(np.int64)
     side = [f"4({a} {b} {b + npt} {a + npt})" for a, b in fp]

@@ -213,6 +213,39 @@ def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=T
     )
 
 
+def renumber_mesh(m: FoamMesh) -> FoamMesh:
+    """``m`` with its cells in reverse Cuthill-McKee order (renumberMesh): internal faces back in
+    upper-triangular order (a face whose owner and neighbour swap has its points swapped, so its
+    normal still leaves the owner), boundary faces sorted by owner within each patch."""
+    nc, nf = m.n_cells, m.n_internal_faces
+    own = m.owner.astype(np.int64)
+    nei = m.neighbour.astype(np.int64)
+    perm = _rcm_permutation(nc, own[:nf], nei)
+    inv = np.empty(nc, dtype=np.int64)
+    inv[perm] = np.arange(nc)
+    o, n = inv[own[:nf]], inv[nei]
+    swap = o > n
+    fp = m.face_pts.astype(np.int64).copy()
+    fp[:nf][swap] = fp[:nf][swap][:, ::-1]
+    o, n = np.minimum(o, n), np.maximum(o, n)
+    fo = np.lexsort((n, o))
+    bown = inv[own[nf:]]
+    border = []
+    for _, _, start, size in m.patches:
+        seg = np.arange(start - nf, start - nf + size)
+        border.append(seg[np.argsort(bown[seg], kind="stable")])
+    bo = np.concatenate(border) if border else np.zeros(0, dtype=np.int64)
+    nv = np.diff(m.cell_ptr.astype(np.int64))[perm]
+    ptr = np.zeros(nc + 1, dtype=np.int64)
+    np.cumsum(nv, out=ptr[1:])
+    old = m.cell_ptr.astype(np.int64)[perm]
+    pts = m.cell_pts[np.repeat(old, nv) + (np.arange(ptr[-1]) - np.repeat(ptr[:-1], nv))]
+    return dataclasses.replace(
+        m, cell_ptr=ptr.astype(np.int32), cell_pts=pts.astype(np.int32),
+        face_pts=np.concatenate([fp[:nf][fo], fp[nf:][bo]]).astype(np.int32),
+        owner=np.concatenate([o[fo], bown[bo]]).astype(np.int32), neighbour=n[fo].astype(np.int32))
+
+
 # ------------------------------------------------------------------------------------ generators
 def quad_grid(nx, ny, x0=0.0, x1=1.0, y0=0.0, y1=1.0, classify=None, patch_defs=None,
               renumber=True, jitter=0.0, seed=0, tri_mask=None):

@@ -37,7 +37,13 @@ def test_forward_step_case_mesh_and_fields(tmp_path):
     assert case.config.cOrder == 5 and case.config.fOrder == 4 and case.config.CFL == 0.2
     assert case.adjust_time_step and case.end_time == 0.02 and case.write_interval == 0.005
     assert np.allclose(case.W, [1.0, 3.0, 0.0, 1.0])
-    assert np.allclose(case.Wb, [1.0, 3.0, 0.0, 1.0])
+    # OpenFOAM's initial patch values: slip walls keep the owner's tangential velocity, so the
+    # step's vertical face (normal -x) starts at rest; every other ghost is the free stream
+    fc = m.boundary_face_centres()
+    riser = np.isclose(fc[:, 0], 0.6) & (fc[:, 1] < 0.2)
+    assert riser.sum() == 2
+    assert np.allclose(case.Wb[riser], [1.0, 0.0, 0.0, 1.0])
+    assert np.allclose(case.Wb[~riser], [1.0, 3.0, 0.0, 1.0])
     hf = precompute(m, case.config, case.W, case.Wb)  # the native precompute accepts the mesh
     assert hf.nc == m.n_cells
 
