@@ -55,6 +55,7 @@ def build_lib(force=False, verbose=False) -> str:
     units = [
         ("afar_solver.cu", "nvcc"),
         ("afar_noalloc.cu", "nvcc"),
+        ("afar_precompute_gpu.cu", "nvcc_nofma"),
         ("afar_precompute.cpp", "cxx"),
         ("afar_error.cpp", "cxx"),
         ("afar_server.cpp", "cxx"),
@@ -69,6 +70,8 @@ def build_lib(force=False, verbose=False) -> str:
         if force or _stale(o, [s] + headers):
             if kind == "nvcc":
                 cmd = [nvcc] + NVCC_FLAGS + ["-c", s, "-o", o]
+            elif kind == "nvcc_nofma":  # bit-identical to the host precompute (-ffp-contract=off)
+                cmd = [nvcc] + NVCC_FLAGS + ["-fmad=false", "-c", s, "-o", o]
             else:
                 cmd = ["g++"] + CXX_FLAGS + ["-c", s, "-o", o]
             jobs.append(cmd)

@@ -491,9 +491,9 @@ static T* xalloc(size_t n) {
   return p;
 }
 
-extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar_caseConfig* cfg, const double* Wc,
-                                              const double* Wb, afar_fieldPointer* h, afar_fieldSizes* sz,
-                                              double** rbf64_out) {
+// The whole precompute; the RBF stage runs on CUDA device `device` when it is >= 0, else on the host.
+static afar_status precompute(const afar_polyMesh* m, const afar_caseConfig* cfg, const double* Wc, const double* Wb,
+                              int device, afar_fieldPointer* h, afar_fieldSizes* sz, double** rbf64_out) {
   if (rbf64_out) *rbf64_out = nullptr;
   if (!check_mesh(m)) return AFAR_ERR_ARGUMENT;
   if (!cfg || !Wc || !h || !sz) {
@@ -609,12 +609,19 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
         pc[fill[point_id(m, m->cellPoints[k])]++] = c;
   }
 
-  // ---- stencils (basicCUDAsolver.cpp:303-398)
+#ifdef _OPENMP
+  const int nthreads = cfg->nThreads > 0 ? cfg->nThreads : omp_get_max_threads();
+#endif
+  // ---- stencils (basicCUDAsolver.cpp:303-398); cells are independent
   const int MAXV = AFAR_MAX_VALID_STENCIL_SIZE;
   std::vector<int> sten((size_t)MAXV * nc, 0);
   h->stencilSize = xalloc<uint8_t>(nc);
   h->compactStencilSize = xalloc<uint8_t>(nc);
   int maxS = 0, maxM = 0;
+  int too_large = nc, too_large_size = 0;  // the first cell over the limit, as a serial walk reports it
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4096) num_threads(nthreads) reduction(max : maxS, maxM)
+#endif
   for (int c = 0; c < nc; ++c) {
     int tmp[64];
     int idx = 0;
@@ -648,13 +655,23 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
     maxS = std::max(maxS, idx);
     maxM = std::max(maxM, m0);
     if (idx > MAXV) {
-      set_error("Too large stencil! maxStencilSize = %d (cell %d, limit %d)", idx, c, MAXV);
-      afar_free_host_fields(h);
-      return AFAR_ERR_LIMIT;
+#ifdef _OPENMP
+#pragma omp critical(afar_stencil_limit)
+#endif
+      if (c < too_large) {
+        too_large = c;
+        too_large_size = idx;
+      }
+      continue;
     }
     for (int k = 0; k < idx; ++k) sten[(size_t)MAXV * c + k] = tmp[k];
     h->stencilSize[c] = (uint8_t)idx;
     h->compactStencilSize[c] = (uint8_t)m0;
+  }
+  if (too_large < nc) {
+    set_error("Too large stencil! maxStencilSize = %d (cell %d, limit %d)", too_large_size, too_large, MAXV);
+    afar_free_host_fields(h);
+    return AFAR_ERR_LIMIT;
   }
   h->cellFaces = xalloc<int>((size_t)maxM * nc);
   std::vector<int> gsten((size_t)maxS * nc, 0);
@@ -665,33 +682,70 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
   std::vector<int>().swap(sten);
 
   // ---- Gauss quadrature of cells and boundary faces (basicCUDAsolver.cpp:420-457)
+  // (point counts from the rule sizes, then every member filled independently)
   std::vector<int> gq_off(nc + nb + 1, 0);
   std::vector<Pt> gq_p;
   std::vector<double> gq_w;
   {
-    std::vector<Pt> tp;
-    std::vector<double> tw;
+    std::vector<Pt> rp;
+    std::vector<double> rw;
+    tri_rule(cfg->cOrder, rp, rw);
+    const int ntri = (int)rp.size();
+    rec_rule(cfg->cOrder, rp, rw);
+    const int nquad = (int)rp.size();
+    std::vector<double> bp;
+    bar_rule(cfg->fOrder, bp, rw);
+    const int nbar = (int)bp.size();
     for (int i = 0; i < nc + nb; ++i) {
-      if (i < nc)
-        cell_gauss(m, g, i, cfg->cOrder, tp, tw);
-      else
-        face_gauss(m, nf + (i - nc), cfg->fOrder, tp, tw);
-      gq_off[i] = (int)gq_p.size();
-      gq_p.insert(gq_p.end(), tp.begin(), tp.end());
-      gq_w.insert(gq_w.end(), tw.begin(), tw.end());
+      const int cnt = i < nc ? (m->cellPointsOffset[i + 1] - m->cellPointsOffset[i] == 3 ? ntri : nquad) : nbar;
+      gq_off[i + 1] = gq_off[i] + cnt;
     }
-    gq_off[nc + nb] = (int)gq_p.size();
+    gq_p.resize(gq_off[nc + nb]);
+    gq_w.resize(gq_off[nc + nb]);
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nthreads)
+#endif
+    {
+      std::vector<Pt> tp;
+      std::vector<double> tw;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 4096)
+#endif
+      for (int i = 0; i < nc + nb; ++i) {
+        if (i < nc)
+          cell_gauss(m, g, i, cfg->cOrder, tp, tw);
+        else
+          face_gauss(m, nf + (i - nc), cfg->fOrder, tp, tw);
+        for (size_t k = 0; k < tp.size() && gq_off[i] + (int)k < gq_off[i + 1]; ++k) {
+          gq_p[gq_off[i] + k] = tp[k];
+          gq_w[gq_off[i] + k] = tw[k];
+        }
+      }
+    }
   }
 
-  // ---- RBF P matrices, pseudo-inverses, trouble flags (basicCUDAsolver.cpp:461-533)
   const int nmax = maxS + 1;
+  const size_t rstride = 2 * (size_t)nmax;
+  h->RBFbasis = xalloc<float>(rstride * nf);
+  double* rbf64 = rbf64_out ? xalloc<double>(rstride * nf) : nullptr;
+  if (device >= 0) {  // the RBF stage on the GPU, bit-identical to the host stage below
+    const RbfInputs in{nc, nf, nb, maxS, h->stencilSize, gsten.data(), h->CELL, h->FACE, h->neighbour,
+                       gq_off.data(), reinterpret_cast<const double*>(gq_p.data()), gq_w.data(), px, py,
+                       cfg->shapeFactor};
+    const afar_status st = rbf_stage_device(device, in, h->RBFbasis, rbf64);
+    if (st != AFAR_OK) {
+      afar_free_host_fields(h);
+      std::free(rbf64);
+      return st;
+    }
+  } else {
+  // ---- RBF P matrices, pseudo-inverses, trouble flags (basicCUDAsolver.cpp:461-533)
   std::vector<double> refd(nc, 0.0);
   std::vector<double> Gall((size_t)nc * nmax * nmax, 0.0);
   std::vector<char> trouble(nc, 0);
   const double shape = cfg->shapeFactor;
   const afar_meshCellData* CELL = h->CELL;
 #ifdef _OPENMP
-  const int nthreads = cfg->nThreads > 0 ? cfg->nThreads : omp_get_max_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
 #endif
   for (int c = 0; c < nc; ++c) {
@@ -729,9 +783,6 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
   }
 
   // ---- O3 face weights (basicCUDAsolver.cpp:538-619), stored as float
-  const size_t rstride = 2 * (size_t)nmax;
-  h->RBFbasis = xalloc<float>(rstride * nf);
-  double* rbf64 = rbf64_out ? xalloc<double>(rstride * nf) : nullptr;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
 #endif
@@ -775,6 +826,7 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
     }
   }
   std::vector<double>().swap(Gall);
+  }
 
   // ---- 128-cell block halo remap (basicCUDAsolver.cpp:697-850)
   const int BD = AFAR_BLOCKDIM;
@@ -875,4 +927,20 @@ extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar
   sz->maxCompactLocalBlockStencilSize = maxCLB;
   if (rbf64_out) *rbf64_out = rbf64;
   return AFAR_OK;
+}
+
+extern "C" afar_status afar_precompute_fields(const afar_polyMesh* m, const afar_caseConfig* cfg, const double* Wc,
+                                              const double* Wb, afar_fieldPointer* h, afar_fieldSizes* sz,
+                                              double** rbf64_out) {
+  return precompute(m, cfg, Wc, Wb, -1, h, sz, rbf64_out);
+}
+
+extern "C" afar_status afar_precompute_fields_device(const afar_polyMesh* m, const afar_caseConfig* cfg,
+                                                     const double* Wc, const double* Wb, int device,
+                                                     afar_fieldPointer* h, afar_fieldSizes* sz, double** rbf64_out) {
+  if (device < 0) {
+    set_error("afar_precompute_fields_device: device %d", device);
+    return AFAR_ERR_ARGUMENT;
+  }
+  return precompute(m, cfg, Wc, Wb, device, h, sz, rbf64_out);
 }

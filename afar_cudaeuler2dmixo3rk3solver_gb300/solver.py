@@ -177,8 +177,12 @@ def _cache_key(mesh: FoamMesh, cfg: CaseConfig, Wc, Wb, want_rbf64) -> str:
     return h.hexdigest()[:32]
 
 
-def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_rbf64=False, cache_dir=None):
+def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_rbf64=False, cache_dir=None,
+               device=None):
     """Mesh + initial fields -> the reference's host field bundle (native precompute).
+
+    With ``device`` (a CUDA device index) the RBF stage -- P matrices, inverses, O3 weights -- runs on
+    that GPU (``afar_precompute_fields_device``); the bundle is bit-identical to the host's.
 
     With ``cache_dir`` the bundle is kept on disk under a hash of every input and read back on the
     next call with the same inputs, instead of recomputing the RBF pseudo-inverses and weights (the
@@ -188,7 +192,7 @@ def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_r
         path = os.path.join(cache_dir, f"afar_bundle_{_cache_key(mesh, cfg, W_cells, W_boundary, want_rbf64)}.npz")
         if os.path.exists(path):
             return HostFields.load(path)
-        hf = precompute(mesh, cfg, W_cells, W_boundary, want_rbf64)
+        hf = precompute(mesh, cfg, W_cells, W_boundary, want_rbf64, device=device)
         os.makedirs(cache_dir, exist_ok=True)
         tmp = path + f".{os.getpid()}.tmp.npz"
         hf.save(tmp)
@@ -204,8 +208,12 @@ def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_r
     sz = _ffi.FieldSizes()
     c = cfg.to_c()
     r64 = C.c_void_p()
-    st = lib().afar_precompute_fields(C.byref(m), C.byref(c), ptr(Wc), ptr(Wb), C.byref(fp), C.byref(sz),
-                                      C.byref(r64) if want_rbf64 else None)
+    if device is None:
+        st = lib().afar_precompute_fields(C.byref(m), C.byref(c), ptr(Wc), ptr(Wb), C.byref(fp), C.byref(sz),
+                                          C.byref(r64) if want_rbf64 else None)
+    else:
+        st = lib().afar_precompute_fields_device(C.byref(m), C.byref(c), ptr(Wc), ptr(Wb), int(device), C.byref(fp),
+                                                 C.byref(sz), C.byref(r64) if want_rbf64 else None)
     check(st)
     try:
         hf = HostFields.from_c(fp, sz)

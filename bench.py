@@ -66,6 +66,8 @@ def parse():
                     help="the batched workload instead: many independent solves stepped by one graph")
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--setup", action="store_true",
+                    help="time the precompute of the workload's mesh on the host and with its RBF stage on the GPU")
     ap.add_argument("--serve-requests", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="arrivals per second")
     return ap.parse_args()
@@ -534,6 +536,43 @@ def run_serve(args, dist: Dist):
     }), flush=True)
 
 
+def run_setup(args, dist: Dist):
+    """Set-up time of the workload's mesh: the native precompute with every stage on the host (all
+    host threads) against the same with its RBF stage (P matrices, inverses, O3 weights) on the GPU;
+    the two bundles are compared bit for bit."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+
+    b.build_all()
+    t0 = time.perf_counter()
+    if args.mesh == "riemann_mixed":
+        m = mesh.riemann_mixed(args.mixed_n, seed=args.seed)
+        W, Wb = mesh.riemann_fields(m)
+    else:
+        m = mesh.forward_step_triangles(args.points, seed=args.seed)
+        W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
+    t_mesh = time.perf_counter() - t0
+    cfg = CaseConfig(stencilType="edgeNeighbour", CFL=args.cfl)
+    precompute(mesh.quad_grid(8, 8), cfg, *mesh.uniform_fields(mesh.quad_grid(8, 8), 1.0, 0.0, 0.0, 1.0),
+               device=dist.local)  # context creation outside the timing
+    times = {}
+    out = {}
+    for where, dev in (("host", None), ("device", dist.local)):
+        t = time.perf_counter()
+        out[where] = precompute(m, cfg, W, Wb, want_rbf64=True, device=dev)
+        times[where] = time.perf_counter() - t
+    same = all(np.array_equal(out["host"].a[k].view(np.uint8), out["device"].a[k].view(np.uint8))
+               for k in out["host"].a)
+    if dist.rank != 0:
+        return
+    print(json.dumps({
+        "metric": "precompute seconds", "workload": args.mesh, "cells": m.n_cells,
+        "internal_faces": m.n_internal_faces, "mesh_generation_s": round(t_mesh, 3),
+        "host_s": round(times["host"], 3), "rbf_stage_on_gpu_s": round(times["device"], 3),
+        "host_threads": os.cpu_count(), "bit_identical": bool(same),
+    }), flush=True)
+
+
 def run_batch(args, dist: Dist):
     """Batched workload (the shape of the batched config): --batch-solves independent supersonic
     compression ramps, cells log-uniform in [5k, 200k] (quads, 2:1 channel), inflow Mach U[1.5, 4]
@@ -602,7 +641,9 @@ def main():
     args = parse()
     dist = Dist()
     try:
-        if args.serve:
+        if args.setup:
+            run_setup(args, dist)
+        elif args.serve:
             run_serve(args, dist)
         elif args.batch:
             run_batch(args, dist)

@@ -187,6 +187,16 @@ afar_status afar_precompute_fields(const afar_polyMesh* mesh, const afar_caseCon
                                    double** RBFbasis64);
 void afar_free_host_fields(afar_fieldPointer* host);
 
+/* afar_precompute_fields with its heaviest stage -- the RBF P matrices, their inverses and the O3
+ * face weights (basicCUDAsolver.cpp:461-619) -- on CUDA device `device` (one warp per cell); every
+ * other stage stays on the host.  The arrays are bit-identical to afar_precompute_fields'.  Device
+ * memory used and released within the call: about (maxStencilSize+1)^2 * 8 bytes per cell plus the
+ * Gauss points and the weights.  AFAR_ERR_CUDA when the device is unusable. */
+afar_status afar_precompute_fields_device(const afar_polyMesh* mesh, const afar_caseConfig* cfg,
+                                          const double* W_cells, const double* W_boundary, int device,
+                                          afar_fieldPointer* host, afar_fieldSizes* sizes,
+                                          double** RBFbasis64);
+
 /* Cell and boundary-face Gauss points/weights (d2GaussQuadrature layout) as CSR lists over
  * nCells + nBoundaryFaces members; boundary-face weights are divided by |Sf| like
  * basicCUDAsolver.cpp:444-457.  offsets: [nCells+nBoundaryFaces+1]; pts: [2*total]; w: [total].
