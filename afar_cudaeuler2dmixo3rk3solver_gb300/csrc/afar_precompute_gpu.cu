@@ -227,6 +227,7 @@ afar_status rbf_stage_device(int device, const RbfInputs& in, float* RBFbasis, d
   cudaError_t err = cudaSetDevice(device);
   if (err != cudaSuccess) {
     set_error("precompute on device %d: %s", device, cudaGetErrorString(err));
+    cudaGetLastError();  // a bad ordinal is not sticky: leave no error for the caller's next check
     return AFAR_ERR_CUDA;
   }
   afar_status st = AFAR_OK;
@@ -313,6 +314,7 @@ afar_status rbf_stage_device(int device, const RbfInputs& in, float* RBFbasis, d
     if (s) cudaStreamDestroy(s);
     if (err != cudaSuccess) {
       set_error("precompute on device %d: %s", device, cudaGetErrorString(err));
+      cudaGetLastError();
       st = AFAR_ERR_CUDA;
     }
   }
