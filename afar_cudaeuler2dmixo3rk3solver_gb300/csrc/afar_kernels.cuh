@@ -350,11 +350,9 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
   return L;
 }
 
-// Issues the bulk copies of tile `blk`'s operator rows (called by warp 0), and arms the barrier for
-// them and for the state slice that recon_tile_fetch_state adds.  Rows of the slot-major arrays
-// hold ldc elements (a multiple of 32), so every slice is a multiple of 128 bytes and 16-byte
-// aligned; the own-state slice holds the tile's cells (16 bytes each).  The operator rows are set
-// up once per solve, so they may be fetched before the previous kernel of the step has finished.
+// Issues the bulk copies of tile `blk` (called by warp 0).  Rows of the slot-major arrays hold
+// ldc elements (a multiple of 32), so every slice is a multiple of 128 bytes and 16-byte aligned;
+// the own-state slice holds the tile's cells (16 bytes each).
 template <class P>
 __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const int blk, const ReconTile& L,
                                                  unsigned char* sm, unsigned long long* bar) {
@@ -363,7 +361,7 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
   const unsigned ne = (unsigned)min(kTile, a.ldc - c0);  // elements of a row slice
   const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
   const int M = a.maxM, S = a.maxS;
-  const int rows = 4 * M + S + M * (S + 1);
+  const int rows = 4 * M + S + M * (S + 1) + 1;
   const unsigned total = ne * (M * (4 + 8 + 8 + 8) + S * 4 + M * (S + 1) * 4) + nw * 16;
   if (lane == 0) mbar_arrive_expect_tx(bar, total);
   __syncwarp();
@@ -395,22 +393,18 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
       dst = sm + L.off_sten + k * kTile * 4;
       src = a.sten + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
-    } else {
+    } else if (r < rows - 1) {
       const int k = r - 4 * M - S;
       dst = sm + L.off_wts + k * kTile * 4;
       src = a.wts + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
+    } else {
+      dst = sm + L.off_w;
+      src = a.W + c0;
+      bytes = nw * 16;
     }
     bulk_to_smem(dst, src, bytes, bar);
   }
-}
-// The tile's own states (lane 0 of warp 0), written by the previous stage's update.
-template <class P>
-__device__ __forceinline__ void recon_tile_fetch_state(const StageArgs<P>& a, const int blk, const ReconTile& L,
-                                                       unsigned char* sm, unsigned long long* bar) {
-  const int c0 = blk * kTile;
-  const unsigned nw = (unsigned)min(kTile, a.Nc - c0);
-  if (threadIdx.x == 0) bulk_to_smem(sm + L.off_w, a.W + c0, nw * 16, bar);
 }
 
 // reconstruct (reference cudaLimiter.h:53-316) for the mixed policy from the staged tile: LS
@@ -430,9 +424,6 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   if (t == 0) mbar_init(bar, 1);
   __syncthreads();
   if (t < 32) recon_tile_fetch(a, blk, L, sm, bar);
-  pdl_wait();
-  pdl_trigger();
-  if (t < 32) recon_tile_fetch_state(a, blk, L, sm, bar);
   const int c = blk * kTile + t;
   const int nS = c < a.Nc ? a.nS[c] : 0, nM = c < a.Nc ? a.nM[c] : 0;
   if (!mbar_wait_bounded(bar, 0)) {  // the copies did not land: flag it, give them a last chance, leave
@@ -1510,8 +1501,6 @@ __device__ __forceinline__ void update_body(const StageArgs<P>& a, const int blk
 // One solve per launch, arguments by value (read from the parameter bank).
 template <class P>
 __global__ void __launch_bounds__(128, 5) k_reconstruct_reg(StageArgs<P> a) {
-  pdl_wait();
-  pdl_trigger();
   recon_reg_body<P>(a, blockIdx.x);
 }
 template <class P, int NF>
@@ -1521,26 +1510,18 @@ __global__ void __launch_bounds__(kTile, 4) k_reconstruct_tile(StageArgs<P> a) {
 }
 template <class P>
 __global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
-  pdl_wait();
-  pdl_trigger();
   recon_staged_body<P>(a, blockIdx.x);
 }
 template <class P>
 __global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
-  pdl_wait();
-  pdl_trigger();
   bvd_body<P>(a, blockIdx.x);
 }
 template <class P, bool DT>
 __global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
-  pdl_wait();
-  pdl_trigger();
   flux_body<P, DT>(a, blockIdx.x);
 }
 template <class P>
 __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const StageCoef k) {
-  pdl_wait();
-  pdl_trigger();
   update_body<P>(a, blockIdx.x, k);
 }
 
@@ -1601,7 +1582,6 @@ __global__ void kb_finish_step(const StageArgs<P>* __restrict__ tab, const int n
 }
 
 __global__ void k_finish_step(StepCtl* ctl) {
-  pdl_wait();
   if (threadIdx.x == 0 && blockIdx.x == 0) finish_one(ctl);
 }
 

@@ -120,15 +120,6 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
   return true;
 }
 
-// Programmatic dependent launch.  A kernel launched with programmatic stream serialization may
-// start while the kernel before it in the stream is still running; pdl_wait() blocks until that
-// kernel has completed and its writes are visible (a no-op for a kernel launched without the
-// attribute), so every read of another kernel's output and every global write comes after it.
-// pdl_trigger() lets the next kernel's blocks be scheduled once every block of this one has
-// issued it; it does not release any data.
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
-
 // cond ? a : b.  The reference writes these selections as arithmetic blends
 // (c1*a + c2*b with c1, c2 in {0,1}); the ref policy keeps the blend so that signed zeros and
 // non-finite operands propagate the same way.

@@ -7,7 +7,6 @@
 // policy-typed intermediates; see afar_kernels.cuh) and owns all device memory.
 #include <cuda_runtime.h>
 
-#include <cstdlib>
 #include <cstring>
 #include <algorithm>
 #include <map>
@@ -189,7 +188,6 @@ struct afar_solver {
   double px = 0.0, py = 0.0;  // periods of a periodic mesh (afar_set_periodic)
   int recon_variant = 0;      // mixed reconstruct: 0 tile-staged, 1 register pass (autotuned)
   int recon_request = -1;     // afar_set_tuning: -1 autotune, else the variant to use
-  bool pdl = true;            // chain the stage kernels by programmatic dependent launch (AFAR_PDL=0: off)
   float tune_ms[2] = {0.f, 0.f};  // the autotuner's measured launch times (0: decision from the cache)
   void* xfer = nullptr;    // mixed: staging for double <-> device-format copies, 32 B x (Nc + Nb)
   int2* on = nullptr;
@@ -319,51 +317,26 @@ size_t recon_smem(const afar_solver* s) {
   return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
 }
 
-// Launches `kernel`; with `pdl` it may begin while the previous kernel in the stream is still
-// running (programmatic stream serialization): its blocks are scheduled once every block of that
-// kernel has passed pdl_trigger(), and they read nothing the previous kernels wrote, and write
-// nothing, before pdl_wait().
-template <typename... KArgs, typename... Args>
-void launch(bool pdl, void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t stream,
-            Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = pdl ? 1 : 0;
-  cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-
 // One solve's stage launches, arguments by value.  The ref policy reconstructs in the staged
-// kernel and runs the reference-layout flux; fp64 reconstructs staged, mixed in registers.  Within
-// a step the fp64 and mixed kernels follow one another by programmatic dependent launch, except
-// the first of the step (its predecessor is the previous step's bookkeeping).
+// kernel and runs the reference-layout flux; fp64 reconstructs staged, mixed in registers.
 template <class P>
 struct Stage {
   afar_solver* s;
   StageArgs<P> a;
-  bool allow_pdl = true;  // false where events between the kernels time them one by one
   int gc() const { return grid_for(s->Nc, kCellBlock); }
-  bool chained() const { return P::id != PolicyRef::id && s->pdl && allow_pdl; }
 
-  void reconstruct(bool first = false) const {
-    const bool pdl = chained() && !first;
+  void reconstruct() const {
     if constexpr (P::id == PolicyMixed::id) {
       if (s->recon_variant == 1)
-        launch(pdl, k_reconstruct_reg<P>, gc(), kCellBlock, 0, s->stream, a);
+        k_reconstruct_reg<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
       else if (s->maxM <= 3)
-        launch(pdl, k_reconstruct_tile<P, 3>, gc(), kTile, recon_smem<P>(s), s->stream, a);
+        k_reconstruct_tile<P, 3><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
       else
-        launch(pdl, k_reconstruct_tile<P, 4>, gc(), kTile, recon_smem<P>(s), s->stream, a);
+        k_reconstruct_tile<P, 4><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
     } else
-      launch(pdl, k_reconstruct_staged<P>, gc(), kCellBlock, recon_smem<P>(s), s->stream, a);
+      k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
   }
-  void bvd() const { launch(chained(), k_bvd<P>, gc(), kCellBlock, 0, s->stream, a); }
+  void bvd() const { k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a); }
   // The face flux.  The ref policy runs the reference-layout kernel (its fused multiply-adds then
   // fall where the reference's do) and, on the first stage, the CFL step as a kernel of its own
   // like the reference's setDeltaT; the other policies fuse the CFL reduction into the flux.
@@ -381,13 +354,13 @@ struct Stage {
     } else {
       const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
       if (dt_stage)
-        launch(chained(), k_flux<P, true>, gf, kFaceBlock, 0, s->stream, a);
+        k_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(a);
       else
-        launch(chained(), k_flux<P, false>, gf, kFaceBlock, 0, s->stream, a);
+        k_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(a);
     }
   }
   void update(int k) const {
-    launch(chained(), k_update<P>, gc(), kCellBlock, 0, s->stream, a, stage_coef(k));
+    k_update<P><<<gc(), kCellBlock, 0, s->stream>>>(a, stage_coef(k));
   }
 };
 
@@ -396,7 +369,6 @@ template <class P>
 afar_status make_stage(afar_solver* s, bool debug, Stage<P>* out) {
   out->s = s;
   out->a = make_args<P>(s);
-  out->allow_pdl = !debug;
   if (debug) out->a.res_dbg = s->res_dbg;
   return AFAR_OK;
 }
@@ -404,7 +376,7 @@ afar_status make_stage(afar_solver* s, bool debug, Stage<P>* out) {
 template <class P>
 void enqueue_step(const Stage<P>& st) {
   for (int k = 0; k < 3; ++k) {
-    st.reconstruct(k == 0);
+    st.reconstruct();
     st.bvd();
     st.flux(k == 0);
     st.update(k);
@@ -571,7 +543,6 @@ extern "C" afar_status afar_solver_create(afar_solver** out, int policy, int dev
   afar_solver* s = new afar_solver();
   s->policy = policy;
   s->device = device;
-  if (const char* e = std::getenv("AFAR_PDL")) s->pdl = std::strcmp(e, "0") != 0;
   if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
     set_error("cudaStreamCreate failed");
     delete s;
@@ -666,7 +637,6 @@ static afar_status tune_reconstruct(afar_solver* s) {
   Stage<PolicyMixed> sg;
   afar_status st = make_stage<PolicyMixed>(s, false, &sg);
   if (st) return st;
-  sg.allow_pdl = false;
   cudaEvent_t e0, e1;
   AFAR_CUDA(cudaEventCreate(&e0));
   AFAR_CUDA(cudaEventCreate(&e1));
@@ -1073,7 +1043,6 @@ extern "C" afar_status afar_profile_step(afar_solver* s, double dt, double CFL, 
     Stage<P> sg;
     afar_status r = make_stage<P>(s, false, &sg);
     if (r) return r;
-    sg.allow_pdl = false;
     mark(-1);
     for (int k = 0; k < 3; ++k) {
       sg.reconstruct();
