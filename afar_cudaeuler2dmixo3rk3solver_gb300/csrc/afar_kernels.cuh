@@ -78,6 +78,7 @@ struct StageArgs {
   const float* vinvf;         // Nc 1/V as float (mixed)
   const uint8_t* nS;          // Nc stencil size
   const uint8_t* nM;          // Nc faces per cell (compact stencil size)
+  const uint8_t* tileS;       // ceil(Nc/128): the largest stencil size of each 128-cell tile
   const int* sten;            // [maxS][ldc]
   const int* cf;              // [maxM][ldc]
   const V2<S>* lsm;           // [maxM][ldc]
@@ -352,7 +353,9 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
 
 // Issues the bulk copies of tile `blk` (called by warp 0).  Rows of the slot-major arrays hold
 // ldc elements (a multiple of 32), so every slice is a multiple of 128 bytes and 16-byte aligned;
-// the own-state slice holds the tile's cells (16 bytes each).
+// the own-state slice holds the tile's cells (16 bytes each).  Only the stencil and weight rows up
+// to the tile's own largest stencil are fetched: the rows past it hold zeros for every cell of the
+// tile and are never read.
 template <class P>
 __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const int blk, const ReconTile& L,
                                                  unsigned char* sm, unsigned long long* bar) {
@@ -360,7 +363,7 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
   const int c0 = blk * kTile;
   const unsigned ne = (unsigned)min(kTile, a.ldc - c0);  // elements of a row slice
   const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
-  const int M = a.maxM, S = a.maxS;
+  const int M = a.maxM, S = a.tileS[blk];
   const int rows = 4 * M + S + M * (S + 1) + 1;
   const unsigned total = ne * (M * (4 + 8 + 8 + 8) + S * 4 + M * (S + 1) * 4) + nw * 16;
   if (lane == 0) mbar_arrive_expect_tx(bar, total);
@@ -394,7 +397,8 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
       src = a.sten + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
     } else if (r < rows - 1) {
-      const int k = r - 4 * M - S;
+      const int q = r - 4 * M - S, fi = q / (S + 1);
+      const int k = fi * (a.maxS + 1) + (q - fi * (S + 1));  // row j = q - fi (S + 1) of face slot fi
       dst = sm + L.off_wts + k * kTile * 4;
       src = a.wts + (size_t)k * a.ldc + c0;
       bytes = ne * 4;

@@ -195,6 +195,7 @@ struct afar_solver {
   uint8_t* btype = nullptr;
   uint8_t* nS = nullptr;
   uint8_t* nM = nullptr;
+  uint8_t* tileS = nullptr;  // per 128-cell tile: its largest stencil size
   int* sten = nullptr;
   int* cf = nullptr;
   V4<double>* U = nullptr;
@@ -260,6 +261,7 @@ StageArgs<P> make_args(afar_solver* s) {
   a.btype = s->btype;
   a.vol = s->vol;
   a.nS = s->nS;
+  a.tileS = s->tileS;
   a.nM = s->nM;
   a.sten = s->sten;
   a.cf = s->cf;
@@ -859,6 +861,13 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
     AFAR_CUDA(cudaMemcpyAsync(s->btype, h->boundaryFacesType, Nb, cudaMemcpyHostToDevice, s->stream));
   }
   AFAR_CUDA(cudaMemcpyAsync(s->nS, h->stencilSize, Nc, cudaMemcpyHostToDevice, s->stream));
+  {
+    const int ntile = (Nc + kTile - 1) / kTile;
+    std::vector<uint8_t> ts(ntile, 0);
+    for (int c = 0; c < Nc; ++c) ts[c / kTile] = std::max(ts[c / kTile], h->stencilSize[c]);
+    if ((st = dalloc_t(s, &s->tileS, (size_t)ntile))) return st;
+    AFAR_CUDA(cudaMemcpy(s->tileS, ts.data(), ntile, cudaMemcpyHostToDevice));
+  }
   AFAR_CUDA(cudaMemcpyAsync(s->nM, h->compactStencilSize, Nc, cudaMemcpyHostToDevice, s->stream));
   {
     uint16_t* dls = nullptr;
