@@ -346,7 +346,7 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
   o += maxM * (maxS + 1) * kTile * 4;
   L.off_w = o;
   o += kTile * 16;
-  L.off_bar = o;
+  L.off_bar = o;  // two mbarriers: the gather inputs, then the rest
   L.bytes = o + 16;
   return L;
 }
@@ -355,7 +355,9 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
 // ldc elements (a multiple of 32), so every slice is a multiple of 128 bytes and 16-byte aligned;
 // the own-state slice holds the tile's cells (16 bytes each).  Only the stencil and weight rows up
 // to the tile's own largest stencil are fetched: the rows past it hold zeros for every cell of the
-// tile and are never read.
+// tile and are never read.  Two barriers: bar[0] covers what the stencil gathers need (face ids,
+// stencil ids, own states, 12 of the ~47 KB), bar[1] the LS rows, face geometry and O3 weights, so
+// the first gathers are in flight while the weights still stream in.
 template <class P>
 __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const int blk, const ReconTile& L,
                                                  unsigned char* sm, unsigned long long* bar) {
@@ -365,17 +367,21 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
   const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
   const int M = a.maxM, S = a.tileS[blk];
   const int rows = 4 * M + S + M * (S + 1) + 1;
-  const unsigned total = ne * (M * (4 + 8 + 8 + 8) + S * 4 + M * (S + 1) * 4) + nw * 16;
-  if (lane == 0) mbar_arrive_expect_tx(bar, total);
+  if (lane == 0) {
+    mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16);
+    mbar_arrive_expect_tx(bar + 1, ne * (M * (8 + 8 + 8) + M * (S + 1) * 4));
+  }
   __syncwarp();
   for (int r = lane; r < rows; r += 32) {
     void* dst;
     const void* src;
     unsigned bytes;
+    unsigned long long* b = bar + 1;
     if (r < M) {
       dst = sm + L.off_cf + r * kTile * 4;
       src = a.cf + (size_t)r * a.ldc + c0;
       bytes = ne * 4;
+      b = bar;
     } else if (r < 2 * M) {
       const int k = r - M;
       dst = sm + L.off_lsm + k * kTile * 8;
@@ -396,6 +402,7 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
       dst = sm + L.off_sten + k * kTile * 4;
       src = a.sten + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
+      b = bar;
     } else if (r < rows - 1) {
       const int q = r - 4 * M - S, fi = q / (S + 1);
       const int k = fi * (a.maxS + 1) + (q - fi * (S + 1));  // row j = q - fi (S + 1) of face slot fi
@@ -406,8 +413,9 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
       dst = sm + L.off_w;
       src = a.W + c0;
       bytes = nw * 16;
+      b = bar;
     }
-    bulk_to_smem(dst, src, bytes, bar);
+    bulk_to_smem(dst, src, bytes, b);
   }
 }
 
@@ -425,17 +433,25 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   const ReconTile L = recon_tile_layout(a.maxM, a.maxS);
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + L.off_bar);
   const int t = threadIdx.x;
-  if (t == 0) mbar_init(bar, 1);
+  if (t == 0) {
+    mbar_init(bar, 1);
+    mbar_init(bar + 1, 1);
+  }
   __syncthreads();
   if (t < 32) recon_tile_fetch(a, blk, L, sm, bar);
   const int c = blk * kTile + t;
   const int nS = c < a.Nc ? a.nS[c] : 0, nM = c < a.Nc ? a.nM[c] : 0;
-  if (!mbar_wait_bounded(bar, 0)) {  // the copies did not land: flag it, give them a last chance, leave
+  // leaving: every copy into this block's shared memory must have landed first
+  auto give_up = [&]() {
     if (t == 0) atomicOr(&a.ctl->err, 1u);
     mbar_wait_bounded(bar, 0);
+    mbar_wait_bounded(bar + 1, 0);
+  };
+  if (!mbar_wait_bounded(bar, 0)) return give_up();
+  if (c >= a.Nc) {
+    if (!mbar_wait_bounded(bar + 1, 0)) give_up();
     return;
   }
-  if (c >= a.Nc) return;
   const int* s_cf = reinterpret_cast<const int*>(sm + L.off_cf);
   const V2<S>* s_lsm = reinterpret_cast<const V2<S>*>(sm + L.off_lsm);
   const V2<G>* s_sg = reinterpret_cast<const V2<G>*>(sm + L.off_sg);
@@ -454,6 +470,12 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   }
   const V4<WT> wc = s_w[t];
   const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  constexpr int U = 8;
+  V4<WT> wj[U];  // the first batch of stencil states, gathered before the weights have landed
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (u < nS) wj[u] = a.W[s_sten[u * kTile + t]];
+  if (!mbar_wait_bounded(bar + 1, 0)) return give_up();
   // O3 weights of boundary-face and missing slots are zero in the operator rows (setup), so only
   // slots past this mesh's largest cell (a batch may stage fewer rows than NF) are skipped
   const int nfm = a.maxM;
@@ -471,12 +493,12 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   S pn[NF];  // pressure of the cell across each face
 #pragma unroll
   for (int fi = 0; fi < NF; ++fi) pn[fi] = S(0);
-  constexpr int U = 8;
   for (int ci0 = 0; ci0 < nS; ci0 += U) {
-    V4<WT> wj[U];
+    if (ci0 > 0) {
 #pragma unroll
-    for (int u = 0; u < U; ++u)
-      if (ci0 + u < nS) wj[u] = a.W[s_sten[(ci0 + u) * kTile + t]];
+      for (int u = 0; u < U; ++u)
+        if (ci0 + u < nS) wj[u] = a.W[s_sten[(ci0 + u) * kTile + t]];
+    }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int ci = ci0 + u;
