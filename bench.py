@@ -38,9 +38,9 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 PROFILE_STEPS = 10
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one mixed-policy reconstruct launch
-# per cell, from an ncu capture of the 500,094-cell version of this workload (traffic grows with
-# the cells of the tile stream); None when no capture matches the current kernels.
-RECON_TRAFFIC_BYTES_PER_CELL = 430.0
+# (tile-staged) per cell, from an ncu capture of the 500,094-cell version of this workload (traffic
+# grows with the cells of the tile stream); None when no capture matches the current kernels.
+RECON_TRAFFIC_BYTES_PER_CELL = 411.9
 
 
 def parse():
@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--mesh", default="step", choices=["step", "riemann_mixed"],
                     help="step: the metric's workload; riemann_mixed: the 4M-cell mixed quad/triangle case")
     ap.add_argument("--mixed-n", type=int, default=1766)
+    ap.add_argument("--recon", default="auto", choices=["auto", "tile", "register"],
+                    help="mixed reconstruct variant: autotuned (default) or forced")
     ap.add_argument("--serve", action="store_true",
                     help="the serving workload instead: Poisson arrivals of solves through afar_server_*")
     ap.add_argument("--batch", action="store_true",
@@ -332,6 +334,8 @@ def run_ours(args, dist: Dist):
     chunks = [min(args.chunk, K - i) for i in range(0, K, args.chunk)]
     for pol in policies:
         s = CudaSolver(hf, cfg, policy=pol, device=device)
+        if pol == "mixed" and args.recon != "auto":
+            s.set_tuning(0 if args.recon == "tile" else 1)
         s.run(Wm)  # warm-up steps (graph capture, first touch)
         s.save()   # every timed chunk restarts here, so every timed step is a physical one
         solvers[pol] = s
@@ -362,6 +366,8 @@ def run_ours(args, dist: Dist):
                 acc[k] = acc.get(k, 0.0) + v / PROFILE_STEPS
         results[pol]["kernels_ms"] = acc
         results[pol]["device_bytes"] = s.device_bytes()
+        if pol == "mixed":
+            results[pol]["tuning"] = s.tuning()
 
     # e2e through the reference-shaped C ABI with host buffers (mixed policy)
     pol0 = policies[0]
@@ -425,8 +431,12 @@ def run_ours(args, dist: Dist):
     b_launch = reconstruct_bytes_per_launch(hf, pol0)
     t_launch = prof["reconstruct"] / 3.0
     achieved = b_launch / (t_launch * 1e-3) / 1e9
+    tuning = head.get("tuning")
+    tile = tuning is not None and tuning["recon_variant"] == 0
     traffic = (RECON_TRAFFIC_BYTES_PER_CELL * hf.nc
-               if RECON_TRAFFIC_BYTES_PER_CELL is not None and pol0 == "mixed" else None)
+               if RECON_TRAFFIC_BYTES_PER_CELL is not None and pol0 == "mixed" and tile else None)
+    recon_kind = ("reconstruct (mixed, tile-staged)" if tile else "reconstruct (mixed, register pass)"
+                  if pol0 == "mixed" else f"reconstruct ({pol0}, staged)")
     by_policy = {}
     for pol in policies:
         r = results[pol]
@@ -449,7 +459,7 @@ def run_ours(args, dist: Dist):
                    "timed_chunks": chunks, "chunk_start": f"state after {Wm} warm-up steps (device snapshot)",
                    "setup_s": round(setup_s, 1)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "peak_kind": peak_kind, "kernel": "reconstruct (mixed, tile-staged)",
+                     "traffic": traffic, "peak_kind": peak_kind, "kernel": recon_kind, "autotune": tuning,
                      "algorithmic_bytes_per_launch": b_launch, "launch_ms": t_launch,
                      "dominant_kernel": dom, "dominant_share": prof[dom] / tot if tot else None,
                      "step": {"algorithmic_bytes": bstep, "achieved_GBps": step_gbps, "frac": step_gbps / hbm}},
