@@ -188,6 +188,12 @@ struct afar_solver {
   double px = 0.0, py = 0.0;  // periods of a periodic mesh (afar_set_periodic)
   int recon_variant = 0;      // mixed reconstruct: 0 tile-staged, 1 register pass (autotuned)
   int recon_request = -1;     // afar_set_tuning: -1 autotune, else the variant to use
+  // The step split for the reference-shaped loop: afar_adjustTimeStep runs the head (stage 1 up to
+  // its flux, whose fused reduction is the Courant step) instead of a separate Courant pass, and the
+  // afar_GPUevolve that follows runs the tail (the rest of the step) with the caller's step size.
+  // head_pending: the head ran on the current state and nothing has touched the solver since.
+  cudaGraphExec_t graph_head = nullptr, graph_tail = nullptr;
+  bool head_pending = false;
   float tune_ms[2] = {0.f, 0.f};  // the autotuner's measured launch times (0: decision from the cache)
   void* xfer = nullptr;    // mixed: staging for double <-> device-format copies, 32 B x (Nc + Nb)
   int2* on = nullptr;
@@ -375,15 +381,28 @@ afar_status make_stage(afar_solver* s, bool debug, Stage<P>* out) {
   return AFAR_OK;
 }
 
+// A step is its head (stage 1 up to the flux, which also reduces the Courant step) and its tail.
 template <class P>
-void enqueue_step(const Stage<P>& st) {
-  for (int k = 0; k < 3; ++k) {
+void enqueue_head(const Stage<P>& st) {
+  st.reconstruct();
+  st.bvd();
+  st.flux(true);
+}
+template <class P>
+void enqueue_tail(const Stage<P>& st) {
+  st.update(0);
+  for (int k = 1; k < 3; ++k) {
     st.reconstruct();
     st.bvd();
-    st.flux(k == 0);
+    st.flux(false);
     st.update(k);
   }
   k_finish_step<<<1, 32, 0, st.s->stream>>>(st.s->ctl);
+}
+template <class P>
+void enqueue_step(const Stage<P>& st) {
+  enqueue_head(st);
+  enqueue_tail(st);
 }
 
 template <class P>
@@ -454,20 +473,31 @@ afar_status setup_operators(afar_solver* s, const afar_fieldPointer* h) {
   }
 }
 
+void destroy_graphs(afar_solver* s) {
+  for (cudaGraphExec_t* g : {&s->graph, &s->graph_head, &s->graph_tail})
+    if (*g) {
+      cudaGraphExecDestroy(*g);
+      *g = nullptr;
+    }
+  s->head_pending = false;
+}
+
+// The step graph, and its head and tail as graphs of their own (the same launches split in two).
 afar_status capture_graph(afar_solver* s) {
-  if (s->graph) {
-    AFAR_CUDA(cudaGraphExecDestroy(s->graph));
-    s->graph = nullptr;
-  }
-  cudaGraph_t g = nullptr;
+  destroy_graphs(s);
+  cudaGraph_t g[3] = {nullptr, nullptr, nullptr};
   auto capture = [&](auto tag) -> afar_status {
     using P = decltype(tag);
     Stage<P> st;
     afar_status r = make_stage<P>(s, false, &st);  // uploads the argument table before the capture
     if (r) return r;
-    AFAR_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step<P>(st);
-    AFAR_CUDA(cudaStreamEndCapture(s->stream, &g));
+    for (int i = 0; i < 3; ++i) {
+      AFAR_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      if (i == 0) enqueue_step<P>(st);
+      if (i == 1) enqueue_head<P>(st);
+      if (i == 2) enqueue_tail<P>(st);
+      AFAR_CUDA(cudaStreamEndCapture(s->stream, &g[i]));
+    }
     return AFAR_OK;
   };
   afar_status r;
@@ -476,12 +506,16 @@ afar_status capture_graph(afar_solver* s) {
     case AFAR_POLICY_FP64: r = capture(PolicyFP64{}); break;
     default: r = capture(PolicyMixed{}); break;
   }
+  cudaGraphExec_t* out[3] = {&s->graph, &s->graph_head, &s->graph_tail};
+  cudaError_t e = cudaSuccess;
+  for (int i = 0; i < 3; ++i) {
+    if (!r && g[i] && e == cudaSuccess) e = cudaGraphInstantiate(out[i], g[i], 0);
+    if (g[i]) cudaGraphDestroy(g[i]);
+  }
   if (r) return r;
-  const cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
-  cudaGraphDestroy(g);
   if (e != cudaSuccess) {
     set_error("cudaGraphInstantiate failed: %s", cudaGetErrorString(e));
-    s->graph = nullptr;
+    destroy_graphs(s);
     return AFAR_ERR_CUDA;
   }
   return AFAR_OK;
@@ -492,6 +526,7 @@ afar_status check_ready(afar_solver* s) {
     set_error("null solver");
     return AFAR_ERR_ARGUMENT;
   }
+  s->head_pending = false;  // every call that goes through here may change what the head computed
   if (!s->have_fields || !s->have_stencil) {
     set_error("call afar_setDeviceFieldData and afar_setDeviceFieldDataStencil first");
     return AFAR_ERR_STATE;
@@ -750,6 +785,7 @@ extern "C" afar_status afar_set_rbf_basis64(afar_solver* s, const double* rbf, s
     set_error("afar_set_rbf_basis64: null argument");
     return AFAR_ERR_ARGUMENT;
   }
+  s->head_pending = false;
   s->rbf64.assign(rbf, rbf + count);
   return AFAR_OK;
 }
@@ -924,6 +960,31 @@ extern "C" afar_status afar_adjustTimeStep(afar_solver* s, int facesNum, double 
     return AFAR_ERR_ARGUMENT;
   }
   const unsigned long long init = 0x40F86A0000000000ull;  // bits of 1e5
+  // Outside a batch the Courant step comes from the head of the coming step -- stage 1 up to its
+  // flux, whose fused reduction is the same Courant minimum over the internal faces (the ref
+  // policy's head runs the reference-shaped Courant kernel itself) -- so no separate pass runs and
+  // the afar_GPUevolve that follows runs only the tail of the step.
+  if (!s->batch && s->Nf > 0) {
+    if ((st = ensure_graph(s, R, Cv))) return st;
+    if (s->graph_head) {
+      k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, 0.0, CFL, 0.0);
+      AFAR_CUDA(cudaMemcpyAsync(&s->ctl->dt_bits, &init, sizeof(init), cudaMemcpyHostToDevice, s->stream));
+      AFAR_CUDA(cudaGraphLaunch(s->graph_head, s->stream));
+      StepCtl c;
+      AFAR_CUDA(cudaMemcpyAsync(&c, s->ctl, sizeof(c), cudaMemcpyDeviceToHost, s->stream));
+      AFAR_CUDA(cudaStreamSynchronize(s->stream));
+      AFAR_CUDA(cudaGetLastError());
+      if (c.err) {  // a bounded device wait gave up, in this head or in the step before it
+        AFAR_CUDA(cudaMemsetAsync(&s->ctl->err, 0, sizeof(c.err), s->stream));
+        AFAR_CUDA(cudaStreamSynchronize(s->stream));
+        set_error("a device-side wait for a bulk copy timed out (error word %u); the state is not valid", c.err);
+        return AFAR_ERR_CUDA;
+      }
+      std::memcpy(dt, &c.dt_bits, sizeof(double));
+      s->head_pending = true;
+      return AFAR_OK;
+    }
+  }
   AFAR_CUDA(cudaMemcpyAsync(s->dt_bits, &init, sizeof(init), cudaMemcpyHostToDevice, s->stream));
   const int gf = grid_for(s->Nf, kFaceBlock);
   if (s->Nf > 0) {
@@ -979,6 +1040,7 @@ static afar_status run_impl(afar_solver* s, int nSteps, double dt, double CFL, d
 extern "C" afar_status afar_GPUevolve(afar_solver* s, double R, double Cv, double deltaT, int cellsNum, int facesNum,
                                       int totalBoundaryFacesNum, int maxStencilSize, int maxCompactStencilSize,
                                       int maxLocalBlockStencilSize, int maxCompactLocalBlockStencilSize) {
+  const bool head_done = s && s->head_pending;  // read before check_ready clears it
   afar_status st = check_ready(s);
   if (st) return st;
   if (cellsNum != s->Nc || facesNum != s->Nf || totalBoundaryFacesNum != s->Nb || maxStencilSize != s->maxS ||
@@ -992,6 +1054,15 @@ extern "C" afar_status afar_GPUevolve(afar_solver* s, double R, double Cv, doubl
     set_error("afar_GPUevolve: deltaT, R and Cv must be positive");
     return AFAR_ERR_ARGUMENT;
   }
+  if (head_done && s->graph_tail && s->R == R && s->Cv == Cv) {
+    // afar_adjustTimeStep ran this step's head on the current state: the tail with the caller's
+    // step size completes it, the same kernels as the whole-step graph.  Enqueued, not waited
+    // for: a device-side error of the step surfaces at the next call that waits.
+    k_set_ctl<<<1, 32, 0, s->stream>>>(s->ctl, deltaT, 1.0, 0.0);
+    AFAR_CUDA(cudaGraphLaunch(s->graph_tail, s->stream));
+    AFAR_CUDA(cudaGetLastError());
+    return AFAR_OK;
+  }
   if ((st = ensure_graph(s, R, Cv))) return st;
   return run_impl(s, 1, deltaT, 1.0, 0.0, true);
 }
@@ -1001,6 +1072,7 @@ extern "C" afar_status afar_set_gas(afar_solver* s, double R, double Cv) {
     set_error("afar_set_gas: bad argument");
     return AFAR_ERR_ARGUMENT;
   }
+  s->head_pending = false;
   return ensure_graph(s, R, Cv);
 }
 
@@ -1113,6 +1185,7 @@ extern "C" afar_status afar_get_time(afar_solver* s, double* t, double* lastDt, 
 
 extern "C" afar_status afar_set_time(afar_solver* s, double t) {
   if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  s->head_pending = false;
   AFAR_CUDA(cudaSetDevice(s->device));
   AFAR_CUDA(cudaMemcpyAsync(&s->ctl->t, &t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
@@ -1201,6 +1274,7 @@ extern "C" afar_status afar_debug_limiter64(afar_solver* s, double* lim) {
 extern "C" afar_status afar_upload_state(afar_solver* s, const afar_basicFieldData* FD, const afar_conservedFieldData* cFD,
                                          const afar_conservedFieldData* cFDold) {
   if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
+  s->head_pending = false;
   AFAR_CUDA(cudaSetDevice(s->device));
   return put_state(s, FD, cFD, cFDold);
 }
@@ -1225,6 +1299,7 @@ extern "C" afar_status afar_copyFieldDataDeviceToHost(afar_fieldPointer* h, afar
 extern "C" afar_status afar_state_snapshot(afar_solver* s, int op) {
   if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
   if (op != AFAR_SNAPSHOT_SAVE && op != AFAR_SNAPSHOT_RESTORE) return (set_error("unknown snapshot op %d", op), AFAR_ERR_ARGUMENT);
+  if (op == AFAR_SNAPSHOT_RESTORE) s->head_pending = false;
   AFAR_CUDA(cudaSetDevice(s->device));
   const size_t wb = w_size(s->policy) * (size_t)(s->Nc + s->Nb);
   const size_t ub = sizeof(V4<double>) * (size_t)s->Nc;
@@ -1291,7 +1366,7 @@ extern "C" afar_status afar_freeFieldData(afar_solver* s) {
   if (s->batch) afar_batch_remove(s->batch, s);  // the batch forgets a freed member
   cudaSetDevice(s->device);
   if (s->stream) cudaStreamSynchronize(s->stream);
-  if (s->graph) cudaGraphExecDestroy(s->graph);
+  destroy_graphs(s);
   for (void* p : s->allocs) cudaFree(p);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -1326,6 +1401,7 @@ extern "C" afar_status afar_set_periodic(afar_solver* s, double px, double py) {
 extern "C" afar_status afar_set_write_interval(afar_solver* s, double writeInterval) {
   if (!s || !s->have_fields) return (set_error("solver not initialised"), AFAR_ERR_STATE);
   if (!(writeInterval >= 0.0)) return (set_error("afar_set_write_interval: negative interval"), AFAR_ERR_ARGUMENT);
+  s->head_pending = false;
   AFAR_CUDA(cudaSetDevice(s->device));
   k_set_write_interval<<<1, 32, 0, s->stream>>>(s->ctl, writeInterval);
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
