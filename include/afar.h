@@ -231,11 +231,16 @@ afar_status afar_setDeviceFieldDataStencil(afar_solver* solver, const afar_field
                                            int maxCompactLocalBlockStencilSize);
 
 /* Replaces adjustTimeStep (GPUevolve.h:31-38, GPUevolve.cu:177-204): CFL time step from the
- * current state, min over internal faces (and 1e5). */
+ * current state, min over internal faces (and 1e5).  Outside a batch it computes it as the first
+ * part of the coming step (stage 1 through its flux, whose reduction is this minimum), which the
+ * next afar_GPUevolve on the same solver then completes; any other call in between discards it. */
 afar_status afar_adjustTimeStep(afar_solver* solver, int facesNum, double R, double Cv, double CFL,
                                 double* deltaT);
 
-/* Replaces GPUevolve (GPUevolve.h:40-53, GPUevolve.cu:207-306): one SSP-RK3 step of deltaT. */
+/* Replaces GPUevolve (GPUevolve.h:40-53, GPUevolve.cu:207-306): one SSP-RK3 step of deltaT.
+ * Right after afar_adjustTimeStep it enqueues the rest of the step begun there and returns without
+ * waiting (results are stream-ordered for every later call; a device-side error of the step is
+ * reported by the next call that waits); otherwise it runs and waits for the whole step. */
 afar_status afar_GPUevolve(afar_solver* solver, double R, double Cv, double deltaT, int cellsNum,
                            int facesNum, int totalBoundaryFacesNum, int maxStencilSize,
                            int maxCompactStencilSize, int maxLocalBlockStencilSize,
