@@ -70,6 +70,11 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=500)
     ap.add_argument("--setup", action="store_true",
                     help="time the precompute of the workload's mesh on the host and with its RBF stage on the GPU")
+    ap.add_argument("--accuracy", default="",
+                    help="instead of timing: the mixed policy against the FP64 policy on the configs listed "
+                         "(comma-separated: vortex, step, riemann_mixed, batch), L1/Linf of density and switch flips")
+    ap.add_argument("--acc-steps", type=int, default=100, help="--accuracy step: RK3 steps of the Mach 3 start")
+    ap.add_argument("--acc-sample", type=int, default=8, help="--accuracy batch: solves of the batch re-run")
     ap.add_argument("--serve-requests", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="arrivals per second")
     return ap.parse_args()
@@ -480,13 +485,13 @@ def run_serve(args, dist: Dist):
     """Serving workload: requests arrive as a Poisson process (rate --serve-rate); each takes a mesh
     drawn log-uniformly from a pool of quad Riemann problems of 10k-2M cells and a step count
     uniform in [100, 2000], stopped earlier at t = 0.3 (the four-quadrant problem's usual end; the
-    coarsest mesh breaks down near t = 0.75); 5% of them are solved in the fp64 policy, the rest in
-    mixed.  Each
-    policy has its own afar_server (180 GB budget, 50-step chunks); a request's latency runs from
-    submit to its fields being back in its host buffers.  The pool's precompute is outside the
-    timed region (request inputs are resident host arrays).  Prints served cell-steps/s and the
-    latency percentiles."""
-    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, Server, mesh, precompute
+    coarsest mesh breaks down near t = 0.75), solved in the mixed policy; a 5% sample is also
+    re-solved in the fp64 policy on a second server, both to the same end time, and compared.  Each
+    server has a 180 GB budget and 50-step chunks; a request's latency runs from submit to its
+    fields being back in its host buffers.  The pool's precompute is outside the timed region
+    (request inputs are resident host arrays).  Prints served cell-steps/s of the mixed requests,
+    the latency percentiles and the sample's accuracy."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, CudaSolver, Server, mesh, precompute
     from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
 
     b.build_all()  # with several ranks, each serves its own queue on its own GPU (replicas)
@@ -502,30 +507,60 @@ def run_serve(args, dist: Dist):
     nreq = args.serve_requests
     pick = [int(np.argmin(np.abs(logp - rng.uniform(logp[0], logp[-1])))) for _ in range(nreq)]
     steps = rng.integers(100, 2001, nreq)
-    fp64 = rng.uniform(size=nreq) < 0.05
+    fp64 = rng.uniform(size=nreq) < 0.05  # the sample re-solved in FP64
     gaps = rng.exponential(1.0 / args.serve_rate, nreq)
+    # A sampled request and its FP64 re-solve end at the same time: t_s = min(0.3, 0.8 x its steps x
+    # the mesh's initial Courant step), with room for three times its steps (both land on t_s).
+    dt0 = []
+    for hf, cfg in pool:
+        s_ = CudaSolver(hf, cfg, policy="mixed", device=dist.local)
+        dt0.append(s_.set_delta_t())
+        s_.close()
+    t_sample = {i: min(0.3, 0.8 * int(steps[i]) * dt0[pick[i]]) for i in range(nreq) if fp64[i]}
     servers = {p: Server(p, device=dist.local, hbm_budget_bytes=180 << 30, chunk_steps=50) for p in ("mixed", "fp64")}
     for srv in servers.values():
         srv.wait(srv.submit(*pool[0], n_steps=5))
     dist.barrier()
     t0 = time.perf_counter()
     ids = []
+    resolve = {}
+    accuracy = []
     t_next = t0
     for i in range(nreq):
         t_next += gaps[i]
         while time.perf_counter() < t_next:
             time.sleep(min(1e-3, max(0.0, t_next - time.perf_counter())))
-        srv = servers["fp64" if fp64[i] else "mixed"]
-        ids.append((srv, srv.submit(*pool[pick[i]], t_end=0.3, n_steps=int(steps[i]))))
+        if fp64[i]:
+            kw = {"t_end": t_sample[i], "n_steps": 3 * int(steps[i])}
+            resolve[i] = servers["fp64"].submit(*pool[pick[i]], **kw)
+        else:
+            kw = {"t_end": 0.3, "n_steps": int(steps[i])}
+        ids.append((servers["mixed"], servers["mixed"].submit(*pool[pick[i]], **kw)))
     lat = []
     done_steps = []
+    results = {}
     ok = True
-    for srv, rid in ids:
+    for i, (srv, rid) in enumerate(ids):
         FD, si, ms, n = srv.wait(rid, with_steps=True)
         lat.append(ms)
         done_steps.append(n)
         ok = ok and bool(np.isfinite(FD).all())
-    wall = dist.max(time.perf_counter() - t0)
+        if fp64[i]:
+            results[i] = (FD, si, n)
+    wall = dist.max(time.perf_counter() - t0)  # the served (mixed) requests; the re-solves may run on
+    fp64_work = 0.0
+    for i, rid in resolve.items():
+        FD, si, ms, n = servers["fp64"].wait(rid, with_steps=True)
+        fp64_work += sizes[pick[i]] * n
+        hf, cfg = pool[pick[i]]
+        FDm, sim, nm = results[i]
+        rho = lambda F: F[:hf.nc, 0] / (cfg.R * F[:hf.nc, 3])
+        V = hf.cellVolume
+        d = np.abs(rho(FDm) - rho(FD))
+        accuracy.append({"request": i, "cells": hf.nc, "t": t_sample[i], "steps_mixed": nm, "steps_fp64": n,
+                         "landed": bool(nm < 3 * int(steps[i]) and n < 3 * int(steps[i])),
+                         "L1_rho": float(np.sum(d * V) / np.sum(V)), "Linf_rho": float(d.max()),
+                         "switch_flips": int(np.count_nonzero(si[1:2 * hf.nc:2] != sim[1:2 * hf.nc:2]))})
     st = {p: srv.stats() for p, srv in servers.items()}
     for srv in servers.values():
         srv.close()
@@ -537,13 +572,137 @@ def run_serve(args, dist: Dist):
         "metric": "served cell-RK3-steps/s", "value": work / wall, "unit": "cell-steps/s", "n_gpus": dist.world,
         "higher_is_better": True, "data": "synthetic (quad Riemann meshes 10k-2M cells, seeded)",
         "config": {"workload": "serve_poisson", "requests": nreq, "rate_per_s": args.serve_rate,
-                   "steps": "U[100,2000], at most to t = 0.3", "policies": "mixed, 5% fp64", "chunk_steps": 50,
-                   "budget_bytes": 180 << 30, "fp64_requests": int(fp64.sum())},
+                   "steps": "U[100,2000], at most to t = 0.3", "policy": "mixed; a 5% sample re-solved in fp64",
+                   "chunk_steps": 50, "budget_bytes": 180 << 30, "fp64_resolves": int(fp64.sum())},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(lat.max())},
         "wall_s": wall, "peak_running": {p: v["peakRunning"] for p, v in st.items()},
         "peak_bytes": {p: v["peakBytes"] for p, v in st.items()}, "finite": ok,
+        "fp64_resolve_cell_steps": fp64_work,
+        "accuracy": {"what": "per sampled request: the mixed result against its FP64 re-solve at the same "
+                             "end time (area-weighted L1 and L-inf of density, cells whose final switch differs)",
+                     "requests": accuracy},
     }), flush=True)
+
+
+def compare_policies(hf, a, b):
+    """Mixed state b against FP64 state a on the cells: area-weighted L1 and the L-inf of the
+    density, and the cells whose troubled-cell flag (si[2c]) or final switch (si[2c+1]) differ."""
+    V = hf.cellVolume
+    ra, rb = a["cFD"][:, 0], b["cFD"][:, 0]
+    d = np.abs(ra - rb)
+    nc = hf.nc
+    sa, sb = a["shockIndicator"][:2 * nc], b["shockIndicator"][:2 * nc]
+    l1 = float(np.sum(d * V) / np.sum(V))
+    return {"L1_rho": l1, "Linf_rho": float(d.max()), "rel_L1_rho": l1 / float(np.sum(np.abs(ra) * V) / np.sum(V)),
+            "switch_flips": int(np.count_nonzero(sa[1::2] != sb[1::2])),
+            "troubled_flips": int(np.count_nonzero(sa[0::2] != sb[0::2])),
+            "finite": bool(np.isfinite(ra).all() and np.isfinite(rb).all())}
+
+
+def accuracy_pair(hf, cfg, device, t_end=0.0, n_steps=0, every=10, init=None):
+    """The FP64 policy (checked against the CPU oracle at 1e-10 on small meshes, the FP64 oracle at
+    this scale) and the mixed policy stepped side by side with the same step sizes -- the FP64
+    policy's Courant step, clipped to t_end -- from the same initial state.  Every `every` steps the
+    states and switch decisions are compared; returns the final comparison, the largest L1 seen and
+    the flips summed over the compared steps."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver
+
+    f = CudaSolver(hf, cfg, policy="fp64", device=device)
+    m = CudaSolver(hf, cfg, policy="mixed", device=device)
+    if init is not None:
+        for s in (f, m):
+            s.upload_state(FD=init[0], cFD=init[1], cFDold=init[1])
+    t, k = 0.0, 0
+    worst, sw_sum, tr_sum, samples = 0.0, 0, 0, 0
+    while (n_steps and k < n_steps) or (not n_steps and t < t_end * (1.0 - 1e-12)):
+        dt = f.set_delta_t()
+        if t_end > 0.0:
+            dt = min(dt, t_end - t)
+        f.evolve(dt)
+        m.evolve(dt)
+        t += dt
+        k += 1
+        if k % every == 0:
+            c = compare_policies(hf, f.state(), m.state())
+            worst = max(worst, c["L1_rho"])
+            sw_sum += c["switch_flips"]
+            tr_sum += c["troubled_flips"]
+            samples += 1
+    a, b = f.state(), m.state()
+    out = compare_policies(hf, a, b)
+    out.update({"steps": k, "t": f.time()[0], "max_L1_rho_over_run": max(worst, out["L1_rho"]),
+                "compared_steps": samples, "switch_flips_summed": sw_sum, "troubled_flips_summed": tr_sum})
+    f.close()
+    m.close()
+    return out, a, b
+
+
+def run_accuracy(args, dist: Dist):
+    """Accuracy of the mixed policy against the FP64 policy, per config: the periodic isentropic
+    vortex (256^2 quads on [0,10]^2, CFL 0.5, to t = 2; also against the exact solution), the
+    Mach 3 step (--acc-steps RK3 steps at CFL 0.2 from the impulsive start: the scheme has no
+    positivity fix and the start breaks down at the step corner after ~180 steps, so t = 4 is out
+    of reach in every policy), the 4M-cell mixed quad/triangle Riemann problem to t = 0.3, and a
+    sample of the batched ramps (500 steps each).  One JSON line per config."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, gauss_quadrature, mesh, precompute
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+
+    b.build_all()
+    dev = dist.local
+    out = []
+    for name in [x.strip() for x in args.accuracy.split(",") if x.strip()]:
+        t0 = time.time()
+        line = {"metric": "mixed vs FP64 policy", "config": name,
+                "steps_dt": "shared: the FP64 policy's Courant step each step"}
+        if name == "vortex":
+            m = mesh.periodic_quad_grid(256, 256, 0.0, 10.0, 0.0, 10.0)
+            cfg = CaseConfig(stencilType="edgeNeighbour", CFL=0.5)
+            q = gauss_quadrature(m, cfg)
+            U0 = mesh.vortex_cell_averages(m, q, 0.0, centre=(5.0, 5.0))
+            W0 = mesh.primitive_from_conserved(U0)
+            hf = precompute(m, cfg, W0, None, want_rbf64=True, device=dev)
+            r, a, bb = accuracy_pair(hf, cfg, dev, t_end=2.0, every=25, init=(W0, U0))
+            exact = mesh.vortex_cell_averages(m, q, 2.0, centre=(5.0, 5.0))[:, 0]
+            area = m.cell_areas()
+            r["L1_rho_vs_exact"] = {p: float(np.sum(np.abs(s_["cFD"][:, 0] - exact) * area) / area.sum())
+                                    for p, s_ in (("fp64", a), ("mixed", bb))}
+        elif name == "step":
+            m = mesh.forward_step_triangles(args.points, seed=args.seed)
+            W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
+            cfg = CaseConfig(stencilType="edgeNeighbour", CFL=args.cfl)
+            hf = precompute(m, cfg, W, Wb, want_rbf64=True, device=dev)
+            r, _, _ = accuracy_pair(hf, cfg, dev, n_steps=args.acc_steps, every=10)
+        elif name == "riemann_mixed":
+            m = mesh.riemann_mixed(args.mixed_n, seed=args.seed)
+            W, Wb = mesh.riemann_fields(m)
+            cfg = CaseConfig(stencilType="edgeNeighbour", CFL=0.3)
+            hf = precompute(m, cfg, W, Wb, want_rbf64=True, device=dev)
+            r, _, _ = accuracy_pair(hf, cfg, dev, t_end=0.3, every=100)
+        elif name == "batch":
+            rng = np.random.default_rng(args.seed)
+            params = [batch_member_params(rng) for _ in range(args.batch_solves)]
+            pick = np.linspace(0, args.batch_solves - 1, args.acc_sample).round().astype(int)
+            members = []
+            for k in pick:
+                mm, W, Wb, cfg = batch_member(params[k])
+                hf = precompute(mm, cfg, W, Wb, want_rbf64=True, device=dev)
+                rk, _, _ = accuracy_pair(hf, cfg, dev, n_steps=args.batch_steps, every=50)
+                rk.update({"member": int(k), "cells": mm.n_cells})
+                members.append(rk)
+            r = {"members": members, "L1_rho_max": max(x["L1_rho"] for x in members),
+                 "Linf_rho_max": max(x["Linf_rho"] for x in members),
+                 "switch_flips_total": sum(x["switch_flips"] for x in members)}
+            hf = None
+        else:
+            raise SystemExit(f"--accuracy: unknown config {name}")
+        if hf is not None:
+            line["cells"] = hf.nc
+        line.update(r)
+        line["wall_s"] = round(time.time() - t0, 1)
+        if dist.rank == 0:
+            print(json.dumps(line), flush=True)
+        out.append(line)
 
 
 def run_setup(args, dist: Dist):
@@ -583,6 +742,29 @@ def run_setup(args, dist: Dist):
     }), flush=True)
 
 
+def batch_member_params(rng):
+    """One solve of the batched workload: cells log-uniform in [5k, 200k], ramp angle U[5, 20]
+    degrees, inflow Mach U[1.5, 4], vortex strength U[0, 5] (drawn in this order)."""
+    nc = float(np.exp(rng.uniform(np.log(5e3), np.log(2e5))))
+    angle = rng.uniform(5.0, 20.0)
+    u0 = rng.uniform(1.5, 4.0) * np.sqrt(1.4)  # rho = p = 1: sound speed sqrt(1.4)
+    strength = rng.uniform(0.0, 5.0)
+    return nc, angle, u0, strength
+
+
+def batch_member(params):
+    """The compression ramp of batch_member_params: quads in a 2:1 channel, label-6 inflow, an
+    isentropic vortex carried in the stream; face-neighbour stencils, CFL 0.3."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh
+
+    nc, angle, u0, strength = params
+    ny = max(8, int(round(np.sqrt(nc / 2.0))))
+    m = mesh.wedge_quads(2 * ny, ny, angle)
+    W = mesh.vortex_fields(m.cell_centres(), strength=strength, xc=0.5, yc=0.6, u0=u0, v0=0.0)
+    Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.5, yc=0.6, u0=u0, v0=0.0)
+    return m, W, Wb, CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+
+
 def run_batch(args, dist: Dist):
     """Batched workload (the shape of the batched config): --batch-solves independent supersonic
     compression ramps, cells log-uniform in [5k, 200k] (quads, 2:1 channel), inflow Mach U[1.5, 4]
@@ -598,14 +780,7 @@ def run_batch(args, dist: Dist):
     t0 = time.time()
     solvers, cells = [], []
     for k in range(args.batch_solves):
-        nc = float(np.exp(rng.uniform(np.log(5e3), np.log(2e5))))
-        ny = max(8, int(round(np.sqrt(nc / 2.0))))
-        m = mesh.wedge_quads(2 * ny, ny, rng.uniform(5.0, 20.0))
-        u0 = rng.uniform(1.5, 4.0) * np.sqrt(1.4)  # rho = p = 1: sound speed sqrt(1.4)
-        strength = rng.uniform(0.0, 5.0)
-        W = mesh.vortex_fields(m.cell_centres(), strength=strength, xc=0.5, yc=0.6, u0=u0, v0=0.0)
-        Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.5, yc=0.6, u0=u0, v0=0.0)
-        cfg = CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+        m, W, Wb, cfg = batch_member(batch_member_params(rng))
         s = CudaSolver(precompute(m, cfg, W, Wb), cfg, policy="mixed", device=dist.local)
         solvers.append(s)
         cells.append(m.n_cells)
@@ -651,7 +826,9 @@ def main():
     args = parse()
     dist = Dist()
     try:
-        if args.setup:
+        if args.accuracy:
+            run_accuracy(args, dist)
+        elif args.setup:
             run_setup(args, dist)
         elif args.serve:
             run_serve(args, dist)
