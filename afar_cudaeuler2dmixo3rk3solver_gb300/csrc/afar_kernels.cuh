@@ -164,15 +164,13 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
   }
   const V4<WT> wc = a.W[c];
   const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  // O3 sums in difference form: sum_i w_i phi_i = phi_c + sum_{i>0} w_i (phi_i - phi_c), since the
+  // weights of every face side sum to one.  In FP32 this drops the error phi_c * (sum of the float
+  // weights' rounding), which is the same every step and grows like a change of scheme; what
+  // remains is rounding relative to the neighbour differences.
   G acc[kMaxFaces][4];
 #pragma unroll
-  for (int fi = 0; fi < kMaxFaces; ++fi) {  // each face side's O3 sum starts with the cell's own term
-    const S w0 = inner[fi] ? a.wts[(size_t)(fi * wrow) * ldc + c] : S(0);
-    acc[fi][0] = w0 * pc;
-    acc[fi][1] = w0 * uxc;
-    acc[fi][2] = w0 * uyc;
-    acc[fi][3] = w0 * tc;
-  }
+  for (int fi = 0; fi < kMaxFaces; ++fi) acc[fi][0] = acc[fi][1] = acc[fi][2] = acc[fi][3] = G(0);
   G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
   S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
   S pn[kMaxFaces];  // pressure of the cell across each face
@@ -193,20 +191,17 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
     for (int u = 0; u < kMaxFaces; ++u) {
       if (u < nS) {
         const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        const S dp = vx - pc, dux = vy - uxc, duy = vz - uyc, dt = vw - tc;
         if (u < nM) {  // reference :148-169 and :190-205
           const S M1 = lm[u].x, M2 = lm[u].y;
-          S dphi = vx - pc;
-          gPx += M1 * dphi;
-          gPy += M2 * dphi;
-          dphi = vy - uxc;
-          gUxx += M1 * dphi;
-          gUyx += M2 * dphi;
-          dphi = vz - uyc;
-          gUxy += M1 * dphi;
-          gUyy += M2 * dphi;
-          dphi = vw - tc;
-          gTx += M1 * dphi;
-          gTy += M2 * dphi;
+          gPx += M1 * dp;
+          gPy += M2 * dp;
+          gUxx += M1 * dux;
+          gUyx += M2 * dux;
+          gUxy += M1 * duy;
+          gUyy += M2 * duy;
+          gTx += M1 * dt;
+          gTy += M2 * dt;
           pMax = fmx(vx, pMax);
           pMin = fmn(vx, pMin);
           uxMax = fmx(vy, uxMax);
@@ -219,10 +214,10 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
         }
 #pragma unroll
         for (int fi = 0; fi < kMaxFaces; ++fi) {
-          acc[fi][0] += wv[u][fi] * vx;
-          acc[fi][1] += wv[u][fi] * vy;
-          acc[fi][2] += wv[u][fi] * vz;
-          acc[fi][3] += wv[u][fi] * vw;
+          acc[fi][0] += wv[u][fi] * dp;
+          acc[fi][1] += wv[u][fi] * dux;
+          acc[fi][2] += wv[u][fi] * duy;
+          acc[fi][3] += wv[u][fi] * dt;
         }
       }
     }
@@ -244,13 +239,13 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       if (ci0 + u < nS) {
-        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        const S dp = (S)wj[u].x - pc, dux = (S)wj[u].y - uxc, duy = (S)wj[u].z - uyc, dt = (S)wj[u].w - tc;
 #pragma unroll
         for (int fi = 0; fi < kMaxFaces; ++fi) {
-          acc[fi][0] += wv[u][fi] * vx;
-          acc[fi][1] += wv[u][fi] * vy;
-          acc[fi][2] += wv[u][fi] * vz;
-          acc[fi][3] += wv[u][fi] * vw;
+          acc[fi][0] += wv[u][fi] * dp;
+          acc[fi][1] += wv[u][fi] * dux;
+          acc[fi][2] += wv[u][fi] * duy;
+          acc[fi][3] += wv[u][fi] * dt;
         }
       }
     }
@@ -291,7 +286,7 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
       const G dx = d.x, dy = d.y;
       const V2<S> rf = a.sr[fi * ldc + c];
       const S deltaR = rf.x, fraction = rf.y;
-      const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
+      const G pf = (G)pc + acc[fi][0], uxf = (G)uxc + acc[fi][1], uyf = (G)uyc + acc[fi][2], tf = (G)tc + acc[fi][3];
       S phif;
       V4<G> o;
       limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
@@ -366,10 +361,11 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
   const unsigned ne = (unsigned)min(kTile, a.ldc - c0);  // elements of a row slice
   const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
   const int M = a.maxM, S = a.tileS[blk];
-  const int rows = 4 * M + S + M * (S + 1) + 1;
+  const int rows = 4 * M + S + M * S + 1;  // weight rows 1..S of each face slot (row 0, the cell's own
+                                           // weight, drops out of the difference-form sums)
   if (lane == 0) {
     mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16);
-    mbar_arrive_expect_tx(bar + 1, ne * (M * (8 + 8 + 8) + M * (S + 1) * 4));
+    mbar_arrive_expect_tx(bar + 1, ne * (M * (8 + 8 + 8) + M * S * 4));
   }
   __syncwarp();
   for (int r = lane; r < rows; r += 32) {
@@ -404,8 +400,8 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
       bytes = ne * 4;
       b = bar;
     } else if (r < rows - 1) {
-      const int q = r - 4 * M - S, fi = q / (S + 1);
-      const int k = fi * (a.maxS + 1) + (q - fi * (S + 1));  // row j = q - fi (S + 1) of face slot fi
+      const int q = r - 4 * M - S, fi = q / S;
+      const int k = fi * (a.maxS + 1) + 1 + (q - fi * S);  // row j = 1 + q - fi S of face slot fi
       dst = sm + L.off_wts + k * kTile * 4;
       src = a.wts + (size_t)k * a.ldc + c0;
       bytes = ne * 4;
@@ -479,15 +475,9 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   // O3 weights of boundary-face and missing slots are zero in the operator rows (setup), so only
   // slots past this mesh's largest cell (a batch may stage fewer rows than NF) are skipped
   const int nfm = a.maxM;
-  G acc[NF][4];
+  G acc[NF][4];  // O3 sums in difference form, as in recon_reg_body
 #pragma unroll
-  for (int fi = 0; fi < NF; ++fi) {  // each face side's O3 sum starts with the cell's own term
-    const S w0 = fi < nfm ? s_wts[(fi * wrow) * kTile + t] : S(0);
-    acc[fi][0] = w0 * pc;
-    acc[fi][1] = w0 * uxc;
-    acc[fi][2] = w0 * uyc;
-    acc[fi][3] = w0 * tc;
-  }
+  for (int fi = 0; fi < NF; ++fi) acc[fi][0] = acc[fi][1] = acc[fi][2] = acc[fi][3] = G(0);
   G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
   S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
   S pn[NF];  // pressure of the cell across each face
@@ -504,21 +494,18 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
       const int ci = ci0 + u;
       if (ci < nS) {
         const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        const S dp = vx - pc, dux = vy - uxc, duy = vz - uyc, dt = vw - tc;
         if (ci < nM) {  // the face neighbours (compact stencil) come first: reference :148-169, :190-205
           const V2<S> lm = s_lsm[ci * kTile + t];
           const S M1 = lm.x, M2 = lm.y;
-          S dphi = vx - pc;
-          gPx += M1 * dphi;
-          gPy += M2 * dphi;
-          dphi = vy - uxc;
-          gUxx += M1 * dphi;
-          gUyx += M2 * dphi;
-          dphi = vz - uyc;
-          gUxy += M1 * dphi;
-          gUyy += M2 * dphi;
-          dphi = vw - tc;
-          gTx += M1 * dphi;
-          gTy += M2 * dphi;
+          gPx += M1 * dp;
+          gPy += M2 * dp;
+          gUxx += M1 * dux;
+          gUyx += M2 * dux;
+          gUxy += M1 * duy;
+          gUyy += M2 * duy;
+          gTx += M1 * dt;
+          gTy += M2 * dt;
           pMax = fmx(vx, pMax);
           pMin = fmn(vx, pMin);
           uxMax = fmx(vy, uxMax);
@@ -534,10 +521,10 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
 #pragma unroll
         for (int fi = 0; fi < NF; ++fi) {
           const S wv = fi < nfm ? s_wts[(fi * wrow + ci + 1) * kTile + t] : S(0);
-          acc[fi][0] += wv * vx;
-          acc[fi][1] += wv * vy;
-          acc[fi][2] += wv * vz;
-          acc[fi][3] += wv * vw;
+          acc[fi][0] += wv * dp;
+          acc[fi][1] += wv * dux;
+          acc[fi][2] += wv * duy;
+          acc[fi][3] += wv * dt;
         }
       }
     }
@@ -578,7 +565,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
       const G dx = d.x, dy = d.y;
       const V2<S> rf = s_sr[fi * kTile + t];
       const S deltaR = rf.x, fraction = rf.y;
-      const G pf = acc[fi][0], uxf = acc[fi][1], uyf = acc[fi][2], tf = acc[fi][3];
+      const G pf = (G)pc + acc[fi][0], uxf = (G)uxc + acc[fi][1], uyf = (G)uyc + acc[fi][2], tf = (G)tc + acc[fi][3];
       S phif;
       V4<G> o;
       limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
