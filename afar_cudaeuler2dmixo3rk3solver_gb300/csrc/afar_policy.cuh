@@ -196,16 +196,22 @@ __device__ __forceinline__ DF df_div(const DF a, const DF b, const float r) {
 // cell that carry the state to about 35 bits.  Differences between neighbouring states (the inputs
 // of the reconstruction, the BVD test and the face fluxes) are then exact to far below their own
 // size, where float states alone would round them at the states' size.
+__device__ __forceinline__ float lo_one(const unsigned short e, const float hi) {
+  return __half2float(__ushort_as_half(e)) * hi * 0x1p-24f;
+}
+// The code of lo, kept so that the decoded remainder stays strictly below half an ulp of hi: then
+// hi + remainder, taken as a double, rounds back to hi, and a state written out as doubles and read
+// back is the same pair (checkpoints resume bitwise).
 __device__ __forceinline__ unsigned short lo_half(const float lo, const float hi) {
-  const float r = hi != 0.f ? __fdividef(lo, hi) * 0x1p24f : 0.f;
-  return __half_as_ushort(__float2half_rn(r));
+  if (hi == 0.f) return 0;
+  unsigned short e = __half_as_ushort(__float2half_rn(__fdividef(lo, hi) * 0x1p24f));
+  const float a = fabsf(hi);
+  if (fabsf(lo_one(e, hi)) >= 0.5f * (nextafterf(a, INFINITY) - a) && (e & 0x7fffu)) e = (unsigned short)(e - 1u);
+  return e;
 }
 __device__ __forceinline__ uint2 lo_pack(const V4<float> hi, const V4<float> lo) {
   return make_uint2((unsigned)lo_half(lo.x, hi.x) | ((unsigned)lo_half(lo.y, hi.y) << 16),
                     (unsigned)lo_half(lo.z, hi.z) | ((unsigned)lo_half(lo.w, hi.w) << 16));
-}
-__device__ __forceinline__ float lo_one(const unsigned short e, const float hi) {
-  return __half2float(__ushort_as_half(e)) * hi * 0x1p-24f;
 }
 __device__ __forceinline__ V4<float> lo_unpack(const V4<float> hi, const uint2 e) {
   return V4<float>{lo_one((unsigned short)(e.x & 0xffffu), hi.x), lo_one((unsigned short)(e.x >> 16), hi.y),
