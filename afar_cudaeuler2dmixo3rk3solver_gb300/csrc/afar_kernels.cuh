@@ -87,21 +87,17 @@ struct StageArgs {
   const S* wts;               // [maxM*(maxS+1)][ldc]
   // state and stage intermediates
   V4<typename P::W>* W;       // Nc+Nb
-  uint2* Wlo;                 // mixed: Nc+Nb packed remainders of W (lo_pack), else null
   V4<double>* U;              // Nc conserved state (mixed: DF4 float pairs, same 32 bytes)
   V4<double>* U0;             // Nc state at the start of the step (mixed: DF4)
   V4<G>* grad;                // 2Nc
   V4<S>* lim;                 // Nc
   int8_t* si;                 // 2(Nc+Nb): [2c] troubled-cell flag, [2c+1] final switch type
   V4<G>* fv;                  // 2Nf
-  V4<typename P::F>* flux;    // Nf+Nb (mixed: the face flux minus the owner's own flux, F - F(W_own).Sf)
-  V4<typename P::F>* fluxB;   // mixed: Nf, the face flux minus the neighbour's own flux
-  const int* bnei;            // Nb owner cell of each boundary face
+  V4<typename P::F>* flux;    // Nf+Nb
   StepCtl* ctl;
   V4<double>* res_dbg;        // optional residual dump (parity hook)
   double R, Cv, invR, gamma;
   float gm1f, invRf;  // gamma - 1 and 1/R as floats (mixed)
-  float gm1lo, invRlo;  // their float-pair remainders (mixed: the primitive state as float pairs)
   float Rf, Cvf, gRf;  // R, Cv and gamma*R as floats (mixed)
   double px, py;       // periods of a periodic mesh (0: none); setup kernels only
   const V2<float>* dtgf;  // Nf (delta r, fraction) as floats (mixed Courant estimate)
@@ -139,76 +135,6 @@ __device__ __forceinline__ void limiter_process_fast(float& limiter, float& phif
 // (d2GaussQuadrature.C:65-148); the stencil upload rejects larger compact stencils.
 constexpr int kMaxFaces = 4;
 
-// The face values, limiter and troubled-cell flag of one mixed-policy cell (reference
-// cudaLimiter.h:208-314) from its data relative to the cell: the O3 sums (difference form), the
-// pressure across each face and the compact-stencil extremes as differences to the cell's state.
-// Face values are written as increments over the cell's state; positivity and the smoothness
-// scale use the absolute pressure and temperature (pc, tc).  sg(fi), sr(fi): the face offset and
-// (delta r, fraction) of face slot fi.
-template <class P, int NF, class SG, class SR>
-__device__ __forceinline__ void mixed_face_values(const StageArgs<P>& a, const int c, const int (&fid)[NF],
-                                                  const bool (&inner)[NF], const float (&acc)[NF][4],
-                                                  const float (&pn)[NF], const float pc, const float tc,
-                                                  const float gPx, const float gPy, const float gUxx,
-                                                  const float gUyx, const float gUxy, const float gUyy,
-                                                  const float gTx, const float gTy, const float pMax,
-                                                  const float pMin, const float uxMax, const float uxMin,
-                                                  const float uyMax, const float uyMin, const float tMax,
-                                                  const float tMin, SG sg, SR sr) {
-  const float SMALL = 1e-5f, VSMALL = 1e-10f;
-  V4<float> Lm;
-  int8_t flag0;
-  if (fabsf(tMax - tMin) < VSMALL) {  // reference :208-233
-    Lm = V4<float>{1.f, 1.f, 1.f, 1.f};
-#pragma unroll
-    for (int fi = 0; fi < NF; ++fi) {
-      if (!inner[fi]) continue;
-      const bool isNei = fid[fi] < 0;
-      const int f = abs(fid[fi]) - 1;
-      const V2<float> d = sg(fi);
-      a.fv[2 * f + isNei] = V4<float>{gPx * d.x + gPy * d.y, gUxx * d.x + gUyx * d.y, gUxy * d.x + gUyy * d.y,
-                                      gTx * d.x + gTy * d.y};
-    }
-    flag0 = 0;
-  } else {  // reference :235-314
-    float lp = 2.f, lux = 2.f, luy = 2.f, lt = 2.f;
-    float smooth = 0.f;
-    bool notTrouble = true;
-#pragma unroll
-    for (int fi = 0; fi < NF; ++fi) {
-      if (!inner[fi]) continue;
-      const bool isNei = fid[fi] < 0;
-      const int f = abs(fid[fi]) - 1;
-      const V2<float> d = sg(fi);
-      const V2<float> rf = sr(fi);
-      const float deltaR = rf.x, fraction = rf.y;
-      float phif;
-      V4<float> o;
-      limiter_process_fast(lp, phif, 0.f, pMax, pMin, gPx, gPy, d.x, d.y);
-      o.x = fabsf(pMax - pMin) >= SMALL ? acc[fi][0] : phif;
-      notTrouble = pc + phif > 0.f;
-      smooth = fmx(smooth, __fdividef(fabsf(fraction * pn[fi] - phif), deltaR) +
-                               (pc + acc[fi][0] <= 0.f) * 1e20f + (pc + phif <= 0.f) * 1e20f);
-      limiter_process_fast(lux, phif, 0.f, uxMax, uxMin, gUxx, gUyx, d.x, d.y);
-      o.y = fabsf(uxMax - uxMin) >= SMALL ? acc[fi][1] : phif;
-      limiter_process_fast(luy, phif, 0.f, uyMax, uyMin, gUxy, gUyy, d.x, d.y);
-      o.z = fabsf(uyMax - uyMin) >= SMALL ? acc[fi][2] : phif;
-      limiter_process_fast(lt, phif, 0.f, tMax, tMin, gTx, gTy, d.x, d.y);
-      o.w = fabsf(tMax - tMin) >= SMALL ? acc[fi][3] : phif;
-      notTrouble = tc + phif > 0.f;
-      a.fv[2 * f + isNei] = o;
-    }
-    Lm.x = fmx(lp, 0.f) * notTrouble;
-    Lm.y = fmx(lux, 0.f) * notTrouble;
-    Lm.z = fmx(luy, 0.f) * notTrouble;
-    Lm.w = fmx(lt, 0.f) * notTrouble;
-    smooth = __fdividef(smooth, (pc + 0.5f * (pMax + pMin)) * notTrouble + VSMALL);
-    flag0 = (smooth > 1.f);
-  }
-  a.lim[c] = Lm;
-  a.si[2 * c] = flag0;
-}
-
 // reconstruct, register-pass variant for the mixed policy (the autotuner's alternative to the
 // tile-staged kernel): LS gradient, stencil min/max, raw limiter, O3 RBF face values of this
 // cell's side of each internal face, troubled-cell flag.
@@ -219,6 +145,9 @@ __device__ __forceinline__ void mixed_face_values(const StageArgs<P>& a, const i
 // still accumulated in stencil order, as in the reference.
 template <class P>
 __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int blk) {
+  using S = typename P::S;
+  using G = typename P::G;
+  using WT = typename P::W;
   const int c = blk * blockDim.x + threadIdx.x;
   if (c >= a.Nc) return;
   const int ldc = a.ldc;
@@ -226,86 +155,163 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
   const int wrow = a.maxS + 1;
   int fid[kMaxFaces];
   bool inner[kMaxFaces];
-  V2<float> lm[kMaxFaces];
+  V2<S> lm[kMaxFaces];
 #pragma unroll
   for (int fi = 0; fi < kMaxFaces; ++fi) {
     fid[fi] = fi < nM ? a.cf[fi * ldc + c] : 1;
     inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
-    lm[fi] = fi < nM ? a.lsm[fi * ldc + c] : V2<float>{0.f, 0.f};
+    lm[fi] = fi < nM ? a.lsm[fi * ldc + c] : V2<S>{S(0), S(0)};
   }
-  const V4<float> wc = a.W[c];
-  const V4<float> wcl = lo_unpack(wc, a.Wlo[c]);
-  float acc[kMaxFaces][4];  // O3 sums in difference form: sum_{i>0} w_i (phi_i - phi_c)
+  const V4<WT> wc = a.W[c];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  // O3 sums in difference form: sum_i w_i phi_i = phi_c + sum_{i>0} w_i (phi_i - phi_c), since the
+  // weights of every face side sum to one.  In FP32 this drops the error phi_c * (sum of the float
+  // weights' rounding), which is the same every step and grows like a change of scheme; what
+  // remains is rounding relative to the neighbour differences.
+  G acc[kMaxFaces][4];
 #pragma unroll
-  for (int fi = 0; fi < kMaxFaces; ++fi) acc[fi][0] = acc[fi][1] = acc[fi][2] = acc[fi][3] = 0.f;
-  float gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
-  float pMax = 0.f, pMin = 0.f, uxMax = 0.f, uxMin = 0.f, uyMax = 0.f, uyMin = 0.f, tMax = 0.f, tMin = 0.f;
-  float pn[kMaxFaces];  // pressure of the cell across each face, relative to the cell
+  for (int fi = 0; fi < kMaxFaces; ++fi) acc[fi][0] = acc[fi][1] = acc[fi][2] = acc[fi][3] = G(0);
+  G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
+  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
+  S pn[kMaxFaces];  // pressure of the cell across each face
+  {  // members 0..3: the face neighbours (compact stencil) come first
+    int j[kMaxFaces];
 #pragma unroll
-  for (int fi = 0; fi < kMaxFaces; ++fi) pn[fi] = 0.f;
-  constexpr int U = 4;
-  for (int ci0 = 0; ci0 < nS; ci0 += U) {
-    int j[U];
+    for (int u = 0; u < kMaxFaces; ++u) j[u] = u < nS ? a.sten[u * ldc + c] : c;
+    V4<WT> wj[kMaxFaces];
 #pragma unroll
-    for (int u = 0; u < U; ++u) j[u] = (ci0 + u < nS) ? a.sten[(ci0 + u) * ldc + c] : c;
-    V4<float> wj[U];
-    uint2 wjl[U];
+    for (int u = 0; u < kMaxFaces; ++u) wj[u] = a.W[j[u]];
+    S wv[kMaxFaces][kMaxFaces];
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      wj[u] = a.W[j[u]];
-      wjl[u] = a.Wlo[j[u]];
-    }
-    float wv[U][kMaxFaces];
-#pragma unroll
-    for (int u = 0; u < U; ++u)
+    for (int u = 0; u < kMaxFaces; ++u)
 #pragma unroll
       for (int fi = 0; fi < kMaxFaces; ++fi)
-        wv[u][fi] = (ci0 + u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + ci0 + u + 1) * ldc + c] : 0.f;
+        wv[u][fi] = (u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + u + 1) * ldc + c] : S(0);
 #pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int ci = ci0 + u;
-      if (ci < nS) {
-        const V4<float> d = state_diff(wc, wcl, wj[u], lo_unpack(wj[u], wjl[u]));
-        if (ci < nM) {  // reference :148-169 and :190-205
-#pragma unroll
-          for (int fi = 0; fi < kMaxFaces; ++fi)
-            if (fi == ci) {
-              const float M1 = lm[fi].x, M2 = lm[fi].y;
-              gPx += M1 * d.x;
-              gPy += M2 * d.x;
-              gUxx += M1 * d.y;
-              gUyx += M2 * d.y;
-              gUxy += M1 * d.z;
-              gUyy += M2 * d.z;
-              gTx += M1 * d.w;
-              gTy += M2 * d.w;
-              pn[fi] = d.x;
-            }
-          pMax = fmx(d.x, pMax);
-          pMin = fmn(d.x, pMin);
-          uxMax = fmx(d.y, uxMax);
-          uxMin = fmn(d.y, uxMin);
-          uyMax = fmx(d.z, uyMax);
-          uyMin = fmn(d.z, uyMin);
-          tMax = fmx(d.w, tMax);
-          tMin = fmn(d.w, tMin);
+    for (int u = 0; u < kMaxFaces; ++u) {
+      if (u < nS) {
+        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        const S dp = vx - pc, dux = vy - uxc, duy = vz - uyc, dt = vw - tc;
+        if (u < nM) {  // reference :148-169 and :190-205
+          const S M1 = lm[u].x, M2 = lm[u].y;
+          gPx += M1 * dp;
+          gPy += M2 * dp;
+          gUxx += M1 * dux;
+          gUyx += M2 * dux;
+          gUxy += M1 * duy;
+          gUyy += M2 * duy;
+          gTx += M1 * dt;
+          gTy += M2 * dt;
+          pMax = fmx(vx, pMax);
+          pMin = fmn(vx, pMin);
+          uxMax = fmx(vy, uxMax);
+          uxMin = fmn(vy, uxMin);
+          uyMax = fmx(vz, uyMax);
+          uyMin = fmn(vz, uyMin);
+          tMax = fmx(vw, tMax);
+          tMin = fmn(vw, tMin);
+          pn[u] = vx;
         }
 #pragma unroll
         for (int fi = 0; fi < kMaxFaces; ++fi) {
-          acc[fi][0] += wv[u][fi] * d.x;
-          acc[fi][1] += wv[u][fi] * d.y;
-          acc[fi][2] += wv[u][fi] * d.z;
-          acc[fi][3] += wv[u][fi] * d.w;
+          acc[fi][0] += wv[u][fi] * dp;
+          acc[fi][1] += wv[u][fi] * dux;
+          acc[fi][2] += wv[u][fi] * duy;
+          acc[fi][3] += wv[u][fi] * dt;
         }
       }
     }
   }
-  a.grad[2 * c] = V4<float>{gPx, gPy, gUxx, gUxy};
-  a.grad[2 * c + 1] = V4<float>{gUyx, gUyy, gTx, gTy};
-  mixed_face_values<P, kMaxFaces>(a, c, fid, inner, acc, pn, wc.x, wc.w, gPx, gPy, gUxx, gUyx, gUxy, gUyy, gTx,
-                                  gTy, pMax, pMin, uxMax, uxMin, uyMax, uyMin, tMax, tMin,
-                                  [&](int fi) { return a.sg[fi * ldc + c]; },
-                                  [&](int fi) { return a.sr[fi * ldc + c]; });
+  constexpr int U = sizeof(WT) == 4 ? 4 : 2;
+  for (int ci0 = kMaxFaces; ci0 < nS; ci0 += U) {  // the rest of the stencil: O3 sums only
+    int j[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) j[u] = (ci0 + u < nS) ? a.sten[(ci0 + u) * ldc + c] : c;
+    V4<WT> wj[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) wj[u] = a.W[j[u]];
+    S wv[U][kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int fi = 0; fi < kMaxFaces; ++fi)
+        wv[u][fi] = (ci0 + u < nS && inner[fi]) ? a.wts[(size_t)(fi * wrow + ci0 + u + 1) * ldc + c] : S(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (ci0 + u < nS) {
+        const S dp = (S)wj[u].x - pc, dux = (S)wj[u].y - uxc, duy = (S)wj[u].z - uyc, dt = (S)wj[u].w - tc;
+#pragma unroll
+        for (int fi = 0; fi < kMaxFaces; ++fi) {
+          acc[fi][0] += wv[u][fi] * dp;
+          acc[fi][1] += wv[u][fi] * dux;
+          acc[fi][2] += wv[u][fi] * duy;
+          acc[fi][3] += wv[u][fi] * dt;
+        }
+      }
+    }
+  }
+  a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
+  a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
+
+  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
+  V4<S> L;
+  int8_t flag0;
+  if (fab(tMax - tMin) < VSMALL) {  // reference :208-233
+    L = V4<S>{S(1), S(1), S(1), S(1)};
+#pragma unroll
+    for (int fi = 0; fi < kMaxFaces; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      V4<G> o;
+      o.x = (G)(pc) + gPx * dx + gPy * dy;
+      o.y = (G)(uxc) + gUxx * dx + gUyx * dy;
+      o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
+      o.w = (G)(tc) + gTx * dx + gTy * dy;
+      a.fv[2 * f + isNei] = o;
+    }
+    flag0 = 0;
+  } else {  // reference :235-314
+    S lp = S(2), lux = S(2), luy = S(2), lt = S(2);
+    S smooth = S(0);
+    bool notTrouble = true;
+#pragma unroll
+    for (int fi = 0; fi < kMaxFaces; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = a.sg[fi * ldc + c];
+      const G dx = d.x, dy = d.y;
+      const V2<S> rf = a.sr[fi * ldc + c];
+      const S deltaR = rf.x, fraction = rf.y;
+      const G pf = (G)pc + acc[fi][0], uxf = (G)uxc + acc[fi][1], uyf = (G)uyc + acc[fi][2], tf = (G)tc + acc[fi][3];
+      S phif;
+      V4<G> o;
+      limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
+      o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
+      notTrouble = phif > S(0);
+      smooth = fmx(smooth, __fdividef(fab((S(1) - fraction) * pc + fraction * pn[fi] - phif), deltaR) +
+                               (pf <= S(0)) * AFAR_LIT(S, 1e20) + (phif <= S(0)) * AFAR_LIT(S, 1e20));
+      limiter_process_fast(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
+      o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
+      limiter_process_fast(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
+      o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
+      limiter_process_fast(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
+      o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
+      notTrouble = phif > S(0);
+      a.fv[2 * f + isNei] = o;
+    }
+    L.x = fmx(lp, S(0)) * notTrouble;
+    L.y = fmx(lux, S(0)) * notTrouble;
+    L.z = fmx(luy, S(0)) * notTrouble;
+    L.w = fmx(lt, S(0)) * notTrouble;
+    smooth = __fdividef(smooth, S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
+    flag0 = (smooth > S(1));
+  }
+  a.lim[c] = L;
+  a.si[2 * c] = flag0;
 }
 
 // ---------------------------------------------------------------- mixed reconstruct, tile-staged
@@ -316,7 +322,7 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
 // while registers stay free for the stencil gathers, which hit L2.
 constexpr int kTile = 128;
 struct ReconTile {
-  unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_wlo, off_bar, bytes;
+  unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_bar, bytes;
 };
 __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int maxS) {
   ReconTile L;
@@ -335,8 +341,6 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
   o += maxM * (maxS + 1) * kTile * 4;
   L.off_w = o;
   o += kTile * 16;
-  L.off_wlo = o;  // the own states' packed remainders
-  o += kTile * 8;
   L.off_bar = o;  // two mbarriers: the gather inputs, then the rest
   L.bytes = o + 16;
   return L;
@@ -359,9 +363,8 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
   const int M = a.maxM, S = a.tileS[blk];
   const int rows = 4 * M + S + M * S + 1;  // weight rows 1..S of each face slot (row 0, the cell's own
                                            // weight, drops out of the difference-form sums)
-  const unsigned nlo = ((nw + 1) & ~1u) * 8;  // a multiple of 16 bytes (the array has two spare entries)
   if (lane == 0) {
-    mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16 + nlo);
+    mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16);
     mbar_arrive_expect_tx(bar + 1, ne * (M * (8 + 8 + 8) + M * S * 4));
   }
   __syncwarp();
@@ -410,7 +413,6 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
     }
     bulk_to_smem(dst, src, bytes, b);
   }
-  if (lane == 0) bulk_to_smem(sm + L.off_wlo, a.Wlo + c0, nlo, bar);
 }
 
 // reconstruct (reference cudaLimiter.h:53-316) for the mixed policy from the staged tile: LS
@@ -462,89 +464,133 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
     fid[fi] = fi < nM ? s_cf[fi * kTile + t] : 1;
     inner[fi] = fi < nM && abs(fid[fi]) - 1 < a.Nf;
   }
-  // the cell's own state and every stencil state as hi + remainder; all work below is on the
-  // differences to the own state (exact far below their size), face values are stored as
-  // increments over their cell's state
-  const V4<float> wc = s_w[t];
-  const V4<float> wcl = lo_unpack(wc, reinterpret_cast<const uint2*>(sm + L.off_wlo)[t]);
-  const float pc = wc.x, tc = wc.w;
+  const V4<WT> wc = s_w[t];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
   constexpr int U = 8;
-  V4<float> wj[U];  // the first batch of stencil states, gathered before the weights have landed
-  uint2 wjl[U];
+  V4<WT> wj[U];  // the first batch of stencil states, gathered before the weights have landed
 #pragma unroll
   for (int u = 0; u < U; ++u)
-    if (u < nS) {
-      const int j = s_sten[u * kTile + t];
-      wj[u] = a.W[j];
-      wjl[u] = a.Wlo[j];
-    }
+    if (u < nS) wj[u] = a.W[s_sten[u * kTile + t]];
   if (!mbar_wait_bounded(bar + 1, 0)) return give_up();
   // O3 weights of boundary-face and missing slots are zero in the operator rows (setup), so only
   // slots past this mesh's largest cell (a batch may stage fewer rows than NF) are skipped
   const int nfm = a.maxM;
-  float acc[NF][4];  // O3 sums in difference form: sum_{i>0} w_i (phi_i - phi_c)
+  G acc[NF][4];  // O3 sums in difference form, as in recon_reg_body
 #pragma unroll
-  for (int fi = 0; fi < NF; ++fi) acc[fi][0] = acc[fi][1] = acc[fi][2] = acc[fi][3] = 0.f;
-  float gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
-  // extremes of the compact stencil, relative to the cell (the cell itself is 0)
-  float pMax = 0.f, pMin = 0.f, uxMax = 0.f, uxMin = 0.f, uyMax = 0.f, uyMin = 0.f, tMax = 0.f, tMin = 0.f;
-  float pn[NF];  // pressure of the cell across each face, relative to the cell
+  for (int fi = 0; fi < NF; ++fi) acc[fi][0] = acc[fi][1] = acc[fi][2] = acc[fi][3] = G(0);
+  G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
+  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
+  S pn[NF];  // pressure of the cell across each face
 #pragma unroll
-  for (int fi = 0; fi < NF; ++fi) pn[fi] = 0.f;
+  for (int fi = 0; fi < NF; ++fi) pn[fi] = S(0);
   for (int ci0 = 0; ci0 < nS; ci0 += U) {
     if (ci0 > 0) {
 #pragma unroll
       for (int u = 0; u < U; ++u)
-        if (ci0 + u < nS) {
-          const int j = s_sten[(ci0 + u) * kTile + t];
-          wj[u] = a.W[j];
-          wjl[u] = a.Wlo[j];
-        }
+        if (ci0 + u < nS) wj[u] = a.W[s_sten[(ci0 + u) * kTile + t]];
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const int ci = ci0 + u;
       if (ci < nS) {
-        const V4<float> d = state_diff(wc, wcl, wj[u], lo_unpack(wj[u], wjl[u]));
+        const S vx = (S)wj[u].x, vy = (S)wj[u].y, vz = (S)wj[u].z, vw = (S)wj[u].w;
+        const S dp = vx - pc, dux = vy - uxc, duy = vz - uyc, dt = vw - tc;
         if (ci < nM) {  // the face neighbours (compact stencil) come first: reference :148-169, :190-205
-          const V2<float> lm = s_lsm[ci * kTile + t];
-          const float M1 = lm.x, M2 = lm.y;
-          gPx += M1 * d.x;
-          gPy += M2 * d.x;
-          gUxx += M1 * d.y;
-          gUyx += M2 * d.y;
-          gUxy += M1 * d.z;
-          gUyy += M2 * d.z;
-          gTx += M1 * d.w;
-          gTy += M2 * d.w;
-          pMax = fmx(d.x, pMax);
-          pMin = fmn(d.x, pMin);
-          uxMax = fmx(d.y, uxMax);
-          uxMin = fmn(d.y, uxMin);
-          uyMax = fmx(d.z, uyMax);
-          uyMin = fmn(d.z, uyMin);
-          tMax = fmx(d.w, tMax);
-          tMin = fmn(d.w, tMin);
+          const V2<S> lm = s_lsm[ci * kTile + t];
+          const S M1 = lm.x, M2 = lm.y;
+          gPx += M1 * dp;
+          gPy += M2 * dp;
+          gUxx += M1 * dux;
+          gUyx += M2 * dux;
+          gUxy += M1 * duy;
+          gUyy += M2 * duy;
+          gTx += M1 * dt;
+          gTy += M2 * dt;
+          pMax = fmx(vx, pMax);
+          pMin = fmn(vx, pMin);
+          uxMax = fmx(vy, uxMax);
+          uxMin = fmn(vy, uxMin);
+          uyMax = fmx(vz, uyMax);
+          uyMin = fmn(vz, uyMin);
+          tMax = fmx(vw, tMax);
+          tMin = fmn(vw, tMin);
 #pragma unroll
           for (int fi = 0; fi < NF; ++fi)
-            if (fi == ci) pn[fi] = d.x;
+            if (fi == ci) pn[fi] = vx;
         }
 #pragma unroll
         for (int fi = 0; fi < NF; ++fi) {
-          const float wv = fi < nfm ? s_wts[(fi * wrow + ci + 1) * kTile + t] : 0.f;
-          acc[fi][0] += wv * d.x;
-          acc[fi][1] += wv * d.y;
-          acc[fi][2] += wv * d.z;
-          acc[fi][3] += wv * d.w;
+          const S wv = fi < nfm ? s_wts[(fi * wrow + ci + 1) * kTile + t] : S(0);
+          acc[fi][0] += wv * dp;
+          acc[fi][1] += wv * dux;
+          acc[fi][2] += wv * duy;
+          acc[fi][3] += wv * dt;
         }
       }
     }
   }
   a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
   a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
-  mixed_face_values<P, NF>(a, c, fid, inner, acc, pn, pc, tc, gPx, gPy, gUxx, gUyx, gUxy, gUyy, gTx, gTy, pMax,
-                           pMin, uxMax, uxMin, uyMax, uyMin, tMax, tMin,
-                           [&](int fi) { return s_sg[fi * kTile + t]; }, [&](int fi) { return s_sr[fi * kTile + t]; });
+
+  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
+  V4<S> Lm;
+  int8_t flag0;
+  if (fab(tMax - tMin) < VSMALL) {  // reference :208-233
+    Lm = V4<S>{S(1), S(1), S(1), S(1)};
+#pragma unroll
+    for (int fi = 0; fi < NF; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = s_sg[fi * kTile + t];
+      const G dx = d.x, dy = d.y;
+      V4<G> o;
+      o.x = (G)(pc) + gPx * dx + gPy * dy;
+      o.y = (G)(uxc) + gUxx * dx + gUyx * dy;
+      o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
+      o.w = (G)(tc) + gTx * dx + gTy * dy;
+      a.fv[2 * f + isNei] = o;
+    }
+    flag0 = 0;
+  } else {  // reference :235-314
+    S lp = S(2), lux = S(2), luy = S(2), lt = S(2);
+    S smooth = S(0);
+    bool notTrouble = true;
+#pragma unroll
+    for (int fi = 0; fi < NF; ++fi) {
+      if (!inner[fi]) continue;
+      const bool isNei = fid[fi] < 0;
+      const int f = abs(fid[fi]) - 1;
+      const V2<G> d = s_sg[fi * kTile + t];
+      const G dx = d.x, dy = d.y;
+      const V2<S> rf = s_sr[fi * kTile + t];
+      const S deltaR = rf.x, fraction = rf.y;
+      const G pf = (G)pc + acc[fi][0], uxf = (G)uxc + acc[fi][1], uyf = (G)uyc + acc[fi][2], tf = (G)tc + acc[fi][3];
+      S phif;
+      V4<G> o;
+      limiter_process_fast(lp, phif, pc, pMax, pMin, gPx, gPy, dx, dy);
+      o.x = pick<P>(fab(pMax - pMin) >= SMALL, fab(pMax - pMin) < SMALL, pf, phif);
+      notTrouble = phif > S(0);
+      smooth = fmx(smooth, __fdividef(fab((S(1) - fraction) * pc + fraction * pn[fi] - phif), deltaR) +
+                               (pf <= S(0)) * AFAR_LIT(S, 1e20) + (phif <= S(0)) * AFAR_LIT(S, 1e20));
+      limiter_process_fast(lux, phif, uxc, uxMax, uxMin, gUxx, gUyx, dx, dy);
+      o.y = pick<P>(fab(uxMax - uxMin) >= SMALL, fab(uxMax - uxMin) < SMALL, uxf, phif);
+      limiter_process_fast(luy, phif, uyc, uyMax, uyMin, gUxy, gUyy, dx, dy);
+      o.z = pick<P>(fab(uyMax - uyMin) >= SMALL, fab(uyMax - uyMin) < SMALL, uyf, phif);
+      limiter_process_fast(lt, phif, tc, tMax, tMin, gTx, gTy, dx, dy);
+      o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
+      notTrouble = phif > S(0);
+      a.fv[2 * f + isNei] = o;
+    }
+    Lm.x = fmx(lp, S(0)) * notTrouble;
+    Lm.y = fmx(lux, S(0)) * notTrouble;
+    Lm.z = fmx(luy, S(0)) * notTrouble;
+    Lm.w = fmx(lt, S(0)) * notTrouble;
+    smooth = __fdividef(smooth, S(0.5) * (pMax + pMin) * notTrouble + VSMALL);
+    flag0 = (smooth > S(1));
+  }
+  a.lim[c] = Lm;
+  a.si[2 * c] = flag0;
 }
 
 // reconstruct for the FP64-heavy policies (ref, fp64): the stencil values are staged in shared
@@ -737,8 +783,6 @@ __device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
   }
 
   const S tc = (S)a.W[c].w;
-  float tcl = 0.f;  // mixed: the remainder of the cell's temperature
-  if constexpr (P::id == PolicyMixed::id) tcl = lo_unpack(a.W[c], a.Wlo[c]).w;
   const V4<G> g1 = a.grad[2 * c + 1];
   const G gTx = g1.z, gTy = g1.w;
   V4<S> L = a.lim[c];
@@ -758,19 +802,10 @@ __device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
     const V2<G> d = a.sg[fi * ldc + c];
     const G tfOwn = a.fv[2 * f].w;
     const G tfNei = a.fv[2 * f + 1].w;
-    G tfCur = pick<P>(isNei, !isNei, tfNei, tfOwn);
-    G tfOther = pick<P>(!isNei, isNei, tfNei, tfOwn);
+    const G tfCur = pick<P>(isNei, !isNei, tfNei, tfOwn);
+    const G tfOther = pick<P>(!isNei, isNei, tfNei, tfOwn);
     const G lim = to_bj(L.w);
-    G tfTVD = tc + lim * (gTx * d.x + gTy * d.y);
-    if constexpr (P::id == PolicyMixed::id) {
-      // the mixed face values are increments over their own cells: everything relative to this
-      // cell, with the temperature across the face (compact stencil member fi) as hi + remainder
-      const int j = a.sten[fi * ldc + c];
-      const V4<float> wj = a.W[j];
-      const float dT = __fadd_rn(__fadd_rn(wj.w, -tc), __fadd_rn(lo_unpack(wj, a.Wlo[j]).w, -tcl));
-      tfOther += dT;
-      tfTVD = lim * (gTx * d.x + gTy * d.y);
-    }
+    const G tfTVD = tc + lim * (gTx * d.x + gTy * d.y);
     const int typeval = fab(tfTVD - tfOther) < AFAR_LIT(S, 0.5) * fab(tfCur - tfOther);
     const int notFlat = fab(tfCur - tfOther) > AFAR_LIT(S, 1e-10);
     const int limited = (lim < AFAR_LIT(S, 0.9)) + (shockTypeExt > 0);
@@ -909,8 +944,7 @@ template <class D>
 __device__ __forceinline__ void roe_flux_fast(D& rhoFlux, D& rhoUxFlux, D& rhoUyFlux, D& rhoEFlux, const D rhoL,
                                               const D rhoR, const D uxL, const D uxR, const D uyL, const D uyR,
                                               const D tL, const D tR, const D deltaP, const D deltaRho, const D R,
-                                              const D Cv, const D gamma, const D magSf, const D nfx, const D nfy,
-                                              const D dUx, const D dUy) {
+                                              const D Cv, const D gamma, const D magSf, const D nfx, const D nfy) {
   const D cvL = uxL * nfx + uyL * nfy;
   const D cvR = uxR * nfx + uyR * nfy;
   const D kL = D(0.5) * (uxL * uxL + uyL * uyL), kR = D(0.5) * (uxR * uxR + uyR * uyR);
@@ -928,6 +962,8 @@ __device__ __forceinline__ void roe_flux_fast(D& rhoFlux, D& rhoUxFlux, D& rhoUy
   const D cT = sqr_(fmx((gamma - D(1)) * (hT - D(0.5) * q2), tiny));
   const D ic2 = fdiv(D(1), cT * cT);
   const D cvT = uxT * nfx + uyT * nfy;
+  const D dUx = uxR - uxL;
+  const D dUy = uyR - uyL;
   const D dCv = dUx * nfx + dUy * nfy;
   const D r1 = (deltaP - rhoT * cT * dCv) * (D(0.5) * ic2);
   const D r2 = deltaRho - deltaP * ic2;
@@ -1104,174 +1140,8 @@ __global__ void __launch_bounds__(128) k_flux_ref_layout(RFlux* __restrict__ Flu
 // boundary face (ids Nf..Nf+Nb-1; the reference's grid covers boundary faces b < 128*ceil(Nf/128)
 // only, which holds on every mesh with Nf >= Nb).  DT: also reduce the CFL step of the reference's
 // setDeltaT (cudaFieldOperation.h:124-180) from the state at the start of the step.
-// ---------------------------------------------------------------- mixed face flux, delta form
-// The mixed policy's face flux is stored relative to each side's own Euler flux: flux[f] = F_f -
-// F(W_own).Sf and fluxB[f] = F_f - F(W_nei).Sf, so the residual of a cell is the sum of its faces'
-// deltas (its own flux integrates to zero over a closed cell: sum_f Sf = 0).  Every quantity is
-// formed from differences to the owner's state -- face-value increments, the neighbour's state
-// difference (hi + remainder) -- and every product of the reference's central flux
-// (cudaRiemannSolver.h:190-232) is expanded around the owner, so FP32 rounds the small deltas, not
-// the O(1) fluxes whose differences make the residual.
-struct MixedRef {
-  float p, u, v, T, rho, q, m, e;  // the owner's state, density, u.Sf, rho u.Sf, Cp T + |u|^2/2
-};
-__device__ __forceinline__ MixedRef mixed_ref(const V4<float> w, const float Sx, const float Sy, const float iR,
-                                              const float Cp) {
-  MixedRef o;
-  o.p = w.x;
-  o.u = w.y;
-  o.v = w.z;
-  o.T = w.w;
-  o.rho = __fdividef(w.x * iR, w.w);
-  o.q = w.y * Sx + w.z * Sy;
-  o.m = o.rho * o.q;
-  o.e = Cp * w.w + 0.5f * (w.y * w.y + w.z * w.z);
-  return o;
-}
-// rho(o + d) - rho(o) = (dp - rho_o R dT) / (R (T_o + dT)).
-__device__ __forceinline__ float mixed_drho(const MixedRef& o, const V4<float> d, const float R, const float iR) {
-  return __fdividef((d.x - o.rho * R * d.w) * iR, o.T + d.w);
-}
-struct MixedSide {
-  float drho, dm, de;  // density, mass flux rho u.Sf and Cp T + |u|^2/2 of o + d, minus o's
-};
-__device__ __forceinline__ MixedSide mixed_side(const MixedRef& o, const V4<float> d, const float Sx, const float Sy,
-                                                const float R, const float iR, const float Cp) {
-  MixedSide s;
-  s.drho = mixed_drho(o, d, R, iR);
-  const float dq = d.y * Sx + d.z * Sy;
-  s.dm = s.drho * o.q + o.rho * dq + s.drho * dq;
-  s.de = Cp * d.w + o.u * d.y + o.v * d.z + 0.5f * (d.y * d.y + d.z * d.z);
-  return s;
-}
-// The central flux of sides o + dL, o + dR minus F(o).Sf: rhoFlux = (mL + mR)/2, momentum rhoFlux
-// times the mean velocity plus the mean pressure times Sf, energy rhoFlux times the mean of
-// Cp T + |u|^2/2 (p/rho = R T).
-__device__ __forceinline__ V4<float> mixed_central(const MixedRef& o, const V4<float> dL, const V4<float> dR,
-                                                   const MixedSide& sL, const MixedSide& sR, const float Sx,
-                                                   const float Sy) {
-  const float dF1 = 0.5f * (sL.dm + sR.dm);
-  const float du = 0.5f * (dL.y + dR.y), dv = 0.5f * (dL.z + dR.z), dp = 0.5f * (dL.x + dR.x);
-  const float de = 0.5f * (sL.de + sR.de);
-  return V4<float>{dF1, dF1 * o.u + o.m * du + dF1 * du + dp * Sx, dF1 * o.v + o.m * dv + dF1 * dv + dp * Sy,
-                   dF1 * o.e + o.m * de + dF1 * de};
-}
-__device__ __forceinline__ V4<float> v4_add(const V4<float> a, const V4<float> b) {
-  return V4<float>{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w};
-}
-
-template <bool DT>
-__device__ __forceinline__ void flux_mixed(const StageArgs<PolicyMixed>& a, const int blk) {
-  const int id = blk * blockDim.x + threadIdx.x;
-  __shared__ float s_cfl;
-  __shared__ int s_cfl_step;
-  if constexpr (DT) {  // the Courant step in FP32 from block constants read once by thread 0
-    if (threadIdx.x == 0) {
-      s_cfl_step = !(a.ctl->dt_fixed > 0.0);
-      s_cfl = (float)a.ctl->cfl;
-    }
-    __syncthreads();
-  }
-  float dtf32 = 1e5f;
-  const float R = a.Rf, Cv = a.Cvf, iR = a.invRf, gam = a.gm1f + 1.f, Cp = a.Cvf + a.Rf;
-  if (id < a.Nf) {
-    const int2 on = a.on[id];
-    const int own = on.x, nei = on.y;
-    const V4<float> fd = a.fd[id];
-    const float dxL = fd.x, dyL = fd.y, dxR = fd.z, dyR = fd.w;
-    const int8_t sL = a.si[2 * own + 1], sR = a.si[2 * nei + 1];
-    const bool tvdL = sL != 0, tvdR = sR != 0;
-    const bool isShock = sL < 0 || sR < 0;
-    const V4<float> fs = a.fs[id];
-    const float Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
-    const V4<float> Wo = a.W[own], Wn = a.W[nei];
-    const V4<float> dn = state_diff(Wo, lo_unpack(Wo, a.Wlo[own]), Wn, lo_unpack(Wn, a.Wlo[nei]));  // W_n - W_o
-    const V4<float> go0 = a.grad[2 * own], go1 = a.grad[2 * own + 1];
-    const V4<float> gn0 = a.grad[2 * nei], gn1 = a.grad[2 * nei + 1];
-    const V4<float> lo = a.lim[own], ln = a.lim[nei];
-    const V4<float> fo = a.fv[2 * id], fn = a.fv[2 * id + 1];  // increments over own and neighbour
-    // both sides relative to the owner: TVD (limited linear) and selected (O3 or TVD)
-    const V4<float> dLT{lo.x * (go0.x * dxL + go0.y * dyL), lo.y * (go0.z * dxL + go1.x * dyL),
-                        lo.z * (go0.w * dxL + go1.y * dyL), lo.w * (go1.z * dxL + go1.w * dyL)};
-    const V4<float> dRT = v4_add(dn, V4<float>{ln.x * (gn0.x * dxR + gn0.y * dyR), ln.y * (gn0.z * dxR + gn1.x * dyR),
-                                              ln.z * (gn0.w * dxR + gn1.y * dyR), ln.w * (gn1.z * dxR + gn1.w * dyR)});
-    const V4<float> dL = tvdL ? dLT : fo;
-    const V4<float> dR = tvdR ? dRT : v4_add(dn, fn);
-    const MixedRef o = mixed_ref(Wo, Sfx, Sfy, iR, Cp);
-    const MixedSide mL = mixed_side(o, dL, Sfx, Sfy, R, iR, Cp), mR = mixed_side(o, dR, Sfx, Sfy, R, iR, Cp);
-    V4<float> A = mixed_central(o, dL, dR, mL, mR, Sfx, Sfy);
-    const float rhoL = o.rho + mL.drho, rhoR = o.rho + mR.drho;
-    const float pL = Wo.x + dL.x, uxL = Wo.y + dL.y, uyL = Wo.z + dL.z, tL = Wo.w + dL.w;
-    const float pR = Wo.x + dR.x, uxR = Wo.y + dR.y, uyR = Wo.z + dR.z, tR = Wo.w + dR.w;
-    const float nfx = Sfx * fs.w, nfy = Sfy * fs.w;  // fs.w = 1/|Sf| (setup)
-    if (isShock) {  // KFVS on the absolute states (shock faces: nothing small to keep)
-      float rhoFlux = 0.5f * rhoL * (uxL * Sfx + uyL * Sfy) + 0.5f * rhoR * (uxR * Sfx + uyR * Sfy);
-      float rhoUxFlux = 0.5f * (rhoFlux * uxL + pL * Sfx) + 0.5f * (rhoFlux * uxR + pR * Sfx);
-      float rhoUyFlux = 0.5f * (rhoFlux * uyL + pL * Sfy) + 0.5f * (rhoFlux * uyR + pR * Sfy);
-      float rhoEFlux = 0.5f * rhoFlux * (Cv * tL + 0.5f * (uxL * uxL + uyL * uyL) + R * tL) +
-                       0.5f * rhoFlux * (Cv * tR + 0.5f * (uxR * uxR + uyR * uyR) + R * tR);
-      kfvs_flux_fast<float>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoL, rhoR, pL, pR, uxL, uxR, uyL, uyR, tL, tR,
-                            R, Cv, 2.f * Cv * iR - 2.f, magSf, nfx, nfy);
-      A = V4<float>{rhoFlux - o.m, rhoUxFlux - (o.m * o.u + o.p * Sfx), rhoUyFlux - (o.m * o.v + o.p * Sfy),
-                    rhoEFlux - o.m * o.e};
-    } else {  // Roe dissipation; its jumps from the deltas
-      const float dP = min_delta<float, float>(dL.x, dR.x, dLT.x, dRT.x);
-      const float dRho = min_delta<float, float>(mL.drho, mR.drho, mixed_drho(o, dLT, R, iR),
-                                                 mixed_drho(o, dRT, R, iR));
-      roe_flux_fast<float>(A.x, A.y, A.z, A.w, rhoL, rhoR, uxL, uxR, uyL, uyR, tL, tR, dP, dRho, R, Cv, gam, magSf,
-                           nfx, nfy, dR.y - dL.y, dR.z - dL.z);
-    }
-    // the neighbour's delta: F_f - F(W_n).Sf = A - (F(W_n) - F(W_o)).Sf
-    const MixedSide mn = mixed_side(o, dn, Sfx, Sfy, R, iR, Cp);
-    const V4<float> dFn = mixed_central(o, dn, dn, mn, mn, Sfx, Sfy);
-    a.flux[id] = A;
-    a.fluxB[id] = V4<float>{A.x - dFn.x, A.y - dFn.y, A.z - dFn.z, A.w - dFn.w};
-    if constexpr (DT) {
-      if (s_cfl_step) {  // setDeltaT, cudaFieldOperation.h:140-157, as an FP32 estimate
-        const V2<float> g = a.dtgf[id];
-        const float deltaR = g.x, fraction = g.y;
-        dtf32 = s_cfl * deltaR * magSf /
-                ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
-                 sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
-      }
-    }
-  } else if (id < a.Nf + a.Nb) {  // boundary faces (reference :254-270): F(W_ghost).Sf - F(W_own).Sf
-    const int b = id - a.Nf;
-    const int own = a.bnei[b];
-    const V4<float> Wo = a.W[own], Wg = a.W[a.Nc + b];
-    const V4<float> dg = state_diff(Wo, lo_unpack(Wo, a.Wlo[own]), Wg, lo_unpack(Wg, a.Wlo[a.Nc + b]));
-    const V4<float> fs = a.fs[id];
-    const MixedRef o = mixed_ref(Wo, fs.x, fs.y, iR, Cp);
-    const MixedSide mg = mixed_side(o, dg, fs.x, fs.y, R, iR, Cp);
-    a.flux[id] = mixed_central(o, dg, dg, mg, mg, fs.x, fs.y);
-  }
-  if constexpr (DT) {
-    // block min of the float estimates on their bit patterns (non-negative floats order like
-    // them; NaN sorts above +inf), then one atomicMin per block on the double's bits
-    unsigned v = (unsigned)__float_as_int(dtf32);
-    if (!(dtf32 >= 0.f)) v = 0x7F800000u;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned u = __shfl_xor_sync(0xffffffffu, v, o);
-      v = u < v ? u : v;
-    }
-    __shared__ unsigned wmin32[8];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) wmin32[warp] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      unsigned m = wmin32[0];
-      for (int k = 1; k < (int)(blockDim.x >> 5); ++k) m = wmin32[k] < m ? wmin32[k] : m;
-      const float mf = __int_as_float((int)m);
-      const unsigned long long bits =
-          m >= 0x7F800000u ? 0x7FF0000000000000ull : (unsigned long long)__double_as_longlong((double)mf);
-      atomicMin(&a.ctl->dt_bits, bits);
-    }
-  }
-}
-
 template <class P, bool DT>
-__device__ __forceinline__ void flux_body_fp(const StageArgs<P>& a, const int blk) {
+__device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) {
   using S = typename P::S;
   using G = typename P::G;
   using D = typename P::D;
@@ -1358,7 +1228,7 @@ __device__ __forceinline__ void flux_body_fp(const StageArgs<P>& a, const int bl
                         tRf, R, Cv, G(2) * Cv * iR - G(2), magSf, nfx, nfy);
     else
       roe_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, uxLf, uxRf, uyLf, uyRf, tLf, tRf, dP,
-                       dRho, R, Cv, gam, magSf, nfx, nfy, uxRf - uxLf, uyRf - uyLf);
+                       dRho, R, Cv, gam, magSf, nfx, nfy);
     a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)rhoUxFlux, (typename P::F)rhoUyFlux,
                                    (typename P::F)rhoEFlux};
     if constexpr (DT && kF32) {
@@ -1446,15 +1316,6 @@ __device__ __forceinline__ void flux_body_fp(const StageArgs<P>& a, const int bl
   }
 }
 
-// The face flux of a stage: the mixed policy's delta form, else the reference's form.
-template <class P, bool DT>
-__device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) {
-  if constexpr (P::id == PolicyMixed::id)
-    flux_mixed<DT>(a, blk);
-  else
-    flux_body_fp<P, DT>(a, blk);
-}
-
 // Ghost state of boundary face b from its owner's state (reference cudaEulerBCs.h:45-95 and
 // BCs/2D/<label>.h:4-10).
 __device__ __forceinline__ V4<double> boundary_value(const int type, const V4<double> w, const V2<double> n) {
@@ -1500,9 +1361,9 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
     int fid[MB];
 #pragma unroll
     for (int u = 0; u < MB; ++u) fid[u] = (f0 + u < nM) ? a.cf[(f0 + u) * ldc + c] : 1;
-    V4<float> fl[MB];  // this side's delta: the owner's (flux) or the neighbour's (fluxB)
+    V4<float> fl[MB];
 #pragma unroll
-    for (int u = 0; u < MB; ++u) fl[u] = fid[u] > 0 ? a.flux[fid[u] - 1] : a.fluxB[-fid[u] - 1];
+    for (int u = 0; u < MB; ++u) fl[u] = reinterpret_cast<const V4<float>*>(a.flux)[abs(fid[u]) - 1];
 #pragma unroll
     for (int u = 0; u < MB; ++u) {
       if (f0 + u < nM) {
@@ -1543,26 +1404,17 @@ __device__ __forceinline__ void update_mixed(const StageArgs<P>& a, const int c,
   irf = __fmaf_rn(irf, __fmaf_rn(-un[0].hi, irf, 1.f), irf);
   const DF ke2 = df_div(df_add(df_sqr(un[1]), df_sqr(un[2])), un[0], irf);  // |rhoU|^2 / rho
   const DF e = df_add(un[3], DF{-0.5f * ke2.hi, -0.5f * ke2.lo});
-  // the primitive state as float pairs -- p = (gamma - 1) e, u = rhoU / rho, T = p / (rho R) --
-  // stored as hi and the packed remainder
-  const DF p = df_mul(DF{a.gm1f, a.gm1lo}, e);
-  const DF ux = df_div(un[1], un[0], irf), uy = df_div(un[2], un[0], irf);
-  const DF T = df_mul(df_div(p, un[0], irf), DF{a.invRf, a.invRlo});
-  const V4<float> wn{p.hi, ux.hi, uy.hi, T.hi};
-  a.W[c] = wn;
-  a.Wlo[c] = lo_pack(wn, V4<float>{p.lo, ux.lo, uy.lo, T.lo});
+  const float pf = a.gm1f * __fadd_rn(e.hi, e.lo);
+  const V4<float> wn{pf, un[1].hi * irf, un[2].hi * irf, pf * irf * a.invRf};
+  reinterpret_cast<V4<float>*>(a.W)[c] = wn;
   for (int fi = 0; fi < nM; ++fi) {
     const int f = abs(a.cf[fi * ldc + c]) - 1;
     if (f < a.Nf) continue;
     const int b = f - a.Nf;
     if (a.btype[b] == AFAR_BC_FIXED_INITIAL) continue;  // the ghost keeps its uploaded state
-    const V4<double> g = boundary_value(
-        a.btype[b],
-        V4<double>{(double)p.hi + p.lo, (double)ux.hi + ux.lo, (double)uy.hi + uy.lo, (double)T.hi + T.lo}, a.bn[b]);
-    const V4<float> gh{(float)g.x, (float)g.y, (float)g.z, (float)g.w};
-    a.W[a.Nc + b] = gh;
-    a.Wlo[a.Nc + b] = lo_pack(gh, V4<float>{(float)(g.x - (double)gh.x), (float)(g.y - (double)gh.y),
-                                            (float)(g.z - (double)gh.z), (float)(g.w - (double)gh.w)});
+    const V4<double> g = boundary_value(a.btype[b], V4<double>{(double)wn.x, (double)wn.y, (double)wn.z, (double)wn.w},
+                                        a.bn[b]);
+    reinterpret_cast<V4<float>*>(a.W)[a.Nc + b] = V4<float>{(float)g.x, (float)g.y, (float)g.z, (float)g.w};
   }
 }
 

@@ -16,7 +16,6 @@
 // FMA-contraction decisions; that is what makes the 1e-12 / identical-switch parity possible.
 #pragma once
 
-#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -189,41 +188,6 @@ __device__ __forceinline__ DF df_div(const DF a, const DF b, const float r) {
   const DF qb = df_mul(DF{q0, 0.f}, b);
   const DF rem = df_add(a, DF{-qb.hi, -qb.lo});
   return df_fast_two_sum(q0, __fmul_rn(__fadd_rn(rem.hi, rem.lo), r));
-}
-
-// The mixed policy's primitive state: a float hi and its rounding remainder lo (|lo| <= ulp(hi)/2,
-// from the float-pair conserved state), lo stored as lo/hi * 2^24 in half precision -- 8 bytes per
-// cell that carry the state to about 35 bits.  Differences between neighbouring states (the inputs
-// of the reconstruction, the BVD test and the face fluxes) are then exact to far below their own
-// size, where float states alone would round them at the states' size.
-__device__ __forceinline__ float lo_one(const unsigned short e, const float hi) {
-  return __half2float(__ushort_as_half(e)) * hi * 0x1p-24f;
-}
-// The code of lo, kept so that the decoded remainder stays strictly below half an ulp of hi: then
-// hi + remainder, taken as a double, rounds back to hi, and a state written out as doubles and read
-// back is the same pair (checkpoints resume bitwise).
-__device__ __forceinline__ unsigned short lo_half(const float lo, const float hi) {
-  if (hi == 0.f) return 0;
-  unsigned short e = __half_as_ushort(__float2half_rn(__fdividef(lo, hi) * 0x1p24f));
-  const float a = fabsf(hi);
-  if (fabsf(lo_one(e, hi)) >= 0.5f * (nextafterf(a, INFINITY) - a) && (e & 0x7fffu)) e = (unsigned short)(e - 1u);
-  return e;
-}
-__device__ __forceinline__ uint2 lo_pack(const V4<float> hi, const V4<float> lo) {
-  return make_uint2((unsigned)lo_half(lo.x, hi.x) | ((unsigned)lo_half(lo.y, hi.y) << 16),
-                    (unsigned)lo_half(lo.z, hi.z) | ((unsigned)lo_half(lo.w, hi.w) << 16));
-}
-__device__ __forceinline__ V4<float> lo_unpack(const V4<float> hi, const uint2 e) {
-  return V4<float>{lo_one((unsigned short)(e.x & 0xffffu), hi.x), lo_one((unsigned short)(e.x >> 16), hi.y),
-                   lo_one((unsigned short)(e.y & 0xffffu), hi.z), lo_one((unsigned short)(e.y >> 16), hi.w)};
-}
-// (b_hi + b_lo) - (a_hi + a_lo): the hi difference is exact for nearby values (Sterbenz).
-__device__ __forceinline__ V4<float> state_diff(const V4<float> ah, const V4<float> al, const V4<float> bh,
-                                                const V4<float> bl) {
-  return V4<float>{__fadd_rn(__fadd_rn(bh.x, -ah.x), __fadd_rn(bl.x, -al.x)),
-                   __fadd_rn(__fadd_rn(bh.y, -ah.y), __fadd_rn(bl.y, -al.y)),
-                   __fadd_rn(__fadd_rn(bh.z, -ah.z), __fadd_rn(bl.z, -al.z)),
-                   __fadd_rn(__fadd_rn(bh.w, -ah.w), __fadd_rn(bl.w, -al.w))};
 }
 
 }  // namespace afar

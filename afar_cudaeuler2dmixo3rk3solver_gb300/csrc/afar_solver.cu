@@ -140,25 +140,6 @@ __global__ void k_df_to_double(int n, const DF4* in, V4<double>* out) {
                       (double)d.hi.z + (double)d.lo.z, (double)d.hi.w + (double)d.lo.w};
 }
 
-// The mixed policy's primitive state: double -> float hi + packed remainder, and back.
-__global__ void k_w_from_double(int n, const V4<double>* in, V4<float>* hi, uint2* lo) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const V4<double> v = in[i];
-  const V4<float> h{(float)v.x, (float)v.y, (float)v.z, (float)v.w};
-  hi[i] = h;
-  lo[i] = lo_pack(h, V4<float>{(float)(v.x - (double)h.x), (float)(v.y - (double)h.y), (float)(v.z - (double)h.z),
-                               (float)(v.w - (double)h.w)});
-}
-__global__ void k_w_to_double(int n, const V4<float>* hi, const uint2* lo, V4<double>* out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const V4<float> h = hi[i];
-  const V4<float> l = lo_unpack(h, lo[i]);
-  out[i] = V4<double>{(double)h.x + (double)l.x, (double)h.y + (double)l.y, (double)h.z + (double)l.z,
-                      (double)h.w + (double)l.w};
-}
-
 template <class A, class B>
 __global__ void k_convert2(int n, const V2<A>* in, V2<B>* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -234,7 +215,6 @@ struct afar_solver {
   unsigned long long* dt_bits = nullptr;
   // policy-typed device arrays (element size depends on the policy)
   void* W = nullptr;
-  void* fluxB = nullptr;   // mixed: the face flux relative to the neighbour's own flux
   void* fd = nullptr;
   void* fs = nullptr;
   void* lsm = nullptr;
@@ -296,10 +276,6 @@ StageArgs<P> make_args(afar_solver* s) {
   a.sr = static_cast<const V2<S>*>(s->sr);
   a.wts = static_cast<const S*>(s->wts);
   a.W = static_cast<V4<typename P::W>*>(s->W);
-  a.Wlo = P::id == PolicyMixed::id ? reinterpret_cast<uint2*>(static_cast<V4<float>*>(s->W) + (s->Nc + s->Nb))
-                                   : nullptr;
-  a.fluxB = static_cast<V4<typename P::F>*>(s->fluxB);
-  a.bnei = s->bnei;
   a.U = s->U;
   a.U0 = s->U0;
   a.grad = static_cast<V4<G>*>(s->grad);
@@ -316,8 +292,6 @@ StageArgs<P> make_args(afar_solver* s) {
   a.gamma = s->Cv > 0.0 ? s->R / s->Cv + 1.0 : 0.0;
   a.gm1f = (float)(a.gamma - 1.0);
   a.invRf = (float)a.invR;
-  a.gm1lo = (float)((a.gamma - 1.0) - (double)a.gm1f);
-  a.invRlo = (float)(a.invR - (double)a.invRf);
   a.vinvf = s->vinvf;
   a.Rf = (float)s->R;
   a.Cvf = (float)s->Cv;
@@ -585,11 +559,7 @@ afar_status check_device_error(afar_solver* s) {
   return AFAR_OK;
 }
 
-// Bytes of the primitive-state array W for n cells and ghosts: mixed holds float hi parts, then the
-// packed remainders (8 bytes each, two spare so a bulk copy of an odd tile stays in bounds).
-size_t w_bytes(int policy, size_t n) {
-  return policy == AFAR_POLICY_MIXED ? sizeof(V4<float>) * n + sizeof(uint2) * (n + 2) : sizeof(V4<double>) * n;
-}
+size_t w_size(int policy) { return policy == AFAR_POLICY_MIXED ? sizeof(V4<float>) : sizeof(V4<double>); }
 
 }  // namespace
 
@@ -629,9 +599,8 @@ static afar_status put_state(afar_solver* s, const afar_basicFieldData* FD, cons
   if (FD) {
     if (mixed) {
       AFAR_CUDA(cudaMemcpyAsync(s->xfer, FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
-      k_w_from_double<<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>(
-          (int)(Nc + Nb), static_cast<const V4<double>*>(s->xfer), static_cast<V4<float>*>(s->W),
-          reinterpret_cast<uint2*>(static_cast<V4<float>*>(s->W) + (Nc + Nb)));
+      k_convert4<double, float><<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>(
+          (int)(Nc + Nb), static_cast<const V4<double>*>(s->xfer), static_cast<V4<float>*>(s->W));
     } else {
       AFAR_CUDA(cudaMemcpyAsync(s->W, FD, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
     }
@@ -653,10 +622,8 @@ static afar_status get_state(afar_solver* s, afar_basicFieldData* FD, afar_conse
   const bool mixed = s->policy == AFAR_POLICY_MIXED;
   if (FD) {
     if (mixed) {
-      k_w_to_double<<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>(
-          (int)(Nc + Nb), static_cast<const V4<float>*>(s->W),
-          reinterpret_cast<const uint2*>(static_cast<const V4<float>*>(s->W) + (Nc + Nb)),
-          static_cast<V4<double>*>(s->xfer));
+      k_convert4<float, double><<<grid_for(Nc + Nb, 256), 256, 0, s->stream>>>(
+          (int)(Nc + Nb), static_cast<const V4<float>*>(s->W), static_cast<V4<double>*>(s->xfer));
       AFAR_CUDA(cudaMemcpyAsync(FD, s->xfer, sizeof(V4<double>) * (Nc + Nb), cudaMemcpyDeviceToHost, s->stream));
       AFAR_CUDA(cudaStreamSynchronize(s->stream));  // xfer is reused below
     } else {
@@ -786,8 +753,7 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   if ((st = dalloc_t(s, &s->si, 2 * (Nc + Nb)))) return st;
   if ((st = dalloc_t(s, &s->ctl, 1))) return st;
   if ((st = dalloc_t(s, &s->dt_bits, 1))) return st;
-  if ((st = dalloc(s, &s->W, w_bytes(s->policy, Nc + Nb)))) return st;
-  AFAR_CUDA(cudaMemsetAsync(s->W, 0, w_bytes(s->policy, Nc + Nb), s->stream));
+  if ((st = dalloc(s, &s->W, w_size(s->policy) * (Nc + Nb)))) return st;
   AFAR_CUDA(cudaMemcpyAsync(s->cellC, h->CELL, sizeof(V2<double>) * (Nc + Nb), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->faceRaw, h->FACE, sizeof(FaceRaw) * (Nf + Nb), cudaMemcpyHostToDevice, s->stream));
   AFAR_CUDA(cudaMemcpyAsync(s->vol, h->cellVolume, sizeof(double) * Nc, cudaMemcpyHostToDevice, s->stream));
@@ -805,7 +771,6 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   if ((st = dalloc(s, &s->lim, l * Nc))) return st;
   if ((st = dalloc(s, &s->fv, g * 2 * Nf))) return st;
   if ((st = dalloc(s, &s->flux, g * (Nf + Nb)))) return st;
-  if (s->policy == AFAR_POLICY_MIXED && (st = dalloc(s, &s->fluxB, g * (Nf > 0 ? Nf : 1)))) return st;
   if ((st = dalloc_t(s, &s->dtg, Nf))) return st;
   if ((st = dalloc_t(s, &s->bn, Nb))) return st;
   AFAR_CUDA(cudaMemsetAsync(s->fv, 0, g * 2 * Nf, s->stream));
@@ -1336,7 +1301,7 @@ extern "C" afar_status afar_state_snapshot(afar_solver* s, int op) {
   if (op != AFAR_SNAPSHOT_SAVE && op != AFAR_SNAPSHOT_RESTORE) return (set_error("unknown snapshot op %d", op), AFAR_ERR_ARGUMENT);
   if (op == AFAR_SNAPSHOT_RESTORE) s->head_pending = false;
   AFAR_CUDA(cudaSetDevice(s->device));
-  const size_t wb = w_bytes(s->policy, (size_t)(s->Nc + s->Nb));
+  const size_t wb = w_size(s->policy) * (size_t)(s->Nc + s->Nb);
   const size_t ub = sizeof(V4<double>) * (size_t)s->Nc;
   if (op == AFAR_SNAPSHOT_SAVE && !s->snap) {
     afar_status st = dalloc(s, &s->snap, wb + 2 * ub + sizeof(StepCtl));

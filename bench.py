@@ -210,8 +210,8 @@ def algorithmic_bytes_per_step(hf, policy: str) -> float:
               + sum_internal_faces [40 + 8 + (S_own + 1 + S_nei + 1) wO]
               + sum_boundary_faces [40 + 4 + 1 + 4 wW]
       B_step  = 3 B_stage + Nc (4 wW + 16) + 48 Nf
-    wW = bytes per primitive word (8 ref/fp64, 6 mixed: float + half remainder); wO = operator word (4 ref/mixed, 8 fp64)."""
-    wW = 6 if policy == "mixed" else 8  # mixed: float hi + half-precision remainder
+    wW = bytes per primitive word (8 ref/fp64, 4 mixed); wO = operator word (4 ref/mixed, 8 fp64)."""
+    wW = 4 if policy == "mixed" else 8
     wO = 8 if policy == "fp64" else 4
     S = hf.stencilSize.astype(np.float64)
     m = hf.compactStencilSize.astype(np.float64)
@@ -229,7 +229,7 @@ def reconstruct_bytes_per_launch(hf, policy: str) -> float:
                 (4 wS), troubled flag out (1)
       per internal face: O3 weights of both sides ((S_own+1 + S_nei+1) wO), face values out (8 wG)
     wG = gradient/face-value word, wS = limiter word (4 for mixed, else 8 and 4/8)."""
-    wW = 6 if policy == "mixed" else 8  # mixed: float hi + half-precision remainder
+    wW = 4 if policy == "mixed" else 8
     wO = 8 if policy == "fp64" else 4
     wG = 4 if policy == "mixed" else 8
     wS = 8 if policy == "fp64" else 4
