@@ -609,6 +609,10 @@ static afar_status put_state(afar_solver* s, const afar_basicFieldData* FD, cons
   V4<double>* dst[2] = {s->U, s->U0};
   for (int i = 0; i < 2; ++i) {
     if (!src[i]) continue;
+    if (i == 1 && cFDold == cFD) {  // the same host array twice: one upload, then a device copy
+      AFAR_CUDA(cudaMemcpyAsync(s->U0, s->U, sizeof(V4<double>) * Nc, cudaMemcpyDeviceToDevice, s->stream));
+      continue;
+    }
     AFAR_CUDA(cudaMemcpyAsync(dst[i], src[i], sizeof(V4<double>) * Nc, cudaMemcpyHostToDevice, s->stream));
     if (mixed) k_df_from_double<<<grid_for(Nc, 256), 256, 0, s->stream>>>((int)Nc, dst[i]);
   }

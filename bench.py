@@ -403,7 +403,7 @@ def run_ours(args, dist: Dist):
         check(L.afar_copyFieldDataDeviceToHost(C.byref(fp), s.h, hf.nc, hf.nb))
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_finite = bool(np.isfinite(out_FD).all() and (out_FD[:hf.nc, 0] > 0).all())
-    h2d = (FD_h.nbytes + 2 * cFD_h.nbytes) * len(chunks) / K + 24
+    h2d = (FD_h.nbytes + cFD_h.nbytes) * len(chunks) / K + 24  # cFDold is cFD: copied on the device
     d2h = (out_FD.nbytes + out_si.nbytes) * len(chunks) / K + 8
 
     cpu = None
