@@ -65,7 +65,7 @@ class ServerStats(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("submitted", "completed", "failed", "queued", "running",
                                              "peakRunning")] + [
         ("bytesInUse", C.c_size_t), ("peakBytes", C.c_size_t), ("budgetBytes", C.c_size_t),
-        ("batchSteps", C.c_longlong)]
+        ("batchSteps", C.c_longlong), ("cancelled", C.c_longlong)]
 
 
 class AfarError(RuntimeError):
@@ -132,6 +132,8 @@ def lib():
                                      C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
             "afar_server_get_stats": (S, [_p, C.POINTER(ServerStats)]),
             "afar_server_destroy": (S, [_p]),
+            "afar_server_cancel": (S, [_p, C.c_longlong]),
+            "afar_switch_counts": (S, [_p, C.POINTER(C.c_longlong)]),
             "afar_batch_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),
             "afar_batch_add": (S, [_p, _p]),
             "afar_batch_remove": (S, [_p, _p]),
@@ -171,5 +173,5 @@ EXPORTED = [
     "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc", "afar_set_step_params",
     "afar_set_write_interval", "afar_set_periodic", "afar_set_tuning", "afar_get_tuning", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
     "afar_batch_destroy", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
-    "afar_server_destroy",
+    "afar_server_destroy", "afar_server_cancel", "afar_switch_counts",
 ]

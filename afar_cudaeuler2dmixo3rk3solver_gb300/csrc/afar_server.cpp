@@ -34,6 +34,7 @@ struct Request {
   size_t bytes = 0;
   long long steps0 = 0;
   long long steps_done = 0;
+  bool cancel = false;  // set by afar_server_cancel while running: retired at the next chunk boundary
 };
 
 // Device memory of a solve before it is built: a per-cell, per-face model of the allocations
@@ -105,10 +106,14 @@ struct afar_server {
 
   void finish(Request* r) {
     std::lock_guard<std::mutex> lock(mu);
+    finish_locked(r);
+  }
+  void finish_locked(Request* r) {
     r->done = true;
     r->t_done = Clock::now();
     if (r->status == AFAR_OK) st.completed++;
     else st.failed++;
+    if (r->status == AFAR_ERR_CANCELLED) st.cancelled++;
     cv_done.notify_all();
   }
 
@@ -167,7 +172,16 @@ struct afar_server {
         double t = 0.0, dt = 0.0;
         long long steps = 0;
         bool fin = false;
-        if (e) {
+        bool cancelled;
+        {
+          std::lock_guard<std::mutex> lock(mu);
+          cancelled = r->cancel;
+        }
+        if (cancelled) {
+          r->status = AFAR_ERR_CANCELLED;
+          r->message = "the request was cancelled";
+          fin = true;
+        } else if (e) {
           fail(r, e, "batch run");
           fin = true;
         } else if ((e = afar_get_time(r->solver, &t, &dt, &steps))) {
@@ -285,6 +299,26 @@ extern "C" afar_status afar_server_wait(afar_server* s, long long id, double tim
     if (steps) *steps = r->steps_done;
     if (r->status != AFAR_OK) set_error("%s", r->message.c_str());
   }
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_server_cancel(afar_server* s, long long id) {
+  using afar::set_error;
+  if (!s) return (set_error("afar_server_cancel: null server"), AFAR_ERR_ARGUMENT);
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->all.find(id);
+  if (it == s->all.end()) return (set_error("afar_server_cancel: unknown request id"), AFAR_ERR_ARGUMENT);
+  Request* r = it->second;
+  if (r->done) return (set_error("afar_server_cancel: the request has finished"), AFAR_ERR_STATE);
+  for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+    if (*q == r) {  // not admitted yet: it never touches the GPU
+      s->queue.erase(q);
+      r->status = AFAR_ERR_CANCELLED;
+      r->message = "the request was cancelled";
+      s->finish_locked(r);
+      return AFAR_OK;
+    }
+  r->cancel = true;  // being built or running: the worker retires it after its current chunk
   return AFAR_OK;
 }
 

@@ -1357,6 +1357,47 @@ extern "C" afar_status afar_download_ls_matrix(afar_solver* s, float* matrix) {
   return AFAR_OK;
 }
 
+namespace {
+// Switch decisions of the last stage: troubled cells (si[2c] != 0), cells on the low-order TVD
+// reconstruction (si[2c+1] == 1), shock cells (si[2c+1] < 0) and KFVS faces (a shock cell on either
+// side).  Per-block counts in shared memory, one atomic per counter and block.
+__global__ void k_switch_counts(int Nc, int Nf, const int8_t* si, const int2* on, unsigned long long* out) {
+  __shared__ unsigned int cnt[4];
+  if (threadIdx.x < 4) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < Nc) {
+    if (si[2 * i] != 0) atomicAdd(&cnt[0], 1u);
+    const int8_t f = si[2 * i + 1];
+    if (f == 1) atomicAdd(&cnt[1], 1u);
+    if (f < 0) atomicAdd(&cnt[2], 1u);
+  }
+  if (i < Nf) {
+    const int2 p = on[i];
+    if (si[2 * p.x + 1] < 0 || si[2 * p.y + 1] < 0) atomicAdd(&cnt[3], 1u);
+  }
+  __syncthreads();
+  if (threadIdx.x < 4 && cnt[threadIdx.x]) atomicAdd(&out[threadIdx.x], (unsigned long long)cnt[threadIdx.x]);
+}
+}  // namespace
+
+extern "C" afar_status afar_switch_counts(afar_solver* s, long long counts[4]) {
+  afar_status st = check_ready(s);
+  if (st) return st;
+  if (!counts) return (set_error("null output"), AFAR_ERR_ARGUMENT);
+  unsigned long long* d = nullptr;
+  AFAR_CUDA(cudaMalloc(&d, 4 * sizeof(unsigned long long)));
+  AFAR_CUDA(cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), s->stream));
+  const int n = std::max(s->Nc, s->Nf);
+  k_switch_counts<<<grid_for(n, 256), 256, 0, s->stream>>>(s->Nc, s->Nf, s->si, s->on, d);
+  unsigned long long h[4];
+  AFAR_CUDA(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+  AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  AFAR_CUDA(cudaFree(d));
+  for (int k = 0; k < 4; ++k) counts[k] = (long long)h[k];
+  return AFAR_OK;
+}
+
 extern "C" afar_status afar_device_bytes(afar_solver* s, size_t* bytes) {
   if (!s || !bytes) return (set_error("null argument"), AFAR_ERR_ARGUMENT);
   *bytes = s->bytes;

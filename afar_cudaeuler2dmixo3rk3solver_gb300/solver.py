@@ -400,6 +400,13 @@ class CudaSolver:
         """Land graph-replayed steps on multiples of ``interval`` (OpenFOAM adjustableRunTime); 0: off."""
         check(lib().afar_set_write_interval(self.h, interval))
 
+    def switch_counts(self) -> dict:
+        """Switch decisions of the last stage: troubled cells, low-order (TVD) cells, shock cells,
+        KFVS faces."""
+        out = (C.c_longlong * 4)()
+        check(lib().afar_switch_counts(self.h, out))
+        return dict(zip(["troubled_cells", "tvd_cells", "shock_cells", "kfvs_faces"], [int(v) for v in out]))
+
     def device_bytes(self) -> int:
         b = C.c_size_t()
         check(lib().afar_device_bytes(self.h, C.byref(b)))
@@ -504,6 +511,10 @@ class Server:
         _, _, _, out_FD, out_si = self._keep.pop(rid)
         check(status.value)
         return (out_FD, out_si, lat.value, steps.value) if with_steps else (out_FD, out_si, lat.value)
+
+    def cancel(self, rid: int):
+        """Cancel a queued or running request; wait() then raises AfarError (AFAR_ERR_CANCELLED)."""
+        check(lib().afar_server_cancel(self.h, int(rid)))
 
     def stats(self) -> dict:
         st = _ffi.ServerStats()

@@ -373,6 +373,7 @@ def run_ours(args, dist: Dist):
         results[pol]["device_bytes"] = s.device_bytes()
         if pol == "mixed":
             results[pol]["tuning"] = s.tuning()
+        results[pol]["switch_counts"] = s.switch_counts()  # the last profiled stage's decisions
 
     # e2e through the reference-shaped C ABI with host buffers (mixed policy)
     pol0 = policies[0]
@@ -450,7 +451,7 @@ def run_ours(args, dist: Dist):
             "value": hf.nc * K / (r["ms"] * 1e-3), "ms_per_step": r["ms"] / K, "finite": r["finite"],
             "algorithmic_GBps": b_s / (r["ms"] / K * 1e-3) / 1e9, "bytes_per_cell_step": b_s / hf.nc,
             "kernels_ms_per_step": r["kernels_ms"], "launches_per_step": r["launches"],
-            "device_bytes": r["device_bytes"],
+            "device_bytes": r["device_bytes"], "switch_counts": r["switch_counts"],
         }
     line = {
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": n, "steps": K, "warmup": Wm,

@@ -40,7 +40,8 @@ typedef enum {
   AFAR_ERR_LIMIT = 3,        /* a compile-time limit of the reference layout is exceeded     */
   AFAR_ERR_CUDA = 4,         /* a CUDA runtime call failed                                    */
   AFAR_ERR_STATE = 5,        /* call out of order (e.g. evolve before the stencil upload)    */
-  AFAR_ERR_NOT_FINITE = 6    /* a non-finite or non-positive state was detected              */
+  AFAR_ERR_NOT_FINITE = 6,   /* a non-finite or non-positive state was detected              */
+  AFAR_ERR_CANCELLED = 7     /* a served request was cancelled before it finished            */
 } afar_status;
 
 const char* afar_last_error(void);
@@ -373,6 +374,7 @@ typedef struct {
   long long peakRunning;
   size_t bytesInUse, peakBytes, budgetBytes;
   long long batchSteps;          /* steps of the batch so far (each steps every running member) */
+  long long cancelled;           /* requests cancelled (also counted in failed) */
 } afar_server_stats;
 afar_status afar_server_create(afar_server** server, int policy, int device, size_t hbmBudgetBytes,
                                int chunkSteps);
@@ -384,6 +386,11 @@ afar_status afar_server_submit(afar_server* server, const afar_request* request,
 afar_status afar_server_wait(afar_server* server, long long requestId, double timeoutSeconds, int* done,
                              int* requestStatus, double* latencyMs, long long* steps);
 afar_status afar_server_get_stats(afar_server* server, afar_server_stats* stats);
+/* Cancels a request: a queued one is dropped at once, a running one leaves the batch at the end of
+ * the chunk being stepped and its device memory is freed; its output buffers are not written and
+ * afar_server_wait reports AFAR_ERR_CANCELLED.  A request that has already finished is left as it
+ * is (AFAR_ERR_STATE). */
+afar_status afar_server_cancel(afar_server* server, long long requestId);
 /* Finishes the running and queued requests, then stops the worker. */
 afar_status afar_server_destroy(afar_server* server);
 
@@ -419,6 +426,9 @@ afar_status afar_adjustTimeStep_noalloc(const afar_basicFieldData* FD, const afa
 
 /* Device memory held by the solver, in bytes. */
 afar_status afar_device_bytes(afar_solver* solver, size_t* bytes);
+/* The switch decisions of the last stage computed: counts[0] troubled cells, [1] cells on the
+ * low-order (TVD) reconstruction, [2] shock cells (KFVS on their faces), [3] KFVS faces. */
+afar_status afar_switch_counts(afar_solver* solver, long long counts[4]);
 
 /* The autotuner (no counterpart in the reference).  The mixed policy's reconstruct has two
  * implementations, tile-staged (0) and register pass (1); at the stencil upload each is timed on

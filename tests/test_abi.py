@@ -133,3 +133,4 @@ def test_server_rejects_bad_arguments_without_a_gpu():
     assert L.afar_server_submit(None, None, None) == 1
     assert L.afar_server_get_stats(None, None) == 1
     assert L.afar_server_destroy(None) == 0
+    assert L.afar_server_cancel(None, 1) == 1

@@ -273,3 +273,20 @@ def test_autotuner_picks_a_reconstruct_and_caches_it(cases):
         outs.append(s.state())
     scale = np.abs(outs[0]["cFD"]).max(axis=0)
     assert (np.abs(outs[0]["cFD"] - outs[1]["cFD"]) <= 1e-5 * scale).all()
+
+
+@pytest.mark.parametrize("policy", ["ref", "mixed"])
+def test_switch_counts_match_the_flags(cases, policy):
+    """afar_switch_counts against counts taken on the host from the downloaded flags."""
+    hf, cfg = cases["mixed_riemann"]
+    s = _solver(hf, cfg, policy)
+    s.run(6)
+    si = s.state()["shockIndicator"]
+    nc = hf.nc
+    flag0, final = si[0:2 * nc:2], si[1:2 * nc:2]
+    nb = hf.neighbour.reshape(-1, 2)
+    shock = final < 0
+    expect = {"troubled_cells": int(np.count_nonzero(flag0)), "tvd_cells": int(np.count_nonzero(final == 1)),
+              "shock_cells": int(np.count_nonzero(shock)), "kfvs_faces": int(np.count_nonzero(shock[nb[:, 0]] | shock[nb[:, 1]]))}
+    assert s.switch_counts() == expect
+    assert expect["troubled_cells"] > 0  # the Riemann problem exercises the switch

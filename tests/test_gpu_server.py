@@ -87,3 +87,53 @@ def test_destroy_finishes_queued_requests(cases):
     for rid in ids:
         FD = keep[rid][3]
         assert np.isfinite(FD).all() and (FD[:, 0] > 0).all()
+
+
+def test_cancel_queued_and_running(cases):
+    """afar_server_cancel: a queued request is dropped at once, a running one leaves after its
+    chunk; neither writes its outputs; the rest of the queue is served as if they had not been."""
+    import time
+
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import AfarError, Server
+
+    srv = Server("mixed", hbm_budget_bytes=1, chunk_steps=4)  # one solve at a time: the rest queue
+    long_id = srv.submit(*cases["ffs_tri"], n_steps=100000)
+    queued_id = srv.submit(*cases["quad_riemann"], n_steps=10)
+    ok_id = srv.submit(*cases["mixed_riemann"], n_steps=12)
+    srv.cancel(queued_id)
+    with pytest.raises(AfarError, match="cancel"):
+        srv.wait(queued_id, timeout=60.0)
+    t0 = time.time()
+    while srv.stats()["running"] < 1 and time.time() - t0 < 60.0:
+        time.sleep(0.01)
+    srv.cancel(long_id)
+    with pytest.raises(AfarError, match="cancel"):
+        srv.wait(long_id, timeout=120.0)
+    FD, si, lat = srv.wait(ok_id, timeout=120.0)
+    assert np.array_equal(FD, _alone(*cases["mixed_riemann"], "mixed", 0.0, 12)["FD"])
+    with pytest.raises(AfarError):
+        srv.cancel(ok_id)  # finished
+    st = srv.stats()
+    assert st["cancelled"] == 2 and st["completed"] == 1 and st["failed"] == 2 and st["bytesInUse"] == 0
+    srv.close()
+
+
+def test_non_finite_request_fails_alone(cases):
+    """A request whose state holds a NaN (injected in its host input) is failed with
+    AFAR_ERR_NOT_FINITE; the solve batched beside it is unaffected (bitwise)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import AfarError, Server
+    from afar_cudaeuler2dmixo3rk3solver_gb300.solver import HostFields
+
+    hf, cfg = cases["quad_riemann"]
+    bad = HostFields(hf.sizes, {k: v.copy() for k, v in hf.a.items()}, hf.period)
+    bad.a["FD"][7] = np.nan
+    bad.a["cFD"][7] = np.nan
+    srv = Server("mixed", chunk_steps=5)
+    ids = [srv.submit(bad, cfg, n_steps=10), srv.submit(*cases["mixed_riemann"], n_steps=10)]
+    with pytest.raises(AfarError, match="finite"):
+        srv.wait(ids[0], timeout=120.0)
+    FD, si, lat = srv.wait(ids[1], timeout=120.0)
+    assert np.array_equal(FD, _alone(*cases["mixed_riemann"], "mixed", 0.0, 10)["FD"])
+    st = srv.stats()
+    assert st["failed"] == 1 and st["completed"] == 1
+    srv.close()
