@@ -14,8 +14,19 @@
 #include <tuple>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "afar_internal.h"
 #include "afar_kernels.cuh"
+
+namespace {
+// A named NVTX range over an entry point (host-side tracing: it shows the library's calls on a
+// profiler timeline beside their kernels; inert without a profiler attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
 
 using namespace afar;
 
@@ -799,6 +810,7 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
                                                       int maxStencilSize, int maxCompactStencilSize,
                                                       int maxLocalBlockStencilSize,
                                                       int maxCompactLocalBlockStencilSize) {
+  NvtxRange nvtx("afar_setDeviceFieldDataStencil");
   if (!s || !h) {
     set_error("afar_setDeviceFieldDataStencil: null argument");
     return AFAR_ERR_ARGUMENT;
@@ -957,6 +969,7 @@ static afar_status ensure_graph(afar_solver* s, double R, double Cv) {
 }
 
 extern "C" afar_status afar_adjustTimeStep(afar_solver* s, int facesNum, double R, double Cv, double CFL, double* dt) {
+  NvtxRange nvtx("afar_adjustTimeStep");
   afar_status st = check_ready(s);
   if (st) return st;
   if (!dt || facesNum != s->Nf || !(R > 0.0) || !(Cv > 0.0) || !(CFL > 0.0)) {
@@ -1026,6 +1039,7 @@ extern "C" afar_status afar_adjustTimeStep(afar_solver* s, int facesNum, double 
 }
 
 static afar_status run_impl(afar_solver* s, int nSteps, double dt, double CFL, double tEnd, bool wait) {
+  NvtxRange nvtx("afar_run");
   afar_status st = check_ready(s);
   if (st || (st = check_not_batched(s))) return st;
   if (nSteps < 0 || (!(dt > 0.0) && !(CFL > 0.0))) {
@@ -1044,6 +1058,7 @@ static afar_status run_impl(afar_solver* s, int nSteps, double dt, double CFL, d
 extern "C" afar_status afar_GPUevolve(afar_solver* s, double R, double Cv, double deltaT, int cellsNum, int facesNum,
                                       int totalBoundaryFacesNum, int maxStencilSize, int maxCompactStencilSize,
                                       int maxLocalBlockStencilSize, int maxCompactLocalBlockStencilSize) {
+  NvtxRange nvtx("afar_GPUevolve");
   const bool head_done = s && s->head_pending;  // read before check_ready clears it
   afar_status st = check_ready(s);
   if (st) return st;
@@ -1618,6 +1633,7 @@ extern "C" afar_status afar_batch_size(afar_batch* b, int* n) {
 }
 
 extern "C" afar_status afar_batch_run(afar_batch* b, int nSteps, float* ms) {
+  NvtxRange nvtx("afar_batch_run");
   if (!b || nSteps < 0) return (set_error("afar_batch_run: bad argument"), AFAR_ERR_ARGUMENT);
   AFAR_CUDA(cudaSetDevice(b->device));
   afar_status st;
