@@ -40,7 +40,7 @@ PROFILE_STEPS = 10
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one mixed-policy reconstruct launch
 # (tile-staged) per cell, from an ncu capture of the 500,094-cell version of this workload (traffic
 # grows with the cells of the tile stream); None when no capture matches the current kernels.
-RECON_TRAFFIC_BYTES_PER_CELL = 411.9
+RECON_TRAFFIC_BYTES_PER_CELL = 399.1
 
 
 def parse():
@@ -227,7 +227,8 @@ def reconstruct_bytes_per_launch(hf, policy: str) -> float:
       per cell: W (4 wW), LS rows (2 m wO), stencil ids (4 S), face ids (4 m), counts (2), face
                 geometry (2 x 2 words per face slot, 4 m wG), gradient out (8 wG), limiter out
                 (4 wS), troubled flag out (1)
-      per internal face: O3 weights of both sides ((S_own+1 + S_nei+1) wO), face values out (8 wG)
+      per internal face: O3 weights of both sides ((S_own+1 + S_nei+1) wO; mixed, whose sums run in
+                         difference form, reads no own-cell weight: (S_own + S_nei) wO), face values out (8 wG)
     wG = gradient/face-value word, wS = limiter word (4 for mixed, else 8 and 4/8)."""
     wW = 4 if policy == "mixed" else 8
     wO = 8 if policy == "fp64" else 4
@@ -237,7 +238,8 @@ def reconstruct_bytes_per_launch(hf, policy: str) -> float:
     m = hf.compactStencilSize.astype(np.float64)
     nb = hf.neighbour.reshape(-1, 2)
     cells = np.sum(4 * wW + 2 * m * wO + 4 * S + 4 * m + 2 + 4 * m * wG + 8 * wG + 4 * wS + 1)
-    faces = np.sum((S[nb[:, 0]] + 1 + S[nb[:, 1]] + 1) * wO + 8 * wG)
+    own_w = 0 if policy == "mixed" else 2
+    faces = np.sum((S[nb[:, 0]] + S[nb[:, 1]] + own_w) * wO + 8 * wG)
     return float(cells + faces)
 
 
