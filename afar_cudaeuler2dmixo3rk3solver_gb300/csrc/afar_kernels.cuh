@@ -814,10 +814,22 @@ __device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
   const int finalType = (shockType > 0) * (shockTypeExt > 1) * (-2) + (bvdType > 0);
   a.si[2 * c + 1] = (int8_t)finalType;
   const bool isShock = finalType < 0;
-  L.x = pick<P>(isShock, !isShock, to_venkat(L.x), to_bj(L.x));
-  L.y = pick<P>(isShock, !isShock, to_venkat(L.y), to_bj(L.y));
-  L.z = pick<P>(isShock, !isShock, to_venkat(L.z), to_bj(L.z));
-  L.w = pick<P>(isShock, !isShock, to_venkat(L.w), to_bj(L.w));
+  if constexpr (P::exact_blend) {  // the reference's blend evaluates both maps
+    L.x = pick<P>(isShock, !isShock, to_venkat(L.x), to_bj(L.x));
+    L.y = pick<P>(isShock, !isShock, to_venkat(L.y), to_bj(L.y));
+    L.z = pick<P>(isShock, !isShock, to_venkat(L.z), to_bj(L.z));
+    L.w = pick<P>(isShock, !isShock, to_venkat(L.w), to_bj(L.w));
+  } else if (isShock) {  // only the map that applies: Venkatakrishnan's has a division
+    L.x = to_venkat(L.x);
+    L.y = to_venkat(L.y);
+    L.z = to_venkat(L.z);
+    L.w = to_venkat(L.w);
+  } else {
+    L.x = to_bj(L.x);
+    L.y = to_bj(L.y);
+    L.z = to_bj(L.z);
+    L.w = to_bj(L.w);
+  }
   a.lim[c] = L;
 }
 
