@@ -963,16 +963,18 @@ __device__ __forceinline__ void roe_flux_fast(D& rhoFlux, D& rhoUxFlux, D& rhoUy
   const D hL = Cv * tL + kL + R * tL;
   const D hR = Cv * tR + kR + R * tR;
   const D tiny = AFAR_LIT(D, 1e-20);
-  const D rhoT = sqr_(fmx(rhoL * rhoR, tiny));
   const D sL = sqr_(fmx(rhoL, tiny)), sR = sqr_(fmx(rhoR, tiny));
+  const D rhoT = sL * sR;  // sqrt(rhoL rhoR) from the two roots the weights need anyway
   const D wL = fdiv(sL, sL + sR);
   const D wR = D(1) - wL;
   const D uxT = uxL * wL + uxR * wR;
   const D uyT = uyL * wL + uyR * wR;
   const D hT = hL * wL + hR * wR;
   const D q2 = uxT * uxT + uyT * uyT;
-  const D cT = sqr_(fmx((gamma - D(1)) * (hT - D(0.5) * q2), tiny));
-  const D ic2 = fdiv(D(1), cT * cT);
+  const D cT2 = fmx((gamma - D(1)) * (hT - D(0.5) * q2), tiny);
+  const D rcT = rsq_(cT2);  // 1/cT: the speed and 1/cT^2 from one reciprocal root
+  const D cT = cT2 * rcT;
+  const D ic2 = rcT * rcT;
   const D cvT = uxT * nfx + uyT * nfy;
   const D dUx = uxR - uxL;
   const D dUy = uyR - uyL;

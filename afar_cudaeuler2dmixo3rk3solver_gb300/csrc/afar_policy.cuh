@@ -78,6 +78,8 @@ __device__ __forceinline__ float fab(float a) { return fabsf(a); }
 __device__ __forceinline__ double fab(double a) { return fabs(a); }
 __device__ __forceinline__ float sqr_(float a) { return sqrtf(a); }
 __device__ __forceinline__ double sqr_(double a) { return sqrt(a); }
+__device__ __forceinline__ float rsq_(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double rsq_(double a) { return rsqrt(a); }
 __device__ __forceinline__ float erfc_(float a) { return erfcf(a); }
 __device__ __forceinline__ double erfc_(double a) { return erfc(a); }
 __device__ __forceinline__ float exp_(float a) { return expf(a); }
