@@ -53,6 +53,11 @@ def small_cases():
     inlet = [p for p in m.patches if p[0] == "inlet"][0]
     Wb[inlet[2] - m.n_internal_faces: inlet[2] - m.n_internal_faces + inlet[3]] = [30.05945, 4.07795, 0.0, 5.97677]
     cases["corner_flow"] = (m, W, Wb, "edgeNeighbour")
+    # the isentropic vortex (strength 5, free stream 1) on 20 x 20 quads of the [-7, 9]^2 box, outlets
+    m = M.vortex_box(20)
+    W = M.vortex_fields(m.cell_centres(), xc=0.0, yc=0.0)
+    Wb = M.vortex_fields(m.boundary_face_centres(), xc=0.0, yc=0.0)
+    cases["vortex_box"] = (m, W, Wb, "edgeNeighbour")
     return cases
 
 

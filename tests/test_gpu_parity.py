@@ -53,7 +53,7 @@ def ref_kernels():
     return ref_harness
 
 
-CASES = ["quad_riemann", "ffs_tri", "mixed_riemann", "corner_flow"]
+CASES = ["quad_riemann", "ffs_tri", "mixed_riemann", "corner_flow", "vortex_box"]
 FIELDS = ["faceFD", "gradFD", "Flux", "Res", "FD", "cFD"]
 
 
