@@ -265,7 +265,7 @@ def _read_boundary(path: str):
     return out
 
 
-def read_poly_mesh(case_dir: str, labels: dict | None = None, renumber: bool = False) -> M.FoamMesh:
+def read_poly_mesh(case_dir: str, labels: dict | None = None, renumber: bool | str = False) -> M.FoamMesh:
     """The 2-D cross-section of the one-cell-deep polyMesh in ``case_dir/constant/polyMesh`` (what the
     reference's solver reads through OpenFOAM, basicCUDAsolver.cpp:122-258).
 
@@ -275,7 +275,8 @@ def read_poly_mesh(case_dir: str, labels: dict | None = None, renumber: bool = F
     patch's index in the boundary file (empty patches included, as fvSchemes ``CUDA { boundary {
     patch<k> ...; } }`` counts them) to its cudaEulerBCs label; a missing label is an error, like the
     reference's lookup.  Face order, owners and neighbours are kept as the file has them (the
-    reference runs on the mesh as renumberMesh left it); ``renumber`` applies reverse Cuthill-McKee."""
+    reference runs on the mesh as renumberMesh left it); ``renumber`` applies reverse Cuthill-McKee
+    (``True``) or the Hilbert-curve order (``"hilbert"``)."""
     d = os.path.join(case_dir, "constant", "polyMesh")
     P3 = _read_numbers(os.path.join(d, "points"), 3, np.float64)
     foff, flab = _read_label_lists(os.path.join(d, "faces"))
@@ -366,7 +367,7 @@ def read_poly_mesh(case_dir: str, labels: dict | None = None, renumber: bool = F
     mesh = M.FoamMesh(points=pts, cell_ptr=cptr.astype(np.int32), cell_pts=cpts.astype(np.int32),
                       face_pts=fpts.astype(np.int32), owner=fown.astype(np.int32),
                       neighbour=neigh.astype(np.int32), patches=patches, depth=depth)
-    return M.renumber_mesh(mesh) if renumber else mesh
+    return M.renumber_mesh(mesh, "rcm" if renumber is True else renumber) if renumber else mesh
 
 
 # ----------------------------------------------------------------------------------- the case

@@ -111,6 +111,48 @@ def _rcm_permutation(n_cells, own, nei):
     return np.asarray(reverse_cuthill_mckee(g, symmetric_mode=True), dtype=np.int64)
 
 
+def _hilbert_permutation(xy, bits=16):
+    """Cells sorted along a Hilbert curve through their centres (new -> old).  Consecutive cells
+    then form compact patches, so the stencils of a 128-cell tile share most of their members
+    (reverse Cuthill-McKee makes a tile a thin strip along its front instead).  The curve index is
+    the classic quadrant-rotation walk from the coarsest level down (Hilbert 1891; the
+    ``xy2d`` form of Butz's algorithm), on a 2^bits grid over the bounding square."""
+    n = 1 << bits
+    xy = np.asarray(xy, dtype=np.float64)
+    if xy.shape[0] == 0:
+        return np.zeros(0, dtype=np.int64)
+    lo = xy.min(axis=0)
+    span = float((xy.max(axis=0) - lo).max()) or 1.0
+    q = np.minimum(((xy - lo) * (n / span)).astype(np.int64), n - 1)
+    x, y = q[:, 0].copy(), q[:, 1].copy()
+    d = np.zeros(xy.shape[0], dtype=np.int64)
+    s = n >> 1
+    while s > 0:
+        rx = ((x & s) > 0).astype(np.int64)
+        ry = ((y & s) > 0).astype(np.int64)
+        d += s * s * ((3 * rx) ^ ry)
+        # turn the quadrant so its sub-curve runs like the parent's: reflect, then transpose
+        refl = (ry == 0) & (rx == 1)
+        x = np.where(refl, n - 1 - x, x)
+        y = np.where(refl, n - 1 - y, y)
+        swap = ry == 0
+        x, y = np.where(swap, y, x), np.where(swap, x, y)
+        s >>= 1
+    return np.argsort(d, kind="stable").astype(np.int64)
+
+
+def _cell_permutation(renumber, nc, own, nei, centres):
+    """new -> old cell order: reverse Cuthill-McKee (``True`` or "rcm"), a Hilbert curve through
+    the cell centres ("hilbert"), or the given order (``False``)."""
+    if renumber == "hilbert":
+        return _hilbert_permutation(centres())
+    if renumber is True or renumber == "rcm":
+        return _rcm_permutation(nc, own, nei)
+    if renumber is False or renumber is None:
+        return np.arange(nc, dtype=np.int64)
+    raise ValueError(f"unknown cell order {renumber!r}: True/'rcm', 'hilbert' or False")
+
+
 def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=True, depth=1.0, alias=None,
                     period=(0.0, 0.0)):
     """Assemble OpenFOAM-ordered face lists from cell polygons.
@@ -152,13 +194,10 @@ def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=T
 
     ci = cell_of[he_i]
     cj = cell_of[he_j]
-    if renumber:
-        perm = _rcm_permutation(nc, ci, cj)  # new -> old
-        inv = np.empty(nc, dtype=np.int64)
-        inv[perm] = np.arange(nc)
-    else:
-        perm = np.arange(nc)
-        inv = perm
+    perm = _cell_permutation(renumber, nc, ci, cj,
+                             lambda: _polygon_centroids(points, cell_ptr, cell_pts)[0])  # new -> old
+    inv = np.empty(nc, dtype=np.int64)
+    inv[perm] = np.arange(nc)
     ni = inv[ci]
     nj = inv[cj]
     own = np.minimum(ni, nj)
@@ -213,14 +252,16 @@ def build_foam_mesh(points, cell_ptr, cell_pts, classify, patch_defs, renumber=T
     )
 
 
-def renumber_mesh(m: FoamMesh) -> FoamMesh:
-    """``m`` with its cells in reverse Cuthill-McKee order (renumberMesh): internal faces back in
-    upper-triangular order (a face whose owner and neighbour swap has its points swapped, so its
-    normal still leaves the owner), boundary faces sorted by owner within each patch."""
+def renumber_mesh(m: FoamMesh, order="rcm") -> FoamMesh:
+    """``m`` with its cells in reverse Cuthill-McKee order (renumberMesh; ``order="hilbert"``: along
+    a Hilbert curve through the cell centres): internal faces back in upper-triangular order (a
+    face whose owner and neighbour swap has its points swapped, so its normal still leaves the
+    owner), boundary faces sorted by owner within each patch."""
     nc, nf = m.n_cells, m.n_internal_faces
     own = m.owner.astype(np.int64)
     nei = m.neighbour.astype(np.int64)
-    perm = _rcm_permutation(nc, own[:nf], nei)
+    perm = _cell_permutation(order, nc, own[:nf], nei,
+                             lambda: _polygon_centroids(m.points, m.cell_ptr, m.cell_pts)[0])
     inv = np.empty(nc, dtype=np.int64)
     inv[perm] = np.arange(nc)
     o, n = inv[own[:nf]], inv[nei]
@@ -443,14 +484,14 @@ def forward_step_triangles(n_points=1_000_000, jitter=0.3, seed=0, renumber=True
                            renumber=renumber)
 
 
-def riemann_mixed(n=1766, radius=0.3, seed=0):
+def riemann_mixed(n=1766, radius=0.3, seed=0, renumber=True):
     """Unit square of quads with the cells inside a central disk of ``radius`` split into seeded
     triangles: a conforming mixed quad/triangle mesh (about 4M cells at n=1766).  All sides are
     outlets (label 4)."""
     def tri_mask(xc, yc):
         return (xc - 0.5) ** 2 + (yc - 0.5) ** 2 < radius * radius
 
-    return quad_grid(n, n, tri_mask=tri_mask, seed=seed)
+    return quad_grid(n, n, tri_mask=tri_mask, seed=seed, renumber=renumber)
 
 
 # ---------------------------------------------------------------------------------- initial fields

@@ -2,7 +2,8 @@
 """Benchmark: cell-RK3-steps/s of the AFAR stage on the Mach 3 forward-facing-step workload.
 
 Workload (one GPU): channel [0,3]x[0,1] with the step [0.6,3]x[0,0.2] removed, Delaunay
-triangulation of ~1M seeded jittered points (jitter 0.3h), RCM-renumbered: about 2.0M triangles,
+triangulation of ~1M seeded jittered points (jitter 0.3h), cells in Hilbert-curve order (--order rcm:
+reverse Cuthill-McKee, the renumberMesh order): about 2.0M triangles,
 3.0M internal faces.  Inflow rho=1.4, p=1, u=3 (label 3), slip walls (label 2), outflow (label 4),
 edge-neighbour stencils, R = 1/1.4, Cv = R/0.4, CFL 0.2, device-side CFL step every step.
 Synthetic, seeded inputs; the working set (~1.5 GB) is larger than L2, so no L2 flush is needed.
@@ -38,9 +39,10 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 PROFILE_STEPS = 10
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one mixed-policy reconstruct launch
-# (tile-staged) per cell, from an ncu capture of the 500,094-cell version of this workload (traffic
-# grows with the cells of the tile stream); None when no capture matches the current kernels.
-RECON_TRAFFIC_BYTES_PER_CELL = 399.1
+# (tile-staged) per cell, from an ncu capture of the 500,094-cell version of this workload in
+# Hilbert-curve order (traffic grows with the cells of the tile stream; the reverse Cuthill-McKee
+# order measured 399.1); None when no capture matches the current kernels.
+RECON_TRAFFIC_BYTES_PER_CELL = 398.5
 
 
 def parse():
@@ -60,6 +62,8 @@ def parse():
     ap.add_argument("--mesh", default="step", choices=["step", "riemann_mixed"],
                     help="step: the metric's workload; riemann_mixed: the 4M-cell mixed quad/triangle case")
     ap.add_argument("--mixed-n", type=int, default=1766)
+    ap.add_argument("--order", default="hilbert", choices=["rcm", "hilbert"],
+                    help="cell order of the workload's mesh: reverse Cuthill-McKee or a Hilbert curve")
     ap.add_argument("--recon", default="auto", choices=["auto", "tile", "register"],
                     help="mixed reconstruct variant: autotuned (default) or forced")
     ap.add_argument("--serve", action="store_true",
@@ -185,7 +189,8 @@ WORKLOADS = {
 }
 
 
-def make_workload(points: int, seed: int, cfl: float, kind: str = "step", mixed_n: int = 1766):
+def make_workload(points: int, seed: int, cfl: float, kind: str = "step", mixed_n: int = 1766,
+                  order: str = "rcm"):
     """step: the Mach 3 forward step (about points/2 x 4 triangles); riemann_mixed: the unit square
     of mixed_n^2 quads with the cells of a central disk (r = 0.3) split into seeded triangles (about
     4.0M cells at 1766), four-quadrant Riemann states, outlets all round."""
@@ -193,10 +198,10 @@ def make_workload(points: int, seed: int, cfl: float, kind: str = "step", mixed_
 
     t0 = time.time()
     if kind == "riemann_mixed":
-        m = mesh.riemann_mixed(mixed_n, seed=seed)
+        m = mesh.riemann_mixed(mixed_n, seed=seed, renumber=order)
         W, Wb = mesh.riemann_fields(m)
     else:
-        m = mesh.forward_step_triangles(points, seed=seed)
+        m = mesh.forward_step_triangles(points, seed=seed, renumber=order)
         W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
     cfg = CaseConfig(stencilType="edgeNeighbour", CFL=cfl)
     hf = precompute(m, cfg, W, Wb, want_rbf64=True)
@@ -280,7 +285,7 @@ def run_reference_arm(args, dist: Dist):
     from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
 
     b.build_all()
-    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n)
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n, args.order)
     rate, cores, el, steps = cpu_oracle_rate(hf, cfg, target_s=20.0, max_steps=min(120, max(2, args.steps)))
     sample = (f"{steps} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle (ref policy), "
               f"{el:.1f} s")
@@ -291,7 +296,7 @@ def run_reference_arm(args, dist: Dist):
         "impl": "reference",
         "config": {"workload": WORKLOADS[args.mesh][0], "cells": hf.nc, "internal_faces": hf.nf,
                    "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
-                   "parallelism": "replicas"},
+                   "cell_order": args.order, "parallelism": "replicas"},
         "cpu_baseline": {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference has no CPU implementation of the path; this is its algorithm restated in C "
@@ -331,7 +336,7 @@ def run_ours(args, dist: Dist):
 
     b.build_all()
     device = dist.local
-    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n)
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n, args.order)
     K, Wm = args.steps, max(3, args.warmup)
     hbm, peak_kind = peaks()
     policies = [p for p in args.policies.split(",") if p]
@@ -462,7 +467,8 @@ def run_ours(args, dist: Dist):
         "data": WORKLOADS[args.mesh][1],
         "config": {"workload": WORKLOADS[args.mesh][0], "policy": pol0, "cells": hf.nc, "internal_faces": hf.nf,
                    "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
-                   "max_stencil": hf.sizes["maxStencilSize"], "dt": "device CFL step every step",
+                   "max_stencil": hf.sizes["maxStencilSize"], "cell_order": args.order,
+                   "dt": "device CFL step every step",
                    "l2": "working set > L2 (no flush needed)", "parallelism": "replicas" if n > 1 else "single",
                    "timed_chunks": chunks, "chunk_start": f"state after {Wm} warm-up steps (device snapshot)",
                    "setup_s": round(setup_s, 1)},

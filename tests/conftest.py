@@ -42,6 +42,9 @@ def small_cases():
     m = M.forward_step_triangles(1500, seed=3)
     W, Wb = M.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
     cases["ffs_tri"] = (m, W, Wb, "edgeNeighbour")
+    m = M.forward_step_triangles(1500, seed=4, renumber="hilbert")  # the benchmark's cell order
+    W, Wb = M.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
+    cases["ffs_tri_hilbert"] = (m, W, Wb, "edgeNeighbour")
     m = M.riemann_mixed(30, seed=5)
     W, Wb = M.riemann_fields(m)
     cases["mixed_riemann"] = (m, W, Wb, "edgeNeighbour")

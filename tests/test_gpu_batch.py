@@ -28,7 +28,7 @@ def cases():
     for name, (m, W, Wb, st) in small_cases().items():
         if name == "corner_flow":
             cfg = CaseConfig(R=0.7142857, Cv=1.7857142857, CFL=0.1, stencilType=st, cOrder=7, fOrder=5)
-        elif name == "ffs_tri":
+        elif name.startswith("ffs_tri"):
             cfg = CaseConfig(stencilType=st, CFL=0.2)
         else:
             cfg = CaseConfig(stencilType=st)

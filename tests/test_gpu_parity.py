@@ -32,7 +32,7 @@ def cases():
     out = {}
     for name, (m, W, Wb, st) in small_cases().items():
         cfg = CaseConfig(stencilType=st)
-        if name == "ffs_tri":
+        if name.startswith("ffs_tri"):
             cfg = CaseConfig(stencilType=st, CFL=0.2)  # the coarse step mesh needs it at start-up
         if name == "corner_flow":
             # the reference's settings (fvSchemes, controlDict) except CFL: its Courant step skips
@@ -53,7 +53,7 @@ def ref_kernels():
     return ref_harness
 
 
-CASES = ["quad_riemann", "ffs_tri", "mixed_riemann", "corner_flow", "vortex_box"]
+CASES = ["quad_riemann", "ffs_tri", "ffs_tri_hilbert", "mixed_riemann", "corner_flow", "vortex_box"]
 FIELDS = ["faceFD", "gradFD", "Flux", "Res", "FD", "cFD"]
 
 

@@ -24,7 +24,7 @@ def _same_bundle(a, b):
         assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), k
 
 
-@pytest.mark.parametrize("name", ["quad_riemann", "ffs_tri", "mixed_riemann", "corner_flow"])
+@pytest.mark.parametrize("name", ["quad_riemann", "ffs_tri", "ffs_tri_hilbert", "mixed_riemann", "corner_flow"])
 def test_device_rbf_stage_is_bit_identical(name):
     from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, precompute
 

@@ -20,7 +20,7 @@ def cases():
     for name, (m, W, Wb, st) in small_cases().items():
         if name == "corner_flow":
             continue
-        cfg = CaseConfig(stencilType=st, CFL=0.2 if name == "ffs_tri" else 0.3)
+        cfg = CaseConfig(stencilType=st, CFL=0.2 if name.startswith("ffs_tri") else 0.3)
         out[name] = (precompute(m, cfg, W, Wb, want_rbf64=True), cfg)
     return out
 

@@ -18,7 +18,7 @@ def cases():
     return out
 
 
-NAMES = ["quad_riemann", "ffs_tri", "mixed_riemann", "corner_flow"]
+NAMES = ["quad_riemann", "ffs_tri", "ffs_tri_hilbert", "mixed_riemann", "corner_flow"]
 
 
 @pytest.mark.parametrize("name", NAMES)
