@@ -2,8 +2,8 @@
 """Benchmark: cell-RK3-steps/s of the AFAR stage on the Mach 3 forward-facing-step workload.
 
 Workload (one GPU): channel [0,3]x[0,1] with the step [0.6,3]x[0,0.2] removed, Delaunay
-triangulation of ~1M seeded jittered points (jitter 0.3h), cells in Hilbert-curve order (--order rcm:
-reverse Cuthill-McKee, the renumberMesh order): about 2.0M triangles,
+triangulation of ~1M seeded jittered points (jitter 0.3h), RCM-renumbered (--order hilbert: cells
+along a Hilbert curve instead): about 2.0M triangles,
 3.0M internal faces.  Inflow rho=1.4, p=1, u=3 (label 3), slip walls (label 2), outflow (label 4),
 edge-neighbour stencils, R = 1/1.4, Cv = R/0.4, CFL 0.2, device-side CFL step every step.
 Synthetic, seeded inputs; the working set (~1.5 GB) is larger than L2, so no L2 flush is needed.
@@ -39,10 +39,10 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 PROFILE_STEPS = 10
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one mixed-policy reconstruct launch
-# (tile-staged) per cell, from an ncu capture of the 500,094-cell version of this workload in
-# Hilbert-curve order (traffic grows with the cells of the tile stream; the reverse Cuthill-McKee
-# order measured 399.1); None when no capture matches the current kernels.
-RECON_TRAFFIC_BYTES_PER_CELL = 398.5
+# (tile-staged) per cell, by cell order, from ncu captures of the 500,094-cell version of this
+# workload (traffic grows with the cells of the tile stream); None when no capture matches the
+# current kernels.
+RECON_TRAFFIC_BYTES_PER_CELL = {"rcm": 399.1, "hilbert": 398.5}
 
 
 def parse():
@@ -62,7 +62,7 @@ def parse():
     ap.add_argument("--mesh", default="step", choices=["step", "riemann_mixed"],
                     help="step: the metric's workload; riemann_mixed: the 4M-cell mixed quad/triangle case")
     ap.add_argument("--mixed-n", type=int, default=1766)
-    ap.add_argument("--order", default="hilbert", choices=["rcm", "hilbert"],
+    ap.add_argument("--order", default="rcm", choices=["rcm", "hilbert"],
                     help="cell order of the workload's mesh: reverse Cuthill-McKee or a Hilbert curve")
     ap.add_argument("--recon", default="auto", choices=["auto", "tile", "register"],
                     help="mixed reconstruct variant: autotuned (default) or forced")
@@ -446,8 +446,8 @@ def run_ours(args, dist: Dist):
     achieved = b_launch / (t_launch * 1e-3) / 1e9
     tuning = head.get("tuning")
     tile = tuning is not None and tuning["recon_variant"] == 0
-    traffic = (RECON_TRAFFIC_BYTES_PER_CELL * hf.nc
-               if RECON_TRAFFIC_BYTES_PER_CELL is not None and pol0 == "mixed" and tile else None)
+    per_cell = (RECON_TRAFFIC_BYTES_PER_CELL or {}).get(args.order) if args.mesh == "step" else None
+    traffic = per_cell * hf.nc if per_cell is not None and pol0 == "mixed" and tile else None
     recon_kind = ("reconstruct (mixed, tile-staged)" if tile else "reconstruct (mixed, register pass)"
                   if pol0 == "mixed" else f"reconstruct ({pol0}, staged)")
     by_policy = {}
