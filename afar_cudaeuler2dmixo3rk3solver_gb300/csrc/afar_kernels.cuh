@@ -1208,22 +1208,37 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
       const G uxLT = (G)Wo.y + lo.y * (go0.z * dxL + go1.x * dyL);
       const G uyLT = (G)Wo.z + lo.z * (go0.w * dxL + go1.y * dyL);
       const G tLT = (G)Wo.w + lo.w * (go1.z * dxL + go1.w * dyL);
-      const G rhoLT = fdiv(pLT * iR, tLT);
       const G pRT = (G)Wn.x + ln.x * (gn0.x * dxR + gn0.y * dyR);
       const G uxRT = (G)Wn.y + ln.y * (gn0.z * dxR + gn1.x * dyR);
       const G uyRT = (G)Wn.z + ln.z * (gn0.w * dxR + gn1.y * dyR);
       const G tRT = (G)Wn.w + ln.w * (gn1.z * dxR + gn1.w * dyR);
-      const G rhoRT = fdiv(pRT * iR, tRT);
       const G pL = pick<P>(!tvdL, tvdL, fo.x, pLT);
       const G uxL = pick<P>(!tvdL, tvdL, fo.y, uxLT);
       const G uyL = pick<P>(!tvdL, tvdL, fo.z, uyLT);
       const G tL = pick<P>(!tvdL, tvdL, fo.w, tLT);
-      const G rhoL = fdiv(pL * iR, tL);
       const G pR = pick<P>(!tvdR, tvdR, fn.x, pRT);
       const G uxR = pick<P>(!tvdR, tvdR, fn.y, uxRT);
       const G uyR = pick<P>(!tvdR, tvdR, fn.z, uyRT);
       const G tR = pick<P>(!tvdR, tvdR, fn.w, tRT);
-      const G rhoR = fdiv(pR * iR, tR);
+      G rhoLT, rhoRT, rhoL, rhoR;  // p / (R T) of the four states
+      if constexpr (kF32) {
+        rhoLT = fdiv(pLT * iR, tLT);
+        rhoRT = fdiv(pRT * iR, tRT);
+        rhoL = fdiv(pL * iR, tL);
+        rhoR = fdiv(pR * iR, tR);
+      } else {
+        // FP64: the four reciprocal temperatures from one division (Montgomery's simultaneous
+        // inversion, a few ulps from four divisions); a double division is among the dearest
+        // operations of GB300's FP64 pipe, which bounds this kernel.  Temperatures stay far from
+        // the range limits of double (their product of four neither overflows nor underflows).
+        const G tt = tL * tR, ttT = tLT * tRT;
+        const G inv = G(1) / (tt * ttT);
+        const G itt = inv * ttT, ittT = inv * tt;  // 1/(tL tR), 1/(tLT tRT)
+        rhoL = pL * iR * (itt * tR);
+        rhoR = pR * iR * (itt * tL);
+        rhoLT = pLT * iR * (ittT * tRT);
+        rhoRT = pRT * iR * (ittT * tLT);
+      }
       dP = min_delta<D, G>(pL, pR, pLT, pRT);
       dRho = min_delta<D, G>(rhoL, rhoR, rhoLT, rhoRT);
       const G h = G(0.5);
