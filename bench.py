@@ -279,6 +279,39 @@ def cpu_oracle_rate(hf, cfg, target_s: float = 10.0, max_steps: int = 100, polic
     return hf.nc * steps / el, max_threads(), el, steps
 
 
+def cpu_baseline_grid(hf, cfg, workload: str, steps: int = 10):
+    """The CPU oracle in its FP64 policy for a fixed number of RK3 steps, on all host cores and on
+    one, on the benchmark mesh and on the 256 x 256 periodic isentropic vortex (the plain-FP64 small
+    case): cell-steps/s of each.  Threads are not pinned."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+    from oracle.oracle import Oracle, max_threads, set_threads
+
+    nproc = max_threads()
+    vm = mesh.periodic_quad_grid(256, 256, 0.0, 10.0, 0.0, 10.0)
+    vcfg = CaseConfig(stencilType="edgeNeighbour", CFL=0.5)
+    vhf = precompute(vm, vcfg, mesh.vortex_fields(vm.cell_centres()), None, want_rbf64=True)
+    if "RBFbasis64" not in hf.a:
+        return [{"unavailable": "the benchmark mesh was precomputed without FP64 weights"}]
+    out = []
+    try:
+        for name, h, c in (("vortex_256x256_periodic", vhf, vcfg), (workload, hf, cfg)):
+            for threads in sorted({nproc, 1}, reverse=True):
+                set_threads(threads)
+                o = Oracle(h, c.R, c.Cv, "fp64")
+                st = o.new_state()
+                o.evolve(st, o.delta_t(st["FD"], c.CFL))  # warm-up (first touch of the work arrays)
+                t0 = time.perf_counter()
+                for _ in range(steps):
+                    o.evolve(st, o.delta_t(st["FD"], c.CFL))
+                el = time.perf_counter() - t0
+                out.append({"mesh": name, "cells": h.nc, "policy": "fp64", "threads": threads, "steps": steps,
+                            "seconds": round(el, 3), "value": h.nc * steps / el, "unit": "cell-steps/s",
+                            "finite": bool(np.isfinite(st["FD"]).all())})
+    finally:
+        set_threads(nproc)
+    return out
+
+
 def run_reference_arm(args, dist: Dist):
     if dist.rank != 0:
         return
@@ -420,7 +453,9 @@ def run_ours(args, dist: Dist):
         rate, cores, el, cs = cpu_oracle_rate(hf, cfg)
         cpu = {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port",
                "sample": f"{cs} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle, ref policy, "
-                         f"{el:.1f} s"}
+                         f"{el:.1f} s",
+               "nproc": os.cpu_count(),
+               "fp64_fixed_steps": cpu_baseline_grid(hf, cfg, WORKLOADS[args.mesh][0])}
     if dist.rank == 0 and not args.no_reference_gpu:
         try:
             refgpu = reference_gpu_rate(hf, cfg, min(K, 50))
