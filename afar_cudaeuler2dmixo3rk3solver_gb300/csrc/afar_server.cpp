@@ -38,13 +38,17 @@ struct Request {
 };
 
 // Device memory of a solve before it is built: a per-cell, per-face model of the allocations
-// (state, intermediates, slot-major operator rows), by policy.
+// (state, intermediates, slot-major operator rows, the state snapshot, the residual dump and, for
+// mixed, the transfer staging), by policy.  The worker also scales it by the largest ratio of
+// built to estimated bytes seen so far, so admission never trusts a model that fell short.
 size_t estimate_bytes(const afar_fieldSizes& z, int policy) {
   const double nc = z.cellsNum, nf = z.facesNum, nb = z.totalBoundaryFacesNum;
   const double s = z.maxStencilSize, m = z.maxCompactStencilSize;
   const double w = policy == AFAR_POLICY_FP64 ? 8.0 : 4.0;  // operator word
   const double g = policy == AFAR_POLICY_MIXED ? 4.0 : 8.0; // state / intermediate word
-  const double per_cell = 4 * g + 64 + 8 * g + 4 * w + 2 + 4 * s + 4 * m + 8 * m * w + 2 * m * w + m * (s + 1) * w + 48;
+  const double snapshot = 4 * g + 64, res_dump = 32, staging = policy == AFAR_POLICY_MIXED ? 32 : 0;
+  const double per_cell = 4 * g + 64 + 8 * g + 4 * w + 2 + 4 * s + 4 * m + 8 * m * w + 2 * m * w + m * (s + 1) * w + 48 +
+                          snapshot + res_dump + staging;
   const double per_face = 8 * g + 4 * g + 48 + 16 + 8;
   return (size_t)(nc * per_cell + (nf + nb) * per_face + nb * 48 + (64u << 20));
 }
@@ -55,6 +59,7 @@ struct afar_server {
   int policy = AFAR_POLICY_MIXED;
   int device = 0;
   size_t budget = 0;
+  double est_scale = 1.0;  // largest built / estimated bytes so far (worker thread only)
   int chunk = 50;
   afar_batch* batch = nullptr;
   std::mutex mu;
@@ -127,7 +132,7 @@ struct afar_server {
         size_t used = st.bytesInUse;
         while (!queue.empty()) {
           Request* r = queue.front();
-          const size_t est = estimate_bytes(r->req.sizes, policy);
+          const size_t est = (size_t)(est_scale * (double)estimate_bytes(r->req.sizes, policy));
           if (!(running.empty() && admit.empty()) && used + est > budget) break;
           queue.pop_front();
           used += est;
@@ -136,6 +141,8 @@ struct afar_server {
       }
       for (Request* r : admit) {
         if (build(r)) {
+          const double est = (double)estimate_bytes(r->req.sizes, policy);
+          if (est > 0.0 && (double)r->bytes > est_scale * est) est_scale = (double)r->bytes / est;
           std::lock_guard<std::mutex> lock(mu);
           running.push_back(r);
           st.bytesInUse += r->bytes;

@@ -64,6 +64,26 @@ def test_server_results_match_alone(cases, policy):
     srv.close()
 
 
+def test_budget_holds_for_requests_that_fit(cases):
+    """With a budget of about two of the largest requests, the device memory of the running solves
+    never exceeds it (the admission model is conservative and calibrated by what was built)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver, Server
+
+    largest = 0
+    for n, _, _ in REQS:
+        probe = CudaSolver(*cases[n], policy="mixed")
+        largest = max(largest, probe.device_bytes())
+        probe.close()
+    budget = int(2.2 * largest)
+    srv = Server("mixed", hbm_budget_bytes=budget, chunk_steps=4)
+    ids = [srv.submit(*cases[n], t_end=t, n_steps=k) for n, t, k in REQS * 2]
+    for rid in ids:
+        assert srv.wait(rid, timeout=120.0) is not None
+    st = srv.stats()
+    assert st["completed"] == 2 * len(REQS) and st["peakBytes"] <= budget
+    srv.close()
+
+
 def test_budget_admits_one_at_a_time(cases):
     from afar_cudaeuler2dmixo3rk3solver_gb300 import Server
 
