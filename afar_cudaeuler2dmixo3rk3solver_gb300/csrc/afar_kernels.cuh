@@ -602,8 +602,10 @@ __device__ __forceinline__ void recon_staged_body(const StageArgs<P>& a, const i
   using S = typename P::S;
   using G = typename P::G;
   using WT = typename P::W;
+  // fp64 stages only the compact stencil (kCompact), ref the whole stencil
+  constexpr bool kCompact = P::id == PolicyFP64::id;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  V4<S>* sv = reinterpret_cast<V4<S>*>(smem_raw);  // [maxS][blockDim] staged stencil values
+  V4<S>* sv = reinterpret_cast<V4<S>*>(smem_raw);  // [maxM or maxS][blockDim] staged stencil values
   const int t = threadIdx.x, B = blockDim.x;
   const int c = blk * B + t;
   if (c >= a.Nc) return;
@@ -611,17 +613,34 @@ __device__ __forceinline__ void recon_staged_body(const StageArgs<P>& a, const i
   const int nS = a.nS[c], nM = a.nM[c];
   const V4<WT> wc = a.W[c];
   const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
-  constexpr int GB = 4;
-  for (int i0 = 0; i0 < nS; i0 += GB) {
-    int j[GB];
+  // fp64: only the compact stencil (the face neighbours, at most kMaxFaces) is staged: the
+  // gradient, the min/max and the uniform-cell test need nothing else, and only cells that are not
+  // uniform read the rest of the stencil, in their O3 loop.  32-byte values make whole-stencil
+  // staging the occupancy limit (3 blocks an SM); with it, 4.  The ref policy's 16-byte values
+  // leave room for the whole stencil, which its smooth-flow cells reuse across faces.
+  if constexpr (!kCompact) {
+    constexpr int GB = 4;
+    for (int i0 = 0; i0 < nS; i0 += GB) {
+      int j[GB];
 #pragma unroll
-    for (int u = 0; u < GB; ++u) j[u] = (i0 + u < nS) ? a.sten[(i0 + u) * ldc + c] : c;
-    V4<WT> wj[GB];
+      for (int u = 0; u < GB; ++u) j[u] = (i0 + u < nS) ? a.sten[(i0 + u) * ldc + c] : c;
+      V4<WT> wj[GB];
 #pragma unroll
-    for (int u = 0; u < GB; ++u) wj[u] = a.W[j[u]];
+      for (int u = 0; u < GB; ++u) wj[u] = a.W[j[u]];
 #pragma unroll
-    for (int u = 0; u < GB; ++u)
-      if (i0 + u < nS) sv[(i0 + u) * B + t] = V4<S>{(S)wj[u].x, (S)wj[u].y, (S)wj[u].z, (S)wj[u].w};
+      for (int u = 0; u < GB; ++u)
+        if (i0 + u < nS) sv[(i0 + u) * B + t] = V4<S>{(S)wj[u].x, (S)wj[u].y, (S)wj[u].z, (S)wj[u].w};
+    }
+  } else {
+    int j[kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) j[u] = u < nM ? a.sten[u * ldc + c] : c;
+    V4<WT> wj[kMaxFaces];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u) wj[u] = a.W[j[u]];
+#pragma unroll
+    for (int u = 0; u < kMaxFaces; ++u)
+      if (u < nM) sv[u * B + t] = V4<S>{(S)wj[u].x, (S)wj[u].y, (S)wj[u].z, (S)wj[u].w};
   }
 
   G gPx = 0, gPy = 0, gUxx = 0, gUxy = 0, gUyx = 0, gUyy = 0, gTx = 0, gTy = 0;
@@ -697,14 +716,43 @@ __device__ __forceinline__ void recon_staged_body(const StageArgs<P>& a, const i
       G uxf = wk * uxc;
       G uyf = wk * uyc;
       G tf = wk * tc;
-      for (int ci0 = 0; ci0 < nS; ci0 += 8) {  // weights in batches of eight; sums in stencil order
-        S wb[8];
+      // fp64: weights, stencil ids and the members past the compact stencil in batches of four
+      // (those from memory, the compact ones staged); ref: weights in batches of eight, every
+      // member staged.  Sums in stencil order either way.
+      if constexpr (!kCompact) {
+        for (int ci0 = 0; ci0 < nS; ci0 += 8) {
+          S wb[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) wb[u] = (ci0 + u < nS) ? w[(size_t)(ci0 + u + 1) * ldc] : S(0);
+          for (int u = 0; u < 8; ++u) wb[u] = (ci0 + u < nS) ? w[(size_t)(ci0 + u + 1) * ldc] : S(0);
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          if (ci0 + u < nS) {
-            const V4<S> v = sv[(ci0 + u) * B + t];
+          for (int u = 0; u < 8; ++u) {
+            if (ci0 + u < nS) {
+              const V4<S> v = sv[(ci0 + u) * B + t];
+              pf += wb[u] * v.x;
+              uxf += wb[u] * v.y;
+              uyf += wb[u] * v.z;
+              tf += wb[u] * v.w;
+            }
+          }
+        }
+      } else
+      for (int ci0 = 0; ci0 < nS; ci0 += 4) {
+        S wb[4];
+        int jj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int ci = ci0 + u;
+          wb[u] = ci < nS ? w[(size_t)(ci + 1) * ldc] : S(0);
+          jj[u] = (ci < nS && ci >= nM) ? a.sten[ci * ldc + c] : c;
+        }
+        V4<WT> wv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) wv[u] = a.W[jj[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int ci = ci0 + u;
+          if (ci < nS) {
+            const V4<S> v = ci < nM ? sv[ci * B + t] : V4<S>{(S)wv[u].x, (S)wv[u].y, (S)wv[u].z, (S)wv[u].w};
             pf += wb[u] * v.x;
             uxf += wb[u] * v.y;
             uyf += wb[u] * v.z;
@@ -1554,6 +1602,11 @@ template <class P>
 __global__ void __launch_bounds__(128) k_reconstruct_staged(StageArgs<P> a) {
   recon_staged_body<P>(a, blockIdx.x);
 }
+// fp64: its compact staging leaves room for 4 blocks an SM, which 128 registers a thread allow
+template <>
+__global__ void __launch_bounds__(128, 4) k_reconstruct_staged<PolicyFP64>(StageArgs<PolicyFP64> a) {
+  recon_staged_body<PolicyFP64>(a, blockIdx.x);
+}
 template <class P>
 __global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
   bvd_body<P>(a, blockIdx.x);
@@ -1584,6 +1637,12 @@ __global__ void __launch_bounds__(128) kb_reconstruct_staged(const StageArgs<P>*
                                                              const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
   recon_staged_body<P>(tab[m.x], m.y);
+}
+template <>
+__global__ void __launch_bounds__(128, 4) kb_reconstruct_staged<PolicyFP64>(const StageArgs<PolicyFP64>* __restrict__ tab,
+                                                                            const int2* __restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  recon_staged_body<PolicyFP64>(tab[m.x], m.y);
 }
 template <class P>
 // mixed: 32 registers, 16 blocks (the full 64 warps) per SM for this gather-bound kernel

@@ -329,11 +329,12 @@ afar_status raise_smem_limit(K kernel, int device, size_t bytes) {
 }
 
 // Dynamic shared memory of the reconstruct: the mixed policy stages a whole 128-cell tile of
-// operator rows (recon_tile_layout); the FP64-bound policies stage the stencil values.
+// operator rows (recon_tile_layout); ref stages the stencil values, fp64 the compact stencil's.
 template <class P>
 size_t recon_smem(const afar_solver* s) {
   if constexpr (P::id == PolicyMixed::id) return recon_tile_layout(s->maxM, s->maxS).bytes;
-  return (size_t)(s->maxS > 0 ? s->maxS : 1) * kCellBlock * sizeof(V4<typename P::S>);
+  const int rows = P::id == PolicyFP64::id ? s->maxM : s->maxS;  // fp64 stages the compact stencil only
+  return (size_t)(rows > 0 ? rows : 1) * kCellBlock * sizeof(V4<typename P::S>);
 }
 
 // One solve's stage launches, arguments by value.  The ref policy reconstructs in the staged
