@@ -24,7 +24,10 @@ static __device__ __align__(256) double g_noalloc_block_min[kNoallocMaxBlocks];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
-double* g_scratch[kMaxDevices] = {};  // device address of g_noalloc_block_min, per device
+// Device address of g_noalloc_block_min, per device, resolved by the first call on that device and
+// kept for the life of the process (a cudaDeviceReset, which reloads this file's device code, is not
+// supported after that first call).
+double* g_scratch[kMaxDevices] = {};
 
 // setDeltaT of the reference (cudaFieldOperation.h:124-180) on the reference layout; one minimum
 // per block into the scratch array.
@@ -37,7 +40,7 @@ __global__ void __launch_bounds__(kNoallocBlock) k_noalloc_block_min(const afar_
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   double dt = 1e5;
   if (f < nf) {
-    const int own = neighbour[2 * f], nei = neighbour[2 * f + 1];
+    const int own = neighbour[2 * f], nei = neighbour[2 * f + 1];  // in [0, Nc+Nb): the caller's guarantee
     const double deltaR = hypot(CELL[nei].x - CELL[own].x, CELL[nei].y - CELL[own].y);
     const double fraction = hypot(FACE[f].x - CELL[own].x, FACE[f].y - CELL[own].y) / deltaR;
     const double Sfx = FACE[f].Sfx, Sfy = FACE[f].Sfy, magSf = FACE[f].magSf;

@@ -408,17 +408,25 @@ afar_status afar_download_ls_matrix(afar_solver* solver, float* matrix);
 /* The Courant time step of a state the caller already holds on the device, for callers that
  * cannot allocate device memory (an application that hands out all GPU memory from its own pool,
  * or has reserved its device memory budget up front, and forbids libraries to allocate).  It has
- * no counterpart in the reference; it computes what adjustTimeStep does (min over internal faces
- * and 1e5) and allocates nothing: no cudaMalloc, no cudaFree, no allocating library call.
+ * no counterpart in the reference; it computes the reference's setDeltaT in FP64 (min over
+ * internal faces and 1e5), which is what afar_adjustTimeStep returns under the fp64 and ref
+ * policies; the mixed policy's afar_adjustTimeStep returns an FP32 estimate of the same minimum,
+ * which differs from this one by rounding.  It allocates nothing: no cudaMalloc, no cudaFree, no
+ * allocating library call.
  *   FD, CELL, FACE, neighbour: device pointers to the reference-layout arrays (Nc+Nb, Nc+Nb,
  *     Nf+Nb and 2*Nf entries); deltaT: device pointer to one double, written in stream order;
  *   stream: a cudaStream_t, or NULL for the default stream.  Returns once the work is enqueued.
+ * The owner and neighbour ids are read on the device and not checked: every entry of neighbour
+ * must lie in [0, Nc+Nb), or the kernel reads out of bounds (checking them would need a copy to
+ * the host, which this entry point exists to avoid).
  * Limit: facesNum <= 16,777,216 (a fixed scratch of 65,536 per-block minima, 512 KiB, in a static
  * device array that every GPU which loads the library holds until the process exits); larger
  * meshes get AFAR_ERR_LIMIT.  Each call overwrites the scratch entries it reads, so nothing needs
  * clearing; all calls share the scratch, so calls that overlap on the GPU race.  The first call on
- * a device resolves the scratch address on that device (cudaGetSymbolAddress); make that first call
- * before any stream capture. */
+ * a device resolves the scratch address on that device (cudaGetSymbolAddress) and keeps it for
+ * the life of the process; make that first call before any stream capture.  A cudaDeviceReset
+ * after that first call is not supported: the reset reloads the library's device code, the array
+ * may move, and later calls would still use the address resolved before. */
 afar_status afar_adjustTimeStep_noalloc(const afar_basicFieldData* FD, const afar_meshCellData* CELL,
                                         const afar_meshFaceData* FACE, const int* neighbour,
                                         int facesNum, double R, double Cv, double CFL,

@@ -7,6 +7,7 @@ import pytest
 
 from conftest import ROOT
 from foam_case import write_case
+from oracle.reference_dir import reference_dir
 
 
 def test_parse_dictionary_forms():
@@ -82,7 +83,7 @@ def test_writers_round_trip(tmp_path):
     assert "defaultFaces" in open(os.path.join(poly, "boundary")).read() and faces is not None
 
 
-REF_CASE = "/root/reference/simulation/cornerFlow/cornerFlow_cuda"
+REF_CASE = os.path.join(reference_dir(), "simulation", "cornerFlow", "cornerFlow_cuda")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="the reference's case files are not on this machine")

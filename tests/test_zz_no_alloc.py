@@ -11,6 +11,8 @@ from conftest import gpu_available, small_cases
 
 pytestmark = pytest.mark.gpu
 
+BLOCK = 256  # faces per block minimum in the entry point's scratch
+
 
 def test_noalloc_courant_step_matches_adjust_time_step_on_two_calls():
     if not gpu_available():
@@ -21,11 +23,15 @@ def test_noalloc_courant_step_matches_adjust_time_step_on_two_calls():
 
     L = _ffi.lib()
     cases = small_cases()
-    # two calls in a row; the second mesh is smaller, so it must not see the first call's scratch
-    for name in ("mixed_riemann", "quad_riemann"):
+    # two calls in a row; the second mesh has fewer blocks of faces than the first, so it reads only
+    # scratch entries the first call also wrote, and must not see that call's minima
+    names = ("mixed_riemann", "quad_riemann")
+    nblocks = []
+    for i, name in enumerate(names):
         m, W, Wb, st = cases[name]
         cfg = CaseConfig(stencilType=st)
         hf = precompute(m, cfg, W, Wb)
+        nblocks.append((hf.nf + BLOCK - 1) // BLOCK)
         s = CudaSolver(hf, cfg, policy="ref")
         s.run(3)  # a non-uniform state
         FD = s.state()["FD"]
@@ -38,11 +44,18 @@ def test_noalloc_courant_step_matches_adjust_time_step_on_two_calls():
         FD_d, CELL_d, FACE_d, NB_d = dev(FD), dev(hf.CELL), dev(hf.FACE), dev(hf.neighbour)
         out = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
         _ffi.check(L.afar_adjustTimeStep_noalloc(FD_d.data_ptr(), CELL_d.data_ptr(), FACE_d.data_ptr(),
                                                  NB_d.data_ptr(), hf.nf, cfg.R, cfg.Cv, cfg.CFL, out.data_ptr(), None))
         torch.cuda.synchronize()
+        free1 = torch.cuda.mem_get_info()[0]
         got = out.item()
         assert got == pytest.approx(expected, rel=1e-15, abs=0), (name, got, expected)
+        if i > 0:
+            # the first call on a device may load this file's device code (with its static scratch
+            # array) once; every later call must leave the device's free memory as it found it
+            assert free1 == free0, f"free device memory changed by {free0 - free1} bytes over the call"
+    assert nblocks[1] < nblocks[0], nblocks
 
 
 def test_noalloc_rejects_meshes_beyond_its_scratch():
