@@ -55,6 +55,7 @@ def build_lib(force=False, verbose=False) -> str:
     units = [
         ("afar_solver.cu", "nvcc"),
         ("afar_noalloc.cu", "nvcc"),
+        ("afar_peak.cu", "nvcc"),
         ("afar_precompute_gpu.cu", "nvcc_nofma"),
         ("afar_precompute.cpp", "cxx"),
         ("afar_error.cpp", "cxx"),

@@ -43,6 +43,14 @@ PROFILE_STEPS = 10
 # workload (traffic grows with the cells of the tile stream); None when no capture matches the
 # current kernels.
 RECON_TRAFFIC_BYTES_PER_CELL = {"rcm": 399.1, "hilbert": 398.5}
+# FP64 work per internal face of the fp64 policy's flux, averaged over a step's three launches (the
+# first also reduces the Courant step), from the ncu instruction counts
+# smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of the three launches on the
+# 500,094-cell version of this workload (748,881 internal faces): instructions (DFMA + DADD + DMUL,
+# divisions and square roots counted as the DFMA sequences they run as) and floating-point
+# operations (2 per DFMA).  The FP64 pipe issues one such instruction per lane per cycle at its peak.
+FP64_FLUX_INST_PER_FACE = 243.77
+FP64_FLUX_FLOPS_PER_FACE = 360.17
 
 
 def parse():
@@ -58,6 +66,9 @@ def parse():
     ap.add_argument("--policies", default="mixed,fp64,ref")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the mixed-vs-FP64 accuracy pass of the main line")
+    ap.add_argument("--floor-in-bench", action="store_true",
+                    help="main line: also the FP64 policy against itself from a 1-ulp perturbed start")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--mesh", default="step", choices=["step", "riemann_mixed", "vortex"],
                     help="step: the metric's workload; riemann_mixed: the 4M-cell mixed quad/triangle case; "
@@ -81,6 +92,14 @@ def parse():
                          "(comma-separated: vortex, step, riemann_mixed, batch), L1/Linf of density and switch flips")
     ap.add_argument("--acc-steps", type=int, default=100, help="--accuracy step: RK3 steps of the Mach 3 start")
     ap.add_argument("--acc-sample", type=int, default=8, help="--accuracy batch: solves of the batch re-run")
+    ap.add_argument("--floor", action="store_true",
+                    help="--accuracy: also the FP64 policy against itself, on the same mesh in another cell order "
+                         "(Hilbert curve instead of RCM: another summation order) and from a 1-ulp perturbed start")
+    ap.add_argument("--cache-mesh", default="", help=argparse.SUPPRESS)  # helper: build the workload, save it
+    ap.add_argument("--cpu-sample", default="", help=argparse.SUPPRESS)  # helper: time the oracle on a saved mesh
+    ap.add_argument("--cpu-policy", default="ref", help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-threads", type=int, default=0, help=argparse.SUPPRESS)
+    ap.add_argument("--sample-steps", type=int, default=5, help=argparse.SUPPRESS)
     ap.add_argument("--serve-requests", type=int, default=60)
     ap.add_argument("--serve-rate", type=float, default=50.0, help="arrivals per second")
     return ap.parse_args()
@@ -266,83 +285,149 @@ def peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-# ------------------------------------------------------------------------------------ arms
-def cpu_oracle_rate(hf, cfg, target_s: float = 10.0, max_steps: int = 100, policy="ref"):
-    """The oracle (the reference's algorithm restated in C) on all host cores: cell-steps/s over a
-    bounded sample of about target_s seconds (whole RK3 steps of the full mesh; at most max_steps,
-    well inside the ~180 steps this start-up runs before its corner breaks down at CFL 0.2)."""
-    from oracle.oracle import Oracle, max_threads
-
-    o = Oracle(hf, cfg.R, cfg.Cv, policy)
-    st = o.new_state()
-    dt = o.delta_t(st["FD"], cfg.CFL)
-    tw = time.perf_counter()
-    o.evolve(st, dt)  # warm-up (first touch of the work arrays)
-    tw = time.perf_counter() - tw
-    steps = int(max(2, min(max_steps, round(target_s / max(tw, 1e-3)))))
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        dt = o.delta_t(st["FD"], cfg.CFL)
-        o.evolve(st, dt)
-    el = time.perf_counter() - t0
-    return hf.nc * steps / el, max_threads(), el, steps
+# ------------------------------------------------------------------------------------ CPU legs
+# The CPU baseline and the reference arm time the oracle (the reference's algorithm restated in C,
+# OpenMP) in a process of its own: threads pinned (OMP_PROC_BIND=close, OMP_PLACES=cores) and counted,
+# on the workload's mesh saved by another helper process.  So the timing process maps the oracle's
+# library only, and both legs measure the same thing the same way.
+CPU_SAMPLE_RK3 = 5  # RK3 steps of the full mesh per timed CPU "step" (a bounded sample)
 
 
-def cpu_baseline_grid(hf, cfg, workload: str, steps: int = 10):
-    """The CPU oracle in its FP64 policy for a fixed number of RK3 steps, on all host cores and on
-    one, on the benchmark mesh and on the 256 x 256 periodic isentropic vortex (the plain-FP64 small
-    case): cell-steps/s of each.  Threads are not pinned."""
-    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+def cpu_samples(steps: int, warmup: int):
+    """Timed and warm-up CPU samples for a run of `steps` timed / `warmup` warm-up steps: the same
+    counts, capped at 20 and 3 so the whole CPU leg stays within ~25 s and its 115 RK3 steps stay
+    inside the ~180 this impulsive start runs before breaking down at the step corner."""
+    return max(1, min(steps, 20)), max(1, min(warmup, 3))
+
+
+def save_workload(hf, cfg, path: str):
+    hf.save(path)
+    with open(path + ".json", "w") as f:
+        json.dump({"R": cfg.R, "Cv": cfg.Cv, "CFL": cfg.CFL}, f)
+
+
+def cached_workload_subprocess(args, path: str):
+    """Builds the workload's mesh and precompute in a helper process (it maps libafar) and saves it."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--cache-mesh", path, "--points", str(args.points),
+           "--seed", str(args.seed), "--cfl", str(args.cfl), "--mesh", args.mesh, "--mixed-n", str(args.mixed_n),
+           "--order", args.order]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("workload helper failed: " + r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def run_cache_mesh(args):
+    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n, args.order)
+    save_workload(hf, cfg, args.cache_mesh)
+    print(json.dumps({"cells": hf.nc, "internal_faces": hf.nf, "boundary_faces": hf.nb, "setup_s": setup_s}))
+
+
+def cpu_rate_subprocess(path: str, threads: int, policy: str, samples: int, warmup: int,
+                        sample_steps: int = CPU_SAMPLE_RK3):
+    """The oracle timed in a pinned process of its own (see run_cpu_sample)."""
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads), OMP_PROC_BIND="close", OMP_PLACES="cores")
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-sample", path, "--cpu-threads", str(threads),
+           "--cpu-policy", policy, "--steps", str(samples), "--warmup", str(warmup), "--sample-steps",
+           str(sample_steps)]
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env)
+    if r.returncode != 0:
+        raise RuntimeError("CPU sample failed: " + r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def run_cpu_sample(args):
+    """Times the oracle on a saved mesh: `warmup` untimed then `steps` timed samples of sample_steps
+    whole RK3 steps each (Courant step from the state each step); prints cell-steps/s."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300.solver import HostFields
     from oracle.oracle import Oracle, max_threads, set_threads
 
-    nproc = max_threads()
-    vm = mesh.periodic_quad_grid(256, 256, 0.0, 10.0, 0.0, 10.0)
-    vcfg = CaseConfig(stencilType="edgeNeighbour", CFL=0.5)
-    vhf = precompute(vm, vcfg, mesh.vortex_fields(vm.cell_centres()), None, want_rbf64=True)
-    if "RBFbasis64" not in hf.a:
-        return [{"unavailable": "the benchmark mesh was precomputed without FP64 weights"}]
+    hf = HostFields.load(args.cpu_sample)
+    with open(args.cpu_sample + ".json") as f:
+        gas = json.load(f)
+    if args.cpu_threads > 0:
+        set_threads(args.cpu_threads)
+    o = Oracle(hf, gas["R"], gas["Cv"], args.cpu_policy)
+    st = o.new_state()
+    n = args.sample_steps
+
+    def sample():
+        for _ in range(n):
+            o.evolve(st, o.delta_t(st["FD"], gas["CFL"]))
+
+    for _ in range(args.warmup):
+        sample()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sample()
+    el = time.perf_counter() - t0
+    W_ = st["FD"][:hf.nc]
+    print(json.dumps({"value": hf.nc * n * args.steps / el, "unit": "cell-steps/s", "seconds": el,
+                      "samples": args.steps, "warmup_samples": args.warmup, "rk3_steps_per_sample": n,
+                      "threads": max_threads(), "policy": args.cpu_policy, "cells": hf.nc,
+                      "pinning": "OMP_PROC_BIND=close OMP_PLACES=cores",
+                      "affinity_cores": len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else None,
+                      "finite": bool(np.isfinite(st["cFD"]).all() and (W_[:, 0] > 0).all())}))
+
+
+def cpu_leg(path: str, samples: int, warmup: int, policy: str = "ref"):
+    """The CPU baseline of a saved workload on all host cores, pinned (the reference arm's measure)."""
+    nproc = os.cpu_count() or 1
+    r = cpu_rate_subprocess(path, nproc, policy, samples, warmup)
+    r["sample"] = (f"{r['samples']} samples of {r['rk3_steps_per_sample']} full RK3 steps (after "
+                   f"{r['warmup_samples']} warm-up samples) of the {r['cells']}-cell mesh, CPU oracle ({policy} "
+                   f"policy), {r['threads']} threads pinned, {r['seconds']:.1f} s")
+    return r
+
+
+def cpu_baseline_grid(path: str, workload: str, vortex_path: str, steps: int = 10):
+    """The CPU oracle in its FP64 policy for a fixed number of RK3 steps, on all host cores and on
+    one (pinned), on the benchmark mesh and on the 256 x 256 periodic isentropic vortex (the
+    plain-FP64 small case): cell-steps/s of each."""
+    nproc = os.cpu_count() or 1
     out = []
-    try:
-        for name, h, c in (("vortex_256x256_periodic", vhf, vcfg), (workload, hf, cfg)):
-            for threads in sorted({nproc, 1}, reverse=True):
-                set_threads(threads)
-                o = Oracle(h, c.R, c.Cv, "fp64")
-                st = o.new_state()
-                o.evolve(st, o.delta_t(st["FD"], c.CFL))  # warm-up (first touch of the work arrays)
-                t0 = time.perf_counter()
-                for _ in range(steps):
-                    o.evolve(st, o.delta_t(st["FD"], c.CFL))
-                el = time.perf_counter() - t0
-                out.append({"mesh": name, "cells": h.nc, "policy": "fp64", "threads": threads, "steps": steps,
-                            "seconds": round(el, 3), "value": h.nc * steps / el, "unit": "cell-steps/s",
-                            "finite": bool(np.isfinite(st["FD"]).all())})
-    finally:
-        set_threads(nproc)
+    for name, p in (("vortex_256x256_periodic", vortex_path), (workload, path)):
+        for threads in sorted({nproc, 1}, reverse=True):
+            r = cpu_rate_subprocess(p, threads, "fp64", 1, 1, sample_steps=steps)
+            out.append({"mesh": name, "cells": r["cells"], "policy": "fp64", "threads": r["threads"], "steps": steps,
+                        "seconds": round(r["seconds"], 3), "value": r["value"], "unit": "cell-steps/s",
+                        "pinning": r["pinning"], "finite": r["finite"]})
     return out
 
 
 def run_reference_arm(args, dist: Dist):
+    """The reference arm: the reference has no CPU implementation of this path, so this times its
+    algorithm restated in C (the oracle, ref policy) on all host cores, pinned.  The mesh comes from
+    a helper process; this process maps neither libafar nor the oracle."""
     if dist.rank != 0:
         return
-    from afar_cudaeuler2dmixo3rk3solver_gb300 import build as b
+    import shutil
+    import tempfile
 
-    b.build_all()
-    m, hf, cfg, setup_s = make_workload(args.points, args.seed, args.cfl, args.mesh, args.mixed_n, args.order)
-    rate, cores, el, steps = cpu_oracle_rate(hf, cfg, target_s=20.0, max_steps=min(120, max(2, args.steps)))
-    sample = (f"{steps} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle (ref policy), "
-              f"{el:.1f} s")
+    tmp = tempfile.mkdtemp(prefix="afar_bench_")
+    try:
+        path = os.path.join(tmp, "workload.npz")
+        info = cached_workload_subprocess(args, path)
+        K, W = cpu_samples(args.steps, args.warmup)
+        r = cpu_leg(path, K, W)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    rate = r["value"]
     line = {
-        "metric": METRIC, "value": rate, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": steps,
-        "warmup": 1, "ms_per_step": el / steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64", "data": WORKLOADS[args.mesh][1],
+        "metric": METRIC, "value": rate, "unit": "cell-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["seconds"] / r["samples"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": WORKLOADS[args.mesh][1],
         "impl": "reference",
-        "config": {"workload": WORKLOADS[args.mesh][0], "cells": hf.nc, "internal_faces": hf.nf,
-                   "boundary_faces": hf.nb, "points": args.points, "cfl": args.cfl, "stencil": "edgeNeighbour",
-                   "cell_order": args.order, "parallelism": "replicas"},
-        "cpu_baseline": {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "config": {"workload": WORKLOADS[args.mesh][0], "cells": info["cells"], "internal_faces": info["internal_faces"],
+                   "boundary_faces": info["boundary_faces"], "points": args.points, "cfl": args.cfl,
+                   "stencil": "edgeNeighbour", "cell_order": args.order, "parallelism": "replicas",
+                   "step": f"one step = a sample of {CPU_SAMPLE_RK3} full RK3 steps of the mesh; "
+                           f"{r['samples']} timed after {r['warmup_samples']} warm-up samples"},
+        "cpu_baseline": {"value": rate, "unit": "cell-steps/s", "cores": r["threads"], "kind": "port",
+                         "sample": r["sample"], "pinning": r["pinning"]},
         "e2e": {"value": rate, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference has no CPU implementation of the path; this is its algorithm restated in C "
-                "(oracle/afar_oracle.c), OpenMP over all host threads",
+                "(oracle/afar_oracle.c), OpenMP over all host threads, pinned",
     }
     print(json.dumps(line), flush=True)
 
@@ -456,15 +541,51 @@ def run_ours(args, dist: Dist):
     h2d = (FD_h.nbytes + cFD_h.nbytes) * len(chunks) / K + 24  # cFDold is cFD: copied on the device
     d2h = (out_FD.nbytes + out_si.nbytes) * len(chunks) / K + 8
 
+    # accuracy of the timed (first) policy against the FP64 policy on this mesh, over the steps a timed
+    # chunk covers from the start (warm-up + chunk), stepped side by side with the FP64 Courant step
+    accuracy = None
+    if pol0 == "mixed" and not args.no_accuracy:
+        nacc = Wm + max(chunks)
+        accuracy, _, _ = accuracy_pair(hf, cfg, device, n_steps=nacc, every=max(1, nacc // 5))
+        accuracy["what"] = (f"mixed against the FP64 policy after {nacc} RK3 steps from the workload's start (the "
+                            f"{Wm} warm-up steps and a timed chunk), same step sizes; area-weighted L1 and L-inf of "
+                            f"density, cells whose final switch differs")
+        if args.floor_in_bench:
+            accuracy["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, device, n_steps=nacc)
+    fp64_peak = None
+    if "fp64" in policies:
+        try:
+            gf, pms = C.c_double(), C.c_float()
+            _ffi.check(L.afar_measure_fp64_peak(device, C.byref(gf), C.byref(pms)))
+            fp64_peak = {"gflops": gf.value, "launch_ms": pms.value,
+                         "method": "independent DFMA chains on every SM, CUDA events, best of 5 (afar_measure_fp64_peak)"}
+        except Exception as e:  # report, do not fail the bench
+            fp64_peak = {"unavailable": str(e)[:200]}
+
     cpu = None
     refgpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
-        rate, cores, el, cs = cpu_oracle_rate(hf, cfg)
-        cpu = {"value": rate, "unit": "cell-steps/s", "cores": cores, "kind": "port",
-               "sample": f"{cs} full RK3 steps (after 1 warm-up) of the {hf.nc}-cell mesh, CPU oracle, ref policy, "
-                         f"{el:.1f} s",
-               "nproc": os.cpu_count(),
-               "fp64_fixed_steps": cpu_baseline_grid(hf, cfg, WORKLOADS[args.mesh][0])}
+        import shutil
+        import tempfile
+
+        from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh, precompute
+
+        tmp = tempfile.mkdtemp(prefix="afar_bench_")
+        try:
+            path = os.path.join(tmp, "workload.npz")
+            save_workload(hf, cfg, path)
+            vm = mesh.periodic_quad_grid(256, 256, 0.0, 10.0, 0.0, 10.0)
+            vcfg = CaseConfig(stencilType="edgeNeighbour", CFL=0.5)
+            vpath = os.path.join(tmp, "vortex.npz")
+            save_workload(precompute(vm, vcfg, mesh.vortex_fields(vm.cell_centres()), None, want_rbf64=True), vcfg,
+                          vpath)
+            Kc, Wc = cpu_samples(K, args.warmup)
+            r = cpu_leg(path, Kc, Wc)
+            cpu = {"value": r["value"], "unit": "cell-steps/s", "cores": r["threads"], "kind": "port",
+                   "sample": r["sample"], "pinning": r["pinning"], "nproc": os.cpu_count(),
+                   "fp64_fixed_steps": cpu_baseline_grid(path, WORKLOADS[args.mesh][0], vpath)}
+        finally:
+            shutil.rmtree(tmp, ignore_errors=True)
     if dist.rank == 0 and not args.no_reference_gpu:
         try:
             refgpu = reference_gpu_rate(hf, cfg, min(K, 50))
@@ -501,9 +622,29 @@ def run_ours(args, dist: Dist):
         by_policy[pol] = {
             "value": hf.nc * K / (r["ms"] * 1e-3), "ms_per_step": r["ms"] / K, "finite": r["finite"],
             "algorithmic_GBps": b_s / (r["ms"] / K * 1e-3) / 1e9, "bytes_per_cell_step": b_s / hf.nc,
+            "hbm_frac": b_s / (r["ms"] / K * 1e-3) / 1e9 / hbm,
             "kernels_ms_per_step": r["kernels_ms"], "launches_per_step": r["launches"],
             "device_bytes": r["device_bytes"], "switch_counts": r["switch_counts"],
         }
+    if "fp64" in by_policy and fp64_peak and "gflops" in fp64_peak:
+        # the fp64 policy's flux is bound by the FP64 pipe: its FP64 instructions per launch (the ncu
+        # counts per face above) over its CUDA-event launch time, against the measured DFMA issue rate
+        flux_ms = results["fp64"]["kernels_ms"]["flux"] / 3.0
+        inst = FP64_FLUX_INST_PER_FACE * hf.nf
+        flops = FP64_FLUX_FLOPS_PER_FACE * hf.nf
+        peak_inst = fp64_peak["gflops"] / 2.0  # DFMA instructions per second (G)
+        by_policy["fp64"]["fp64_roofline"] = {
+            "bound": "fp64 pipe", "kernel": "flux (fp64)", "peak_gflops": fp64_peak["gflops"],
+            "peak_method": fp64_peak["method"], "launch_ms": flux_ms,
+            "fp64_inst_per_face": FP64_FLUX_INST_PER_FACE, "fp64_flops_per_face": FP64_FLUX_FLOPS_PER_FACE,
+            "achieved_ginst_per_s": inst / (flux_ms * 1e-3) / 1e9,
+            "frac": inst / (flux_ms * 1e-3) / 1e9 / peak_inst,
+            "achieved_gflops": flops / (flux_ms * 1e-3) / 1e9,
+            "flops_frac": flops / (flux_ms * 1e-3) / 1e9 / fp64_peak["gflops"],
+            "frac_is": "FP64 instructions issued per second over the peak DFMA issue rate (the pipe's occupancy); "
+                       "flops_frac counts DADD and DMUL as one operation against the DFMA's two",
+            "note": "hbm_frac is the whole fp64 step's algorithmic bytes over the HBM peak; its flux and update "
+                    "are bound by the FP64 pipe, not by memory"}
     line = {
         "metric": METRIC, "value": value, "unit": "cell-steps/s", "n_gpus": n, "steps": K, "warmup": Wm,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -529,6 +670,7 @@ def run_ours(args, dist: Dist):
                 "d2h_bytes_per_step": int(d2h), "finite": e2e_finite,
                 "path": "per chunk: afar_upload_state (pinned host), n x (afar_adjustTimeStep + afar_GPUevolve), "
                         "afar_copyFieldDataDeviceToHost"},
+        "accuracy": accuracy,
         "policies": by_policy,
         "cpu_baseline": cpu,
         "reference_gpu": refgpu,
@@ -693,6 +835,98 @@ def accuracy_pair(hf, cfg, device, t_end=0.0, n_steps=0, every=10, init=None):
     return out, a, b
 
 
+def fp64_perturbation_floor(hf, cfg, device, n_steps=0, t_end=0.0, every=10, init=None, seed=1):
+    """The FP64 policy against itself from a start perturbed by one unit in the last place (each
+    stored double moved up or down one ulp at random), with the same step sizes: how far rounding
+    alone carries two FP64 solves apart on this configuration (the floor under any mixed-precision
+    form's difference from FP64)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver
+
+    a = CudaSolver(hf, cfg, policy="fp64", device=device)
+    b = CudaSolver(hf, cfg, policy="fp64", device=device)
+    FD0, U0 = (hf.FD, hf.cFD) if init is None else (np.concatenate([init[0], hf.FD[hf.nc:]]), init[1])
+    rng = np.random.default_rng(seed)
+
+    def ulp_nudge(x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        return np.where(rng.integers(0, 2, x.shape) == 1, np.nextafter(x, np.inf), np.nextafter(x, -np.inf))
+
+    a.upload_state(FD=FD0, cFD=U0, cFDold=U0)
+    Up = ulp_nudge(U0)
+    FDp = np.array(FD0, dtype=np.float64, copy=True)
+    FDp[:hf.nc] = ulp_nudge(FDp[:hf.nc])
+    b.upload_state(FD=FDp, cFD=Up, cFDold=Up)
+    t, k, worst = 0.0, 0, 0.0
+    while (n_steps and k < n_steps) or (not n_steps and t < t_end * (1.0 - 1e-12)):
+        dt = a.set_delta_t()
+        if t_end > 0.0:
+            dt = min(dt, t_end - t)
+        a.evolve(dt)
+        b.evolve(dt)
+        t += dt
+        k += 1
+        if k % every == 0:
+            worst = max(worst, compare_policies(hf, a.state(), b.state())["L1_rho"])
+    out = compare_policies(hf, a.state(), b.state())
+    out.update({"steps": k, "max_L1_rho_over_run": max(worst, out["L1_rho"]),
+                "what": "FP64 policy vs itself from a start perturbed by 1 ulp per stored value, same step sizes"})
+    a.close()
+    b.close()
+    return out
+
+
+def fp64_reorder_floor(m, make_fields, cfg, device, n_steps=0, t_end=0.0, every=10):
+    """The FP64 policy against itself on the same mesh with its cells in another order (reverse
+    Cuthill-McKee as generated, and along a Hilbert curve): the face and stencil lists, and so every
+    summation, follow the numbering, and the O3 weights are solved with the stencil rows permuted.
+    Both solves take the first one's step sizes; the states are compared cell for cell (matched by
+    centroid).  make_fields(mesh) -> (W, Wb, U or None)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver, mesh, precompute
+
+    m2 = mesh.renumber_mesh(m, "hilbert")
+    c1, c2 = m.cell_centres(), m2.cell_centres()
+    o1, o2 = np.lexsort((c1[:, 1], c1[:, 0])), np.lexsort((c2[:, 1], c2[:, 0]))
+    to2 = np.empty(m.n_cells, dtype=np.int64)
+    to2[o1] = o2  # cell i of m is cell to2[i] of m2
+    assert np.array_equal(c1, c2[to2]), "cell centroids do not match between the two orders"
+    solvers, hfs = [], []
+    for mm in (m, m2):
+        W, Wb, U = make_fields(mm)
+        hf = precompute(mm, cfg, W, Wb, want_rbf64=True, device=device)
+        s = CudaSolver(hf, cfg, policy="fp64", device=device)
+        if U is not None:
+            s.upload_state(FD=np.concatenate([W, hf.FD[hf.nc:]]), cFD=U, cFDold=U)
+        solvers.append(s)
+        hfs.append(hf)
+    a, b = solvers
+
+    def cmp():
+        sa, sb = a.state(), b.state()
+        si = sb["shockIndicator"]
+        sb = {"cFD": sb["cFD"][to2],
+              "shockIndicator": np.stack([si[0:2 * hfs[1].nc:2][to2], si[1:2 * hfs[1].nc:2][to2]], axis=1).reshape(-1)}
+        return compare_policies(hfs[0], sa, sb)
+
+    t, k, worst = 0.0, 0, 0.0
+    while (n_steps and k < n_steps) or (not n_steps and t < t_end * (1.0 - 1e-12)):
+        dt = a.set_delta_t()
+        if t_end > 0.0:
+            dt = min(dt, t_end - t)
+        a.evolve(dt)
+        b.evolve(dt)
+        t += dt
+        k += 1
+        if k % every == 0:
+            worst = max(worst, cmp()["L1_rho"])
+    out = cmp()
+    out.update({"steps": k, "t": t, "max_L1_rho_over_run": max(worst, out["L1_rho"]),
+                "what": "FP64 policy vs itself, cells in RCM vs Hilbert-curve order (other summation orders), "
+                        "same step sizes"})
+    a.close()
+    b.close()
+    return out
+
+
 def run_accuracy(args, dist: Dist):
     """Accuracy of the mixed policy against the FP64 policy, per config: the periodic isentropic
     vortex (256^2 quads on [0,10]^2, CFL 0.5, to t = 2; also against the exact solution), the
@@ -722,18 +956,34 @@ def run_accuracy(args, dist: Dist):
             area = m.cell_areas()
             r["L1_rho_vs_exact"] = {p: float(np.sum(np.abs(s_["cFD"][:, 0] - exact) * area) / area.sum())
                                     for p, s_ in (("fp64", a), ("mixed", bb))}
+
+            def fields(mm):
+                U = mesh.vortex_cell_averages(mm, gauss_quadrature(mm, cfg), 0.0, centre=(5.0, 5.0))
+                return mesh.primitive_from_conserved(U), None, U
+
+            run, init = {"t_end": 2.0, "every": 25}, (W0, U0)
         elif name == "step":
             m = mesh.forward_step_triangles(args.points, seed=args.seed)
             W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
             cfg = CaseConfig(stencilType="edgeNeighbour", CFL=args.cfl)
             hf = precompute(m, cfg, W, Wb, want_rbf64=True, device=dev)
             r, _, _ = accuracy_pair(hf, cfg, dev, n_steps=args.acc_steps, every=10)
+
+            def fields(mm):
+                return (*mesh.uniform_fields(mm, 1.0, 3.0, 0.0, 1.0), None)
+
+            run, init = {"n_steps": args.acc_steps, "every": 10}, None
         elif name == "riemann_mixed":
             m = mesh.riemann_mixed(args.mixed_n, seed=args.seed)
             W, Wb = mesh.riemann_fields(m)
             cfg = CaseConfig(stencilType="edgeNeighbour", CFL=0.3)
             hf = precompute(m, cfg, W, Wb, want_rbf64=True, device=dev)
             r, _, _ = accuracy_pair(hf, cfg, dev, t_end=0.3, every=100)
+
+            def fields(mm):
+                return (*mesh.riemann_fields(mm), None)
+
+            run, init = {"t_end": 0.3, "every": 100}, None
         elif name == "batch":
             rng = np.random.default_rng(args.seed)
             params = [batch_member_params(rng) for _ in range(args.batch_solves)]
@@ -744,6 +994,11 @@ def run_accuracy(args, dist: Dist):
                 hf = precompute(mm, cfg, W, Wb, want_rbf64=True, device=dev)
                 rk, _, _ = accuracy_pair(hf, cfg, dev, n_steps=args.batch_steps, every=50)
                 rk.update({"member": int(k), "cells": mm.n_cells})
+                if args.floor:
+                    brun = {"n_steps": args.batch_steps, "every": 50}
+                    rk["fp64_floor_reorder"] = fp64_reorder_floor(
+                        mm, lambda m_, p_=params[k]: (*batch_member_fields(m_, p_), None), cfg, dev, **brun)
+                    rk["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, dev, **brun)
                 members.append(rk)
             r = {"members": members, "L1_rho_max": max(x["L1_rho"] for x in members),
                  "Linf_rho_max": max(x["Linf_rho"] for x in members),
@@ -753,6 +1008,9 @@ def run_accuracy(args, dist: Dist):
             raise SystemExit(f"--accuracy: unknown config {name}")
         if hf is not None:
             line["cells"] = hf.nc
+            if args.floor:
+                r["fp64_floor_reorder"] = fp64_reorder_floor(m, fields, cfg, dev, **run)
+                r["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, dev, init=init, **run)
         line.update(r)
         line["wall_s"] = round(time.time() - t0, 1)
         if dist.rank == 0:
@@ -815,9 +1073,18 @@ def batch_member(params):
     nc, angle, u0, strength = params
     ny = max(8, int(round(np.sqrt(nc / 2.0))))
     m = mesh.wedge_quads(2 * ny, ny, angle)
+    W, Wb = batch_member_fields(m, params)
+    return m, W, Wb, CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+
+
+def batch_member_fields(m, params):
+    """Initial cells and inflow ghosts of a batched solve: the vortex carried in the stream."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import mesh
+
+    _, _, u0, strength = params
     W = mesh.vortex_fields(m.cell_centres(), strength=strength, xc=0.5, yc=0.6, u0=u0, v0=0.0)
     Wb = mesh.vortex_fields(m.boundary_face_centres(), strength=0.0, xc=0.5, yc=0.6, u0=u0, v0=0.0)
-    return m, W, Wb, CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+    return W, Wb
 
 
 def run_batch(args, dist: Dist):
@@ -880,6 +1147,10 @@ def run_batch(args, dist: Dist):
 def main():
     args = parse()
     dist = Dist()
+    if args.cache_mesh:
+        return run_cache_mesh(args)
+    if args.cpu_sample:
+        return run_cpu_sample(args)
     try:
         if args.accuracy:
             run_accuracy(args, dist)

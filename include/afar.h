@@ -447,6 +447,12 @@ afar_status afar_switch_counts(afar_solver* solver, long long counts[4]);
 afar_status afar_set_tuning(afar_solver* solver, int reconVariant);
 afar_status afar_get_tuning(afar_solver* solver, int* reconVariant, float* msTile, float* msRegister);
 
+/* The device's FP64 multiply-add rate, measured (no counterpart in the reference): a kernel of
+ * independent DFMA chains over every SM, timed with CUDA events (best of five ~70 ms launches);
+ * *gflops counts two operations per DFMA, *ms (optional) is the timed launch.  The roofline of the
+ * fp64 policy, whose flux and update are bound by the FP64 pipe rather than by memory. */
+afar_status afar_measure_fp64_peak(int device, double* gflops, float* ms);
+
 /* Number of kernel launches one afar_run step issues on this solver (for accounting). */
 int afar_launches_per_step(afar_solver* solver);
 
