@@ -1078,124 +1078,118 @@ __device__ __forceinline__ void kfvs_flux_fast(D& rhoFlux, D& rhoUxFlux, D& rhoU
   rhoFlux += trho * magSf - D(0.5) * rhoL * (uxL * Sfx + uyL * Sfy) - D(0.5) * rhoR * (uxR * Sfx + uyR * Sfy);
 }
 
-// Out-of-line dissipation with the reference's parameter passing (outputs by reference, float
-// states by const reference) behind a device function-pointer table like the reference's
-// calcFlux[] (cudaRiemannSolver.h:139-152); used by the ref policy's k_flux_ref_layout.
-__device__ __noinline__ void roe_ref(double& rhoFlux, double& rhoUxFlux, double& rhoUyFlux, double& rhoEFlux,
+// ---------------------------------------------------------------- ref policy: face flux
+// The ref policy's face flux reproduces the reference kernel's results bit for bit.  Two things
+// besides the arithmetic itself decide that, both established by comparing with the reference
+// kernels' results on the parity meshes (never by reading compiled code):
+//  * nvcc contracts plain a*b + c expressions into fused multiply-adds in ways that depend on the
+//    surrounding code, so every double-precision rounding of the state selection and the central
+//    flux is written out (__fma_rn / __dmul_rn / __dadd_rn) in the pattern the reference's build
+//    produces (identified on 24,300 faces of a mixed quad/triangle Riemann mesh, every candidate
+//    rounding evaluated exactly);
+//  * the float Roe/KFVS dissipation rounds like the reference's only when it is compiled as a
+//    function of its own that takes its inputs by reference and is called through a pointer: inlined,
+//    called directly, or taking its inputs by value, its float expressions round differently on a
+//    few hundred flux entries per mesh (a few ulp of float).
+// A blend c1*a + c2*b with c in {0, 1} is exact either way; it keeps the reference's propagation of
+// a non-finite unused operand.
+
+// One side of an internal face: the limited linear (TVD) state at the face centre, and the state
+// the flux uses (the O3 face value, or the TVD state where the cell's switch asks for it), with
+// p/(R T) of both; reference cudaRiemannSolver.h:190-216.
+struct RefSide {
+  double p, ux, uy, T, rho;  // the state the flux uses
+  double pT, rhoT;           // pressure and density of the TVD state
+};
+__device__ __forceinline__ double ref_tvd(const double w, const float lim, const double ga, const double gb,
+                                          const double dx, const double dy) {
+  return __fma_rn((double)lim, __fma_rn(ga, dx, __dmul_rn(gb, dy)), w);  // w + lim (ga dx + gb dy)
+}
+__device__ __forceinline__ double ref_blend(const bool tvd, const double o3, const double t) {
+  return __dadd_rn(__dmul_rn((double)(1 - tvd), o3), __dmul_rn((double)tvd, t));
+}
+__device__ __forceinline__ RefSide ref_face_side(const StageArgs<PolicyRef>& a, const int c, const int slot,
+                                                 const double dx, const double dy, const bool tvd) {
+  const V4<double> w = a.W[c];
+  const V4<double> g0 = a.grad[2 * c], g1 = a.grad[2 * c + 1];  // (px py uxx uxy), (uyx uyy tx ty)
+  const V4<float> lm = a.lim[c];
+  const V4<double> o3 = a.fv[slot];
+  const double R = a.R;
+  const double pT = ref_tvd(w.x, lm.x, g0.x, g0.y, dx, dy);
+  const double uxT = ref_tvd(w.y, lm.y, g0.z, g1.x, dx, dy);
+  const double uyT = ref_tvd(w.z, lm.z, g0.w, g1.y, dx, dy);
+  const double tT = ref_tvd(w.w, lm.w, g1.z, g1.w, dx, dy);
+  RefSide s;
+  s.pT = pT;
+  s.rhoT = pT / __dmul_rn(R, tT);
+  s.p = ref_blend(tvd, o3.x, pT);
+  s.ux = ref_blend(tvd, o3.y, uxT);
+  s.uy = ref_blend(tvd, o3.z, uyT);
+  s.T = ref_blend(tvd, o3.w, tT);
+  s.rho = s.p / __dmul_rn(R, s.T);
+  return s;
+}
+// Cv T + |u|^2 / 2 + p / rho of a side (its total enthalpy per unit mass)
+__device__ __forceinline__ double ref_enthalpy(const RefSide& s, const double Cv) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(Cv, s.T), __dmul_rn(0.5, __fma_rn(s.ux, s.ux, __dmul_rn(s.uy, s.uy)))),
+                   s.p / s.rho);
+}
+
+// The float dissipation of the ref policy: adds the Roe dissipation, or replaces the central flux
+// by the KFVS flux, in the four double flux components (reference cudaRiemannSolver.h:16-136).
+using RefDissipation = void (*)(double&, double&, double&, double&, const float&, const float&, const float&,
+                                const float&, const float&, const float&, const float&, const float&, const float&,
+                                const float&, const float&, const float&, const double&, const double&, const float,
+                                const float, const float);
+__device__ __noinline__ void ref_roe(double& rhoFlux, double& rhoUxFlux, double& rhoUyFlux, double& rhoEFlux,
                                      const float& rhoL, const float& rhoR, const float& pL, const float& pR,
                                      const float& uxL, const float& uxR, const float& uyL, const float& uyR,
-                                     const float& tL, const float& tR, const float& deltaP, const float& deltaRho,
+                                     const float& tL, const float& tR, const float& dP, const float& dRho,
                                      const double& R, const double& Cv, const float magSf, const float Sfx,
                                      const float Sfy) {
   roe_flux<float, double, double>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoL, rhoR, pL, pR, uxL, uxR, uyL, uyR, tL,
-                                  tR, deltaP, deltaRho, R, Cv, magSf, Sfx, Sfy);
+                                  tR, dP, dRho, R, Cv, magSf, Sfx, Sfy);
 }
-__device__ __noinline__ void kfvs_ref(double& rhoFlux, double& rhoUxFlux, double& rhoUyFlux, double& rhoEFlux,
+__device__ __noinline__ void ref_kfvs(double& rhoFlux, double& rhoUxFlux, double& rhoUyFlux, double& rhoEFlux,
                                       const float& rhoL, const float& rhoR, const float& pL, const float& pR,
                                       const float& uxL, const float& uxR, const float& uyL, const float& uyR,
-                                      const float& tL, const float& tR, const float& deltaP, const float& deltaRho,
+                                      const float& tL, const float& tR, const float&, const float&,
                                       const double& R, const double& Cv, const float magSf, const float Sfx,
                                       const float Sfy) {
-  (void)deltaP;
-  (void)deltaRho;
   kfvs_flux<float, double, double>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoL, rhoR, pL, pR, uxL, uxR, uyL, uyR, tL,
                                    tR, R, Cv, magSf, Sfx, Sfy);
 }
-__device__ void (*ref_flux_table[])(double&, double&, double&, double&, const float&, const float&, const float&,
-                                    const float&, const float&, const float&, const float&, const float&,
-                                    const float&, const float&, const float&, const float&, const double&,
-                                    const double&, const float, const float, const float) = {roe_ref, kfvs_ref};
 
-// Reference-layout structs (basicDataStructure.h:10-65) for the ref-policy flux kernel below.
-struct RCell { double x, y; };
-struct RFace { double x, y, magSf, Sfx, Sfy; };
-struct RField { double p, Ux, Uy, T; };
-struct RGrad { double gradPx, gradPy, gradUxx, gradUxy, gradUyx, gradUyy, gradTx, gradTy; };
-struct RLim { float pLimiter, UxLimiter, UyLimiter, TLimiter; };
-struct RFlux { double rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux; };
-
-// The ref-policy face flux on the reference's array-of-structs layout, one statement per
-// statement of evaluateFlux (cudaRiemannSolver.h:171-251) in the same order: nvcc's multiply-add
-// fusion depends on how the surrounding code is arranged, and matching the arrangement is what
-// keeps the ref policy's flux bit-identical to the reference kernel's.
-__global__ void __launch_bounds__(128) k_flux_ref_layout(RFlux* __restrict__ Flux, const RField* __restrict__ FD,
-                                                         const RGrad* __restrict__ gradFD,
-                                                         const RLim* __restrict__ limiter,
-                                                         const RField* __restrict__ faceFD,
-                                                         const int8_t* __restrict__ shockIndicator,
-                                                         const RCell* __restrict__ CELL,
-                                                         const RFace* __restrict__ FACE,
-                                                         const int* __restrict__ neighbour, const int facesNum,
-                                                         const int cellsNum, const int totalBoundaryFacesNum,
-                                                         const double R, const double Cv) {
-  const int f = threadIdx.x + blockIdx.x * blockDim.x;
-  if (f < facesNum) {
-    const int own = neighbour[2 * f];
-    const int nei = neighbour[2 * f + 1];
-    const double dxL = FACE[f].x - CELL[own].x;
-    const double dyL = FACE[f].y - CELL[own].y;
-    const double dxR = FACE[f].x - CELL[nei].x;
-    const double dyR = FACE[f].y - CELL[nei].y;
-    const bool tvdL = shockIndicator[2 * own + 1] != 0;
-    const bool tvdR = shockIndicator[2 * nei + 1] != 0;
-    const bool isShock = shockIndicator[2 * own + 1] < 0 || shockIndicator[2 * nei + 1] < 0;
-    const double magSf = FACE[f].magSf;
-    const double Sfx = FACE[f].Sfx;
-    const double Sfy = FACE[f].Sfy;
-    double rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux;
-    float pLf, uxLf, uyLf, tLf, rhoLf, pRf, uxRf, uyRf, tRf, rhoRf, dP, dRho;
-    {
-      const double pLT = FD[own].p + limiter[own].pLimiter * (gradFD[own].gradPx * dxL + gradFD[own].gradPy * dyL);
-      const double uxLT = FD[own].Ux + limiter[own].UxLimiter * (gradFD[own].gradUxx * dxL + gradFD[own].gradUyx * dyL);
-      const double uyLT = FD[own].Uy + limiter[own].UyLimiter * (gradFD[own].gradUxy * dxL + gradFD[own].gradUyy * dyL);
-      const double tLT = FD[own].T + limiter[own].TLimiter * (gradFD[own].gradTx * dxL + gradFD[own].gradTy * dyL);
-      const double rhoLT = pLT / (R * tLT);
-      const double pRT = FD[nei].p + limiter[nei].pLimiter * (gradFD[nei].gradPx * dxR + gradFD[nei].gradPy * dyR);
-      const double uxRT = FD[nei].Ux + limiter[nei].UxLimiter * (gradFD[nei].gradUxx * dxR + gradFD[nei].gradUyx * dyR);
-      const double uyRT = FD[nei].Uy + limiter[nei].UyLimiter * (gradFD[nei].gradUxy * dxR + gradFD[nei].gradUyy * dyR);
-      const double tRT = FD[nei].T + limiter[nei].TLimiter * (gradFD[nei].gradTx * dxR + gradFD[nei].gradTy * dyR);
-      const double rhoRT = pRT / (R * tRT);
-      const double pL = (1 - tvdL) * faceFD[2 * f].p + tvdL * pLT;
-      const double uxL = (1 - tvdL) * faceFD[2 * f].Ux + tvdL * uxLT;
-      const double uyL = (1 - tvdL) * faceFD[2 * f].Uy + tvdL * uyLT;
-      const double tL = (1 - tvdL) * faceFD[2 * f].T + tvdL * tLT;
-      const double rhoL = pL / (R * tL);
-      const double pR = (1 - tvdR) * faceFD[2 * f + 1].p + tvdR * pRT;
-      const double uxR = (1 - tvdR) * faceFD[2 * f + 1].Ux + tvdR * uxRT;
-      const double uyR = (1 - tvdR) * faceFD[2 * f + 1].Uy + tvdR * uyRT;
-      const double tR = (1 - tvdR) * faceFD[2 * f + 1].T + tvdR * tRT;
-      const double rhoR = pR / (R * tR);
-      dP = min_delta<float, double>(pL, pR, pLT, pRT);
-      dRho = min_delta<float, double>(rhoL, rhoR, rhoLT, rhoRT);
-      rhoFlux = 0.5 * rhoL * (uxL * Sfx + uyL * Sfy) + 0.5 * rhoR * (uxR * Sfx + uyR * Sfy);
-      rhoUxFlux = 0.5 * (rhoFlux * uxL + pL * Sfx) + 0.5 * (rhoFlux * uxR + pR * Sfx);
-      rhoUyFlux = 0.5 * (rhoFlux * uyL + pL * Sfy) + 0.5 * (rhoFlux * uyR + pR * Sfy);
-      rhoEFlux = 0.5 * rhoFlux * (Cv * tL + 0.5 * (uxL * uxL + uyL * uyL) + pL / rhoL) +
-                 0.5 * rhoFlux * (Cv * tR + 0.5 * (uxR * uxR + uyR * uyR) + pR / rhoR);
-      pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
-      pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
-    }
-    ref_flux_table[isShock](rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf,
-                            tLf, tRf, dP, dRho, R, Cv, magSf, Sfx, Sfy);
-    Flux[f].rhoFlux = rhoFlux;
-    Flux[f].rhoUxFlux = rhoUxFlux;
-    Flux[f].rhoUyFlux = rhoUyFlux;
-    Flux[f].rhoEFlux = rhoEFlux;
-  }
-  if (f < totalBoundaryFacesNum) {
-    const double Sfx = FACE[facesNum + f].Sfx;
-    const double Sfy = FACE[facesNum + f].Sfy;
-    const double bp = FD[cellsNum + f].p;
-    const double bUx = FD[cellsNum + f].Ux;
-    const double bUy = FD[cellsNum + f].Uy;
-    const double bT = FD[cellsNum + f].T;
-    const double rho = bp / (R * bT);
-    const double rf = rho * (bUx * Sfx + bUy * Sfy);
-    Flux[facesNum + f].rhoFlux = rf;
-    Flux[facesNum + f].rhoUxFlux = rf * bUx + bp * Sfx;
-    Flux[facesNum + f].rhoUyFlux = rf * bUy + bp * Sfy;
-    Flux[facesNum + f].rhoEFlux = rf * (Cv * bT + 0.5 * (bUx * bUx + bUy * bUy) + bp / rho);
-  }
+// evaluateFlux of internal face f under the ref policy (reference cudaRiemannSolver.h:171-251):
+// both sides' states, the minimised jumps of p and rho, the central flux in double, then the float
+// Roe dissipation, or the KFVS flux where either cell is a shock cell.
+__device__ __forceinline__ void flux_ref_face(const StageArgs<PolicyRef>& a, const int f) {
+  const int2 on = a.on[f];
+  const V4<double> d = a.fd[f];   // face centre - owner centre, face centre - neighbour centre
+  const V4<double> sf = a.fs[f];  // Sfx, Sfy, |Sf|
+  const int8_t swL = a.si[2 * on.x + 1], swR = a.si[2 * on.y + 1];
+  const RefSide L = ref_face_side(a, on.x, 2 * f, d.x, d.y, swL != 0);
+  const RefSide Rs = ref_face_side(a, on.y, 2 * f + 1, d.z, d.w, swR != 0);
+  const double Sfx = sf.x, Sfy = sf.y, magSf = sf.z, Cv = a.Cv, R = a.R;
+  const float dP = min_delta<float, double>(L.p, Rs.p, L.pT, Rs.pT);
+  const float dRho = min_delta<float, double>(L.rho, Rs.rho, L.rhoT, Rs.rhoT);
+  // central flux: the mean of the two sides' Euler fluxes through Sf
+  double F0, F1, F2, F3;
+  const double unL = __fma_rn(L.ux, Sfx, __dmul_rn(L.uy, Sfy)), unR = __fma_rn(Rs.ux, Sfx, __dmul_rn(Rs.uy, Sfy));
+  F0 = __fma_rn(__dmul_rn(0.5, L.rho), unL, __dmul_rn(__dmul_rn(0.5, Rs.rho), unR));
+  F1 = __dadd_rn(__dmul_rn(0.5, __fma_rn(L.p, Sfx, __dmul_rn(F0, L.ux))),
+                 __dmul_rn(0.5, __fma_rn(Rs.p, Sfx, __dmul_rn(F0, Rs.ux))));
+  F2 = __dadd_rn(__dmul_rn(0.5, __fma_rn(L.p, Sfy, __dmul_rn(F0, L.uy))),
+                 __dmul_rn(0.5, __fma_rn(Rs.p, Sfy, __dmul_rn(F0, Rs.uy))));
+  const double half = __dmul_rn(0.5, F0);
+  F3 = __fma_rn(half, ref_enthalpy(L, Cv), __dmul_rn(half, ref_enthalpy(Rs, Cv)));
+  // the dissipation sees the states, face vector and jumps as floats; R and Cv stay double
+  const float rhoL = L.rho, rhoR = Rs.rho, pL = L.p, pR = Rs.p, uxL = L.ux, uxR = Rs.ux, uyL = L.uy, uyR = Rs.uy,
+              tL = L.T, tR = Rs.T;
+  const RefDissipation diss = (swL < 0 || swR < 0) ? ref_kfvs : ref_roe;
+  diss(F0, F1, F2, F3, rhoL, rhoR, pL, pR, uxL, uxR, uyL, uyR, tL, tR, dP, dRho, R, Cv, (float)magSf, (float)Sfx,
+       (float)Sfy);
+  a.flux[f] = V4<double>{F0, F1, F2, F3};
 }
 
 // evaluateFlux (reference cudaRiemannSolver.h:155-271): one thread per internal face, then one per
@@ -1223,110 +1217,115 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
   double dtf = 1e5;
   float dtf32 = 1e5f;
   if (id < a.Nf) {
-    const int2 on = a.on[id];
-    const int own = on.x, nei = on.y;
-    const V4<G> fd = a.fd[id];
-    const G dxL = fd.x, dyL = fd.y, dxR = fd.z, dyR = fd.w;
-    const int8_t sL = a.si[2 * own + 1], sR = a.si[2 * nei + 1];
-    const bool tvdL = sL != 0, tvdR = sR != 0;
-    const bool isShock = sL < 0 || sR < 0;
-    const V4<G> fs = a.fs[id];
-    const G Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
-    G R, Cv, iR, gam;
-    if constexpr (kF32) {
-      R = a.Rf;
-      Cv = a.Cvf;
-      iR = a.invRf;
-      gam = a.gm1f + 1.f;
+    if constexpr (P::id == PolicyRef::id) {
+      static_assert(!DT, "under the ref policy the Courant step is a kernel of its own, as in the reference");
+      flux_ref_face(a, id);
     } else {
-      R = (G)a.R;
-      Cv = (G)a.Cv;
-      iR = (G)a.invR;
-      gam = (G)a.gamma;
-    }
-    const V4<typename P::W> Wo = a.W[own], Wn = a.W[nei];
-    const V4<G> go0 = a.grad[2 * own], go1 = a.grad[2 * own + 1];
-    const V4<G> gn0 = a.grad[2 * nei], gn1 = a.grad[2 * nei + 1];
-    const V4<S> lo = a.lim[own], ln = a.lim[nei];
-    const V4<G> fo = a.fv[2 * id], fn = a.fv[2 * id + 1];
-    G rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux;
-    D pLf, uxLf, uyLf, tLf, rhoLf, pRf, uxRf, uyRf, tRf, rhoRf, dP, dRho;
-    {
-      const G pLT = (G)Wo.x + lo.x * (go0.x * dxL + go0.y * dyL);
-      const G uxLT = (G)Wo.y + lo.y * (go0.z * dxL + go1.x * dyL);
-      const G uyLT = (G)Wo.z + lo.z * (go0.w * dxL + go1.y * dyL);
-      const G tLT = (G)Wo.w + lo.w * (go1.z * dxL + go1.w * dyL);
-      const G pRT = (G)Wn.x + ln.x * (gn0.x * dxR + gn0.y * dyR);
-      const G uxRT = (G)Wn.y + ln.y * (gn0.z * dxR + gn1.x * dyR);
-      const G uyRT = (G)Wn.z + ln.z * (gn0.w * dxR + gn1.y * dyR);
-      const G tRT = (G)Wn.w + ln.w * (gn1.z * dxR + gn1.w * dyR);
-      const G pL = pick<P>(!tvdL, tvdL, fo.x, pLT);
-      const G uxL = pick<P>(!tvdL, tvdL, fo.y, uxLT);
-      const G uyL = pick<P>(!tvdL, tvdL, fo.z, uyLT);
-      const G tL = pick<P>(!tvdL, tvdL, fo.w, tLT);
-      const G pR = pick<P>(!tvdR, tvdR, fn.x, pRT);
-      const G uxR = pick<P>(!tvdR, tvdR, fn.y, uxRT);
-      const G uyR = pick<P>(!tvdR, tvdR, fn.z, uyRT);
-      const G tR = pick<P>(!tvdR, tvdR, fn.w, tRT);
-      G rhoLT, rhoRT, rhoL, rhoR;  // p / (R T) of the four states
+      const int2 on = a.on[id];
+      const int own = on.x, nei = on.y;
+      const V4<G> fd = a.fd[id];
+      const G dxL = fd.x, dyL = fd.y, dxR = fd.z, dyR = fd.w;
+      const int8_t sL = a.si[2 * own + 1], sR = a.si[2 * nei + 1];
+      const bool tvdL = sL != 0, tvdR = sR != 0;
+      const bool isShock = sL < 0 || sR < 0;
+      const V4<G> fs = a.fs[id];
+      const G Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
+      G R, Cv, iR, gam;
       if constexpr (kF32) {
-        rhoLT = fdiv(pLT * iR, tLT);
-        rhoRT = fdiv(pRT * iR, tRT);
-        rhoL = fdiv(pL * iR, tL);
-        rhoR = fdiv(pR * iR, tR);
+        R = a.Rf;
+        Cv = a.Cvf;
+        iR = a.invRf;
+        gam = a.gm1f + 1.f;
       } else {
-        // FP64: the four reciprocal temperatures from one division (Montgomery's simultaneous
-        // inversion, a few ulps from four divisions); a double division is among the dearest
-        // operations of GB300's FP64 pipe, which bounds this kernel.  Temperatures stay far from
-        // the range limits of double (their product of four neither overflows nor underflows).
-        const G tt = tL * tR, ttT = tLT * tRT;
-        const G inv = G(1) / (tt * ttT);
-        const G itt = inv * ttT, ittT = inv * tt;  // 1/(tL tR), 1/(tLT tRT)
-        rhoL = pL * iR * (itt * tR);
-        rhoR = pR * iR * (itt * tL);
-        rhoLT = pLT * iR * (ittT * tRT);
-        rhoRT = pRT * iR * (ittT * tLT);
+        R = (G)a.R;
+        Cv = (G)a.Cv;
+        iR = (G)a.invR;
+        gam = (G)a.gamma;
       }
-      dP = min_delta<D, G>(pL, pR, pLT, pRT);
-      dRho = min_delta<D, G>(rhoL, rhoR, rhoLT, rhoRT);
-      const G h = G(0.5);
-      rhoFlux = h * rhoL * (uxL * Sfx + uyL * Sfy) + h * rhoR * (uxR * Sfx + uyR * Sfy);
-      rhoUxFlux = h * (rhoFlux * uxL + pL * Sfx) + h * (rhoFlux * uxR + pR * Sfx);
-      rhoUyFlux = h * (rhoFlux * uyL + pL * Sfy) + h * (rhoFlux * uyR + pR * Sfy);
-      rhoEFlux = h * rhoFlux * (Cv * tL + h * (uxL * uxL + uyL * uyL) + R * tL) +  // p/rho = R T
-                 h * rhoFlux * (Cv * tR + h * (uxR * uxR + uyR * uyR) + R * tR);
-      pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
-      pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
-    }
-    static_assert(std::is_same<D, G>::value, "fp64 and mixed run the dissipation in their face-value type");
-    const G nfx = Sfx * fs.w, nfy = Sfy * fs.w;  // fs.w = 1/|Sf| (setup)
-    if (isShock)
-      kfvs_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
-                        tRf, R, Cv, G(2) * Cv * iR - G(2), magSf, nfx, nfy);
-    else
-      roe_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, uxLf, uxRf, uyLf, uyRf, tLf, tRf, dP,
-                       dRho, R, Cv, gam, magSf, nfx, nfy);
-    a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)rhoUxFlux, (typename P::F)rhoUyFlux,
-                                   (typename P::F)rhoEFlux};
-    if constexpr (DT && kF32) {
-      if (s_cfl_step) {  // setDeltaT, cudaFieldOperation.h:140-157, as an FP32 estimate
-        const V2<float> g = a.dtgf[id];
-        const float deltaR = g.x, fraction = g.y;
-        dtf32 = s_cfl * deltaR * magSf /
-                ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
-                 sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+      const V4<typename P::W> Wo = a.W[own], Wn = a.W[nei];
+      const V4<G> go0 = a.grad[2 * own], go1 = a.grad[2 * own + 1];
+      const V4<G> gn0 = a.grad[2 * nei], gn1 = a.grad[2 * nei + 1];
+      const V4<S> lo = a.lim[own], ln = a.lim[nei];
+      const V4<G> fo = a.fv[2 * id], fn = a.fv[2 * id + 1];
+      G rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux;
+      D pLf, uxLf, uyLf, tLf, rhoLf, pRf, uxRf, uyRf, tRf, rhoRf, dP, dRho;
+      {
+        const G pLT = (G)Wo.x + lo.x * (go0.x * dxL + go0.y * dyL);
+        const G uxLT = (G)Wo.y + lo.y * (go0.z * dxL + go1.x * dyL);
+        const G uyLT = (G)Wo.z + lo.z * (go0.w * dxL + go1.y * dyL);
+        const G tLT = (G)Wo.w + lo.w * (go1.z * dxL + go1.w * dyL);
+        const G pRT = (G)Wn.x + ln.x * (gn0.x * dxR + gn0.y * dyR);
+        const G uxRT = (G)Wn.y + ln.y * (gn0.z * dxR + gn1.x * dyR);
+        const G uyRT = (G)Wn.z + ln.z * (gn0.w * dxR + gn1.y * dyR);
+        const G tRT = (G)Wn.w + ln.w * (gn1.z * dxR + gn1.w * dyR);
+        const G pL = pick<P>(!tvdL, tvdL, fo.x, pLT);
+        const G uxL = pick<P>(!tvdL, tvdL, fo.y, uxLT);
+        const G uyL = pick<P>(!tvdL, tvdL, fo.z, uyLT);
+        const G tL = pick<P>(!tvdL, tvdL, fo.w, tLT);
+        const G pR = pick<P>(!tvdR, tvdR, fn.x, pRT);
+        const G uxR = pick<P>(!tvdR, tvdR, fn.y, uxRT);
+        const G uyR = pick<P>(!tvdR, tvdR, fn.z, uyRT);
+        const G tR = pick<P>(!tvdR, tvdR, fn.w, tRT);
+        G rhoLT, rhoRT, rhoL, rhoR;  // p / (R T) of the four states
+        if constexpr (kF32) {
+          rhoLT = fdiv(pLT * iR, tLT);
+          rhoRT = fdiv(pRT * iR, tRT);
+          rhoL = fdiv(pL * iR, tL);
+          rhoR = fdiv(pR * iR, tR);
+        } else {
+          // FP64: the four reciprocal temperatures from one division (Montgomery's simultaneous
+          // inversion, a few ulps from four divisions); a double division is among the dearest
+          // operations of GB300's FP64 pipe, which bounds this kernel.  Temperatures stay far from
+          // the range limits of double (their product of four neither overflows nor underflows).
+          const G tt = tL * tR, ttT = tLT * tRT;
+          const G inv = G(1) / (tt * ttT);
+          const G itt = inv * ttT, ittT = inv * tt;  // 1/(tL tR), 1/(tLT tRT)
+          rhoL = pL * iR * (itt * tR);
+          rhoR = pR * iR * (itt * tL);
+          rhoLT = pLT * iR * (ittT * tRT);
+          rhoRT = pRT * iR * (ittT * tLT);
+        }
+        dP = min_delta<D, G>(pL, pR, pLT, pRT);
+        dRho = min_delta<D, G>(rhoL, rhoR, rhoLT, rhoRT);
+        const G h = G(0.5);
+        rhoFlux = h * rhoL * (uxL * Sfx + uyL * Sfy) + h * rhoR * (uxR * Sfx + uyR * Sfy);
+        rhoUxFlux = h * (rhoFlux * uxL + pL * Sfx) + h * (rhoFlux * uxR + pR * Sfx);
+        rhoUyFlux = h * (rhoFlux * uyL + pL * Sfy) + h * (rhoFlux * uyR + pR * Sfy);
+        rhoEFlux = h * rhoFlux * (Cv * tL + h * (uxL * uxL + uyL * uyL) + R * tL) +  // p/rho = R T
+                   h * rhoFlux * (Cv * tR + h * (uxR * uxR + uyR * uyR) + R * tR);
+        pLf = pL; uxLf = uxL; uyLf = uyL; tLf = tL; rhoLf = rhoL;
+        pRf = pR; uxRf = uxR; uyRf = uyR; tRf = tR; rhoRf = rhoR;
       }
-    } else if (DT) {
-      const StepCtl* ctl = a.ctl;
-      if (!(ctl->dt_fixed > 0.0)) {  // setDeltaT, cudaFieldOperation.h:140-157
-        const V2<double> g = a.dtg[id];
-        const double deltaR = g.x, fraction = g.y;
-        const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
-        const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
-        dtf = CFL * deltaR * msf /
-              ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
-               fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
-               sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
+      static_assert(std::is_same<D, G>::value, "fp64 and mixed run the dissipation in their face-value type");
+      const G nfx = Sfx * fs.w, nfy = Sfy * fs.w;  // fs.w = 1/|Sf| (setup)
+      if (isShock)
+        kfvs_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, pLf, pRf, uxLf, uxRf, uyLf, uyRf, tLf,
+                          tRf, R, Cv, G(2) * Cv * iR - G(2), magSf, nfx, nfy);
+      else
+        roe_flux_fast<G>(rhoFlux, rhoUxFlux, rhoUyFlux, rhoEFlux, rhoLf, rhoRf, uxLf, uxRf, uyLf, uyRf, tLf, tRf, dP,
+                         dRho, R, Cv, gam, magSf, nfx, nfy);
+      a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)rhoUxFlux, (typename P::F)rhoUyFlux,
+                                     (typename P::F)rhoEFlux};
+      if constexpr (DT && kF32) {
+        if (s_cfl_step) {  // setDeltaT, cudaFieldOperation.h:140-157, as an FP32 estimate
+          const V2<float> g = a.dtgf[id];
+          const float deltaR = g.x, fraction = g.y;
+          dtf32 = s_cfl * deltaR * magSf /
+                  ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
+                   sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+        }
+      } else if (DT) {
+        const StepCtl* ctl = a.ctl;
+        if (!(ctl->dt_fixed > 0.0)) {  // setDeltaT, cudaFieldOperation.h:140-157
+          const V2<double> g = a.dtg[id];
+          const double deltaR = g.x, fraction = g.y;
+          const double sfx = (double)Sfx, sfy = (double)Sfy, msf = (double)magSf;
+          const double CFL = ctl->cfl, Rd = a.R, Cvd = a.Cv;
+          dtf = CFL * deltaR * msf /
+                ((1.0 - fraction) * fabs((double)Wo.y * sfx + (double)Wo.z * sfy) +
+                 fraction * fabs((double)Wn.y * sfx + (double)Wn.z * sfy) +
+                 sqrt((Rd / Cvd + 1.0) * Rd * ((1.0 - fraction) * (double)Wo.w + fraction * (double)Wn.w)) * msf);
+        }
       }
     }
   } else if (id < a.Nf + a.Nb) {  // boundary faces, reference :254-270

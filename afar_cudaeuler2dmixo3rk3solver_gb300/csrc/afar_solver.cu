@@ -357,22 +357,15 @@ struct Stage {
       k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
   }
   void bvd() const { k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a); }
-  // The face flux.  The ref policy runs the reference-layout kernel (its fused multiply-adds then
-  // fall where the reference's do) and, on the first stage, the CFL step as a kernel of its own
-  // like the reference's setDeltaT; the other policies fuse the CFL reduction into the flux.
+  // The face flux.  The ref policy computes the CFL step as a kernel of its own before the first
+  // stage's flux, like the reference's setDeltaT; the other policies fuse it into that flux.
   void flux(bool dt_stage) const {
+    const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
     if constexpr (P::id == PolicyRef::id) {
       if (dt_stage && s->Nf > 0)
         k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
-      const int gr = grid_for(std::max(s->Nf, s->Nb), 128);
-      k_flux_ref_layout<<<gr, 128, 0, s->stream>>>(
-          reinterpret_cast<RFlux*>(s->flux), reinterpret_cast<const RField*>(s->W),
-          reinterpret_cast<const RGrad*>(s->grad), reinterpret_cast<const RLim*>(s->lim),
-          reinterpret_cast<const RField*>(s->fv), s->si, reinterpret_cast<const RCell*>(s->cellC),
-          reinterpret_cast<const RFace*>(s->faceRaw), reinterpret_cast<const int*>(s->on), s->Nf, s->Nc, s->Nb, a.R,
-          a.Cv);
+      k_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(a);
     } else {
-      const int gf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
       if (dt_stage)
         k_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(a);
       else
