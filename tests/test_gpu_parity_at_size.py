@@ -2,10 +2,10 @@
 
 * the ref policy against the reference's own kernels (oracle/_ref cubins), stage by stage for one
   RK3 step from identical inputs, on the 2.0M-triangle Mach 3 step mesh (stencils up to 17) and the
-  4.0M-cell mixed quad/triangle Riemann mesh (quads and triangles, stencils up to 20): every
+  4.0M-cell mixed quad/triangle Riemann mesh (quads and triangles, stencils up to 15): every
   intermediate within 1e-12 relative and identical troubled-cell / switch flags;
 * the fp64 policy against the CPU oracle (FP64 restatement) for one stage on the 2.0M mesh: 1e-10;
-* the mixed policy's tile-staged reconstruct (four-face path, stencils up to 20) on the 4.0M mesh
+* the mixed policy's tile-staged reconstruct (four-face path, stencils up to 15) on the 4.0M mesh
   against the fp64 policy and against its register-pass variant, one stage each.
 
 These are the sizes the benchmark runs; the small-mesh tests in test_gpu_parity.py cover more
@@ -97,7 +97,7 @@ def test_ref_policy_matches_reference_kernels_on_the_2M_step_mesh(step_case, ref
 
 def test_ref_policy_matches_reference_kernels_on_the_4M_mixed_mesh(mixed_case, ref_kernels):
     hf, cfg = mixed_case
-    assert hf.nc > 3_900_000 and hf.sizes["maxCompactStencilSize"] == 4 and hf.sizes["maxStencilSize"] >= 20
+    assert hf.nc > 3_900_000 and hf.sizes["maxCompactStencilSize"] == 4 and hf.sizes["maxStencilSize"] >= 15
     _ref_vs_reference_one_step(hf, cfg, ref_kernels, min_flags=1000)
 
 
@@ -121,7 +121,7 @@ def test_fp64_policy_matches_the_oracle_for_one_stage_on_the_2M_step_mesh(step_c
 
 
 def test_mixed_tile_reconstruct_on_the_4M_mixed_mesh(mixed_case):
-    """The four-face tile path with stencils up to 20: one stage against the fp64 policy and
+    """The four-face tile path with stencils up to 15: one stage against the fp64 policy and
     against the register-pass reconstruct, both to FP32 rounding (the mixed policy reconstructs and
     forms fluxes in FP32)."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver
