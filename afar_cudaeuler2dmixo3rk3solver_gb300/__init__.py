@@ -6,6 +6,7 @@ generators used by the tests and the benchmark.
 """
 from . import mesh  # noqa: F401
 from ._ffi import AfarError, lib  # noqa: F401
-from .solver import Batch, CaseConfig, Server, CudaSolver, HostFields, gauss_quadrature, precompute  # noqa: F401
+from .solver import (Batch, CaseConfig, CudaSolver, HostFields, Server, face_gauss_quadrature,  # noqa: F401
+                     gauss_quadrature, precompute)
 
-__all__ = ["Batch", "Server", "mesh", "lib", "AfarError", "CaseConfig", "CudaSolver", "HostFields", "precompute", "gauss_quadrature"]
+__all__ = ["Batch", "Server", "mesh", "lib", "AfarError", "CaseConfig", "CudaSolver", "HostFields", "precompute", "gauss_quadrature", "face_gauss_quadrature"]

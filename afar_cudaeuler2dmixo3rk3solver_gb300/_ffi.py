@@ -94,6 +94,7 @@ def lib():
             "afar_precompute_fields_device": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), _p, _p, C.c_int,
                                                   C.POINTER(FieldPointer), C.POINTER(FieldSizes), C.POINTER(_p)]),
             "afar_gauss_quadrature": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), _p, _p, _p, C.POINTER(C.c_int)]),
+            "afar_face_gauss_quadrature": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), C.POINTER(C.c_int), _p, _p]),
             "afar_solver_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),
             "afar_setDeviceFieldData": (S, [_p, C.POINTER(FieldPointer), C.c_int, C.c_int, C.c_int]),
             "afar_setDeviceFieldDataStencil": (S, [_p, C.POINTER(FieldPointer)] + [C.c_int] * 8),
@@ -166,7 +167,7 @@ def ptr(a):
 EXPORTED = [
     "afar_last_error", "afar_default_case_config", "afar_precompute_fields", "afar_free_host_fields",
     "afar_precompute_fields_device",
-    "afar_gauss_quadrature", "afar_solver_create", "afar_setDeviceFieldData", "afar_setDeviceFieldDataStencil",
+    "afar_gauss_quadrature", "afar_face_gauss_quadrature", "afar_solver_create", "afar_setDeviceFieldData", "afar_setDeviceFieldDataStencil",
     "afar_adjustTimeStep", "afar_GPUevolve", "afar_copyFieldDataDeviceToHost", "afar_freeFieldData", "afar_set_gas",
     "afar_set_rbf_basis64", "afar_run", "afar_run_async", "afar_synchronize", "afar_get_stream", "afar_get_time",
     "afar_set_time", "afar_stage_debug", "afar_debug_limiter64", "afar_upload_state", "afar_download_state",

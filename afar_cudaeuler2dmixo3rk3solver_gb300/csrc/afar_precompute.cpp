@@ -434,6 +434,40 @@ static bool check_mesh(const afar_polyMesh* m) {
   return true;
 }
 
+// The face Gauss points of d2GaussQuadrature::calcFaceGaussQuadrature (d2GaussQuadrature.C:153-214,
+// and :216-277 for the boundary patches) for every face in face order: the bar rule of fOrder mapped
+// onto the edge from its first to its second point, x_k = (p0 (1 - xi_k) + p1 (1 + xi_k)) / 2, weight
+// w_k * |p1 - p0| / 2 * depth (the face area included, as the reference keeps it for face fluxes).
+extern "C" afar_status afar_face_gauss_quadrature(const afar_polyMesh* m, const afar_caseConfig* cfg,
+                                                  int* pointsPerFace, double* pts, double* w) {
+  if (!check_mesh(m) || !cfg || !pointsPerFace) {
+    if (!cfg || !pointsPerFace) set_error("afar_face_gauss_quadrature: null argument");
+    return AFAR_ERR_ARGUMENT;
+  }
+  std::vector<double> sp, sw;
+  bar_rule(cfg->fOrder, sp, sw);
+  if (sp.empty()) {
+    set_error("no Gauss rule stored for fOrder=%d", cfg->fOrder);
+    return AFAR_ERR_ARGUMENT;
+  }
+  const int ng = (int)sp.size();
+  *pointsPerFace = ng;
+  if (!pts || !w) return AFAR_OK;
+  for (int f = 0; f < m->nFaces; ++f) {
+    const int a = m->facePoints[2 * f], b = m->facePoints[2 * f + 1];
+    const double xa = m->points[2 * a], ya = m->points[2 * a + 1];
+    const double xb = m->points[2 * b], yb = m->points[2 * b + 1];
+    const double jac = std::sqrt((0.5 * (xa - xb)) * (0.5 * (xa - xb)) + (0.5 * (ya - yb)) * (0.5 * (ya - yb)));
+    for (int k = 0; k < ng; ++k) {
+      const double xi = sp[k];
+      pts[2 * ((size_t)f * ng + k)] = 0.5 * xa * (1 - xi) + 0.5 * xb * (1 + xi);
+      pts[2 * ((size_t)f * ng + k) + 1] = 0.5 * ya * (1 - xi) + 0.5 * yb * (1 + xi);
+      w[(size_t)f * ng + k] = sw[k] * jac * m->depth;
+    }
+  }
+  return AFAR_OK;
+}
+
 extern "C" afar_status afar_gauss_quadrature(const afar_polyMesh* m, const afar_caseConfig* cfg, int* offsets,
                                              double* pts, double* w, int* total) {
   if (!check_mesh(m) || !cfg || !total) {

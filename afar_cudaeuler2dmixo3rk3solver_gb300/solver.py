@@ -245,6 +245,21 @@ def gauss_quadrature(mesh: FoamMesh, cfg: CaseConfig):
     return off, pts, w
 
 
+def face_gauss_quadrature(mesh: FoamMesh, cfg: CaseConfig):
+    """Face Gauss points and weights of every face, internal then boundary in face order (the
+    d2GaussQuadrature faceGaussPoints / faceGaussWeights layout): points [nFaces, n, 2], weights
+    [nFaces, n] (each face's weights sum to |Sf|)."""
+    m, keep = poly_mesh_c(mesh)
+    c = cfg.to_c()
+    n = C.c_int()
+    check(lib().afar_face_gauss_quadrature(C.byref(m), C.byref(c), C.byref(n), None, None))
+    pts = np.zeros((mesh.n_faces, n.value, 2))
+    w = np.zeros((mesh.n_faces, n.value))
+    check(lib().afar_face_gauss_quadrature(C.byref(m), C.byref(c), C.byref(n), ptr(pts), ptr(w)))
+    del keep
+    return pts, w
+
+
 class CudaSolver:
     """The reference's basicCUDAsolver on libafar (one mesh, one GPU)."""
 

@@ -198,6 +198,16 @@ afar_status afar_precompute_fields_device(const afar_polyMesh* mesh, const afar_
                                           afar_fieldPointer* host, afar_fieldSizes* sizes,
                                           double** RBFbasis64);
 
+/* The face Gauss points and weights of every face, internal then boundary in face order (the
+ * d2GaussQuadrature faceGaussPoints/faceGaussWeights layout, d2GaussQuadrature.C:153-277 and the
+ * getters of d2GaussQuadrature.H:75-83): the fOrder bar rule (1, 2, 3 or 4 points) on each edge from
+ * its first to its second point; each weight is the rule's weight times half the edge length times
+ * the mesh depth, so a face's weights sum to |Sf|.  *pointsPerFace receives the rule's size n;
+ * pts: [2*n*nFaces] (x, y of point k of face f at 2*(f*n + k)), w: [n*nFaces].  Call with pts or w
+ * NULL to get n alone. */
+afar_status afar_face_gauss_quadrature(const afar_polyMesh* mesh, const afar_caseConfig* cfg, int* pointsPerFace,
+                                       double* pts, double* w);
+
 /* Cell and boundary-face Gauss points/weights (d2GaussQuadrature layout) as CSR lists over
  * nCells + nBoundaryFaces members; boundary-face weights are divided by |Sf| like
  * basicCUDAsolver.cpp:444-457.  offsets: [nCells+nBoundaryFaces+1]; pts: [2*total]; w: [total].

@@ -156,6 +156,34 @@ def test_gauss_quadrature_exactness():
                 np.testing.assert_allclose(approx[~is_tri], exact[~is_tri], rtol=1e-12, atol=1e-15)
 
 
+@pytest.mark.parametrize("fOrder,npts", [(1, 1), (3, 2), (5, 3), (7, 4)])
+def test_face_gauss_quadrature_layout(fOrder, npts):
+    """The face-point layout (d2GaussQuadrature faceGaussPoints / faceGaussWeights) against a numpy
+    restatement: every face in face order, points from the first to the second face point, weights
+    times half the edge length times the depth; each face's weights sum to |Sf| and the rule
+    integrates polynomials of degree 2n-1 along the edge exactly."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, face_gauss_quadrature, mesh
+
+    m = mesh.riemann_mixed(6, seed=2)
+    pts, w = face_gauss_quadrature(m, CaseConfig(fOrder=fOrder))
+    assert pts.shape == (m.n_faces, npts, 2) and w.shape == (m.n_faces, npts)
+    a = m.points[m.face_pts[:, 0]]
+    b = m.points[m.face_pts[:, 1]]
+    xi, wi = np.polynomial.legendre.leggauss(npts)
+    # the reference lists its 4-point rule from +0.861 down, the others from -xi up
+    if npts == 4:
+        xi, wi = xi[::-1], wi[::-1]
+    half = 0.5 * np.linalg.norm(b - a, axis=1)
+    expect_p = 0.5 * a[:, None, :] * (1 - xi)[None, :, None] + 0.5 * b[:, None, :] * (1 + xi)[None, :, None]
+    np.testing.assert_allclose(pts, expect_p, rtol=0, atol=1e-14)
+    np.testing.assert_allclose(w, wi[None, :] * half[:, None] * m.depth, rtol=1e-12)
+    np.testing.assert_allclose(w.sum(axis=1), 2.0 * half * m.depth, rtol=1e-12)
+    for deg in range(2 * npts):
+        t = np.linalg.norm(pts - a[:, None, :], axis=2) / (2.0 * half[:, None])  # 0..1 along the edge
+        approx = np.sum(w * t ** deg, axis=1)
+        np.testing.assert_allclose(approx, 2.0 * half * m.depth / (deg + 1), rtol=1e-9)
+
+
 def _poly_moment(m, px, py):
     """Integral of x^px y^py over each cell polygon (fan triangulation, degree-8 Dunavant-free
     approach: exact by the divergence theorem along edges with Gauss-Legendre)."""
