@@ -1,5 +1,6 @@
 """OpenFOAM case files for the AFAR solver: reading the dictionaries a reference case holds, a 2-D
-blockMesh, and writing the fields (and the mesh) back in OpenFOAM's ascii format.
+blockMesh or a polyMesh, and writing the fields (and the mesh) back, in OpenFOAM's ascii or binary
+format (controlDict ``writeFormat``).
 
 The reference application reads an OpenFOAM case: ``system/blockMeshDict`` (meshed by blockMesh),
 ``system/controlDict`` (end time, write interval, Courant number), ``system/fvSchemes`` (the
@@ -220,19 +221,101 @@ def block_mesh_2d(bmd: FoamDict, labels: dict, renumber: bool = True) -> M.FoamM
                              depth=depth if depth > 0 else 1.0)
 
 
+# ----------------------------------------------------------------------------------- file formats
+# OpenFOAM writes a file in ascii or binary (controlDict writeFormat).  The header and every
+# dictionary stay text either way; in binary a list of a contiguous type (labels, scalars, vectors)
+# is written as its size and then its raw bytes in parentheses, "N\n(<bytes>)" -- little-endian
+# (LSB), labels of 32 or 64 bits and scalars of 64 bits as the header's arch entry says
+# ("LSB;label=32;scalar=64", OpenFOAM's default build).  Files are read as bytes and decoded as
+# latin-1, so text offsets are byte offsets and the raw payloads can be cut out exactly.
+@dataclasses.dataclass
+class _Fmt:
+    binary: bool = False
+    label: str = "<i4"
+    scalar: str = "<f8"
+
+
+def _load(path: str):
+    """(raw bytes, the same as latin-1 text, the format, the offset just past the header)."""
+    raw = open(path, "rb").read()
+    txt = raw.decode("latin-1")
+    fmt = _Fmt()
+    m = re.search(r"FoamFile\s*\{([^{}]*)\}", txt)
+    if not m:
+        return raw, txt, fmt, 0
+    head = _strip_comments(m.group(1))
+    fmt.binary = re.search(r"format\s+binary", head) is not None
+    arch = re.search(r'arch\s+"([^"]*)"', head)
+    if arch:
+        a = arch.group(1)
+        if "MSB" in a:
+            raise ValueError(f"{path}: big-endian (MSB) binary files are not supported")
+        lab = re.search(r"label=(\d+)", a)
+        sca = re.search(r"scalar=(\d+)", a)
+        fmt.label = {"32": "<i4", "64": "<i8"}[lab.group(1)] if lab else "<i4"
+        if sca and sca.group(1) != "64":
+            raise ValueError(f"{path}: only 64-bit scalars are supported (arch {a})")
+    return raw, txt, fmt, m.end()
+
+
+def _binary_block(raw: bytes, txt: str, pos: int, count: int, dtype: str, path: str):
+    """The payload "(<count items>)" that starts at the next "(" at or after pos: (array, end)."""
+    i = pos
+    while i < len(txt) and txt[i] in " \t\r\n":
+        i += 1
+    if count == 0 and (i >= len(txt) or txt[i] != "("):
+        return np.zeros(0, dtype=dtype), i  # an empty list carries no parentheses
+    if i >= len(txt) or txt[i] != "(":
+        raise ValueError(f"{path}: binary list without its opening parenthesis")
+    nbytes = count * np.dtype(dtype).itemsize
+    end = i + 1 + nbytes
+    if end >= len(raw) or txt[end] != ")":
+        raise ValueError(f"{path}: binary list of {count} items is cut short")
+    return np.frombuffer(raw[i + 1:end], dtype=dtype).copy(), end + 1
+
+
+_SIZE = re.compile(r"\s*(\d+)")
+
+
+def _binary_list(raw, txt, pos, items_dtype, per_item, path):
+    """A binary "N (<bytes>)" list at pos: (array (N,) or (N, per_item), end)."""
+    m = _SIZE.match(txt, pos)
+    if not m:
+        raise ValueError(f"{path}: binary list without its size")
+    n = int(m.group(1))
+    a, end = _binary_block(raw, txt, m.end(), n * per_item, items_dtype, path)
+    return (a.reshape(n, per_item) if per_item > 1 else a), end
+
+
+def _header(cls, obj, location=None, binary=False):
+    loc = f'    location    "{location}";\n' if location is not None else ""
+    arch = '    arch        "LSB;label=32;scalar=64";\n' if binary else ""
+    return (f"FoamFile\n{{\n    version     2.0;\n    format      {'binary' if binary else 'ascii'};\n{arch}"
+            f"    class       {cls};\n{loc}    object      {obj};\n}}\n\n")
+
+
+def _binary_payload(a: np.ndarray, dtype: str) -> bytes:
+    """A list's raw bytes between parentheses, as OpenFOAM writes it in binary (size excluded)."""
+    return b"(" + np.ascontiguousarray(a, dtype=dtype).tobytes() + b")"
+
+
 # ----------------------------------------------------------------------------------- polyMesh (2-D)
 def _body(path: str) -> str:
-    """A file's text after its FoamFile header, comments removed; ascii only."""
-    txt = _strip_comments(open(path).read())
-    m = re.search(r"FoamFile\s*\{(.*?)\}", txt, re.S)
-    if m and re.search(r"format\s+binary", m.group(1)):
-        raise ValueError(f"{path}: binary files are not supported; write the case in ascii")
-    return txt[m.end():] if m else txt
+    """A text file's content after its FoamFile header, comments removed (dictionaries: the same
+    in ascii and binary files)."""
+    _, txt, _, end = _load(path)
+    return _strip_comments(txt[end:])
 
 
 def _read_numbers(path: str, per_item: int, dtype) -> np.ndarray:
-    """``N ( item ... )`` with items of ``per_item`` numbers (``(x y z)`` or a bare label)."""
-    a = np.fromstring(_body(path).replace("(", " ").replace(")", " "), dtype=np.float64, sep=" ")
+    """``N ( item ... )`` with items of ``per_item`` numbers (``(x y z)`` or a bare label): labels
+    when dtype is an integer type, else scalars; ascii or binary."""
+    raw, txt, fmt, end = _load(path)
+    if fmt.binary:
+        kind = fmt.label if np.issubdtype(np.dtype(dtype), np.integer) else fmt.scalar
+        a, _ = _binary_list(raw, txt, end, kind, per_item, path)
+        return a.astype(dtype)
+    a = np.fromstring(_strip_comments(txt[end:]).replace("(", " ").replace(")", " "), dtype=np.float64, sep=" ")
     n = int(a[0]) if a.shape[0] else -1
     if n < 0 or a.shape[0] != 1 + n * per_item:
         raise ValueError(f"{path}: malformed list ({a.shape[0] - 1} numbers for {n} items of {per_item})")
@@ -241,8 +324,26 @@ def _read_numbers(path: str, per_item: int, dtype) -> np.ndarray:
 
 
 def _read_label_lists(path: str):
-    """A ``List<labelList>`` (the polyMesh ``faces``) as CSR: offsets (N+1,), labels."""
-    a = np.fromstring(_body(path).replace("(", " -1 ").replace(")", " -2 "), dtype=np.float64, sep=" ")
+    """A ``List<labelList>`` (the polyMesh ``faces``) as CSR: offsets (N+1,), labels.  A
+    ``faceCompactList`` -- how OpenFOAM writes faces in binary, and may in ascii -- is the offsets
+    list followed by the labels list."""
+    raw, txt, fmt, end = _load(path)
+    compact = re.search(r"class\s+faceCompactList", txt[:end]) is not None
+    if fmt.binary or compact:
+        if fmt.binary:
+            off, pos = _binary_list(raw, txt, end, fmt.label, 1, path)
+            lab, _ = _binary_list(raw, txt, pos, fmt.label, 1, path)
+        else:
+            a = np.fromstring(_strip_comments(txt[end:]).replace("(", " ").replace(")", " "), dtype=np.float64,
+                              sep=" ")
+            n1 = int(a[0])
+            off = a[1:1 + n1]
+            lab = a[2 + n1:2 + n1 + int(a[1 + n1])]
+        off, lab = off.astype(np.int64), lab.astype(np.int64)
+        if off.shape[0] < 1 or off[0] != 0 or off[-1] != lab.shape[0] or np.any(np.diff(off) < 0):
+            raise ValueError(f"{path}: malformed compact face list")
+        return off, lab
+    a = np.fromstring(_strip_comments(txt[end:]).replace("(", " -1 ").replace(")", " -2 "), dtype=np.float64, sep=" ")
     if a.shape[0] < 3 or a[1] != -1 or a[-1] != -2:
         raise ValueError(f"{path}: malformed list of lists")
     n = int(a[0])
@@ -392,8 +493,11 @@ _SLIP = ("slip", "symmetryPlane", "symmetry")
 
 def read_field_dict(path: str):
     """A volField file as a FoamDict, its ``nonuniform List<...>`` values read by numpy into arrays
-    ((N,) for scalars, (N, 3) for vectors) instead of being tokenised."""
-    txt = _strip_comments(open(path).read())
+    ((N,) for scalars, (N, 3) for vectors) instead of being tokenised; ascii or binary."""
+    raw, txt, fmt, hend = _load(path)
+    if fmt.binary:
+        return _read_binary_field_dict(raw, txt, fmt, hend, path)
+    txt = _strip_comments(txt)
     arrays, parts, i = [], [], 0
     while True:
         m = _NONUNIFORM.search(txt, i)
@@ -415,8 +519,13 @@ def read_field_dict(path: str):
         parts += [txt[i:m.start()], f" __afar_list_{len(arrays) - 1}__ "]
         i = end
     parts.append(txt[i:])
-    d = parse_foam("".join(parts))
+    return _resolve_lists(parse_foam("".join(parts)), arrays)
 
+
+_NONUNIFORM_BIN = re.compile(r"nonuniform\s+List<(scalar|vector)>\s*(\d+)")
+
+
+def _resolve_lists(d, arrays):
     def resolve(v):
         if isinstance(v, str) and v.startswith("__afar_list_"):
             return arrays[int(v[12:-2])]
@@ -428,6 +537,23 @@ def read_field_dict(path: str):
         return v
 
     return resolve(d)
+
+
+def _read_binary_field_dict(raw, txt, fmt, hend, path):
+    """read_field_dict of a binary file: each nonuniform list's payload is cut out of the bytes and
+    the text around the payloads parsed as a dictionary."""
+    arrays, parts, i = [], [], hend
+    while True:
+        m = _NONUNIFORM_BIN.search(txt, i)
+        if not m:
+            break
+        k = 3 if m.group(1) == "vector" else 1
+        a, end = _binary_block(raw, txt, m.end(), int(m.group(2)) * k, fmt.scalar, path)
+        arrays.append(a.reshape(-1, 3) if k == 3 else a)
+        parts += [txt[i:m.start()], f" __afar_list_{len(arrays) - 1}__ "]
+        i = end
+    parts.append(txt[i:])
+    return _resolve_lists(parse_foam(_strip_comments("".join(parts))), arrays)
 
 
 def _values(v, n, is_vector, what):
@@ -519,24 +645,21 @@ def _truth(v) -> bool:
 
 
 # ----------------------------------------------------------------------------------- writing
-def _header(cls, obj, location=None):
-    loc = f'    location    "{location}";\n' if location is not None else ""
-    return ("FoamFile\n{\n    version     2.0;\n    format      ascii;\n"
-            f"    class       {cls};\n{loc}    object      {obj};\n}}\n\n")
-
-
 def _fmt(v):
     return f"{v:.9g}"
 
 
-def write_poly_mesh(out_dir: str, m: M.FoamMesh):
+def write_poly_mesh(out_dir: str, m: M.FoamMesh, binary: bool = False):
     """``constant/polyMesh`` of the one-cell-deep 3-D mesh: points on z = 0 and z = depth, a quad
     per 2-D face (internal faces first, then the named patches), and the front and back polygons
-    of every cell in the empty patch ``defaultFaces``."""
+    of every cell in the empty patch ``defaultFaces``; in ascii, or in OpenFOAM's binary form
+    (faces as a ``faceCompactList``)."""
     d = os.path.join(out_dir, "constant", "polyMesh")
     os.makedirs(d, exist_ok=True)
     npt = m.points.shape[0]
     P3 = np.concatenate([np.c_[m.points, np.zeros(npt)], np.c_[m.points, np.full(npt, m.depth)]])
+    if binary:
+        return _write_poly_mesh_binary(d, m, P3)
     with open(os.path.join(d, "points"), "w") as f:
         f.write(_header("vectorField", "points", "constant/polyMesh"))
         f.write(f"{P3.shape[0]}\n(\n")
@@ -561,8 +684,46 @@ def write_poly_mesh(out_dir: str, m: M.FoamMesh):
     with open(os.path.join(d, "neighbour"), "w") as f:
         f.write(_header("labelList", "neighbour", "constant/polyMesh"))
         f.write(f"{m.neighbour.shape[0]}\n(\n" + "\n".join(map(str, m.neighbour)) + "\n)\n")
+    _write_boundary(d, m, False)
+
+
+def _poly_faces(m: M.FoamMesh):
+    """The 3-D faces as CSR (offsets, labels): side quads, then front and back cell polygons."""
+    npt = m.points.shape[0]
+    fp = m.face_pts.astype(np.int64)
+    side = np.stack([fp[:, 0], fp[:, 1], fp[:, 1] + npt, fp[:, 0] + npt], axis=1).reshape(-1)
+    cnt = np.diff(m.cell_ptr.astype(np.int64))
+    polys = m.cell_pts.astype(np.int64)
+    # each cell's polygon reversed (front, normal -z) and as it is, on the upper plane (back)
+    rev = np.concatenate([polys[m.cell_ptr[c]:m.cell_ptr[c + 1]][::-1] for c in range(m.n_cells)]) \
+        if m.n_cells else np.zeros(0, dtype=np.int64)
+    labels = np.concatenate([side, rev, polys + npt])
+    counts = np.concatenate([np.full(fp.shape[0], 4), cnt, cnt])
+    off = np.zeros(counts.shape[0] + 1, dtype=np.int64)
+    np.cumsum(counts, out=off[1:])
+    return off, labels
+
+
+def _write_poly_mesh_binary(d, m, P3):
+    cells = np.arange(m.n_cells)
+    owner = np.concatenate([m.owner.astype(np.int64), cells, cells])
+    off, lab = _poly_faces(m)
+    for name, cls, parts in (
+            ("points", "vectorField", [(P3.shape[0], P3, "<f8")]),
+            ("faces", "faceCompactList", [(off.shape[0], off, "<i4"), (lab.shape[0], lab, "<i4")]),
+            ("owner", "labelList", [(owner.shape[0], owner, "<i4")]),
+            ("neighbour", "labelList", [(m.neighbour.shape[0], m.neighbour, "<i4")])):
+        with open(os.path.join(d, name), "wb") as f:
+            f.write(_header(cls, name, "constant/polyMesh", binary=True).encode())
+            for n, a, dt in parts:
+                f.write(f"\n{n}\n".encode() + _binary_payload(a, dt) + b"\n")
+            f.write(b"\n")
+    _write_boundary(d, m, True)
+
+
+def _write_boundary(d, m, binary):
     with open(os.path.join(d, "boundary"), "w") as f:
-        f.write(_header("polyBoundaryMesh", "boundary", "constant/polyMesh"))
+        f.write(_header("polyBoundaryMesh", "boundary", "constant/polyMesh", binary=binary))
         f.write(f"{len(m.patches) + 1}\n(\n")
         for name, _, start, size in m.patches:
             f.write(f"    {name}\n    {{\n        type            patch;\n        nFaces          {size};\n"
@@ -571,8 +732,10 @@ def write_poly_mesh(out_dir: str, m: M.FoamMesh):
                 f"        startFace       {m.n_faces};\n    }}\n)\n")
 
 
-def _write_field(path, name, cls, dims, cells, ghosts, patches, time_name):
+def _write_field(path, name, cls, dims, cells, ghosts, patches, time_name, binary=False):
     vec = cls == "volVectorField"
+    if binary:
+        return _write_field_binary(path, name, cls, dims, cells, ghosts, patches, time_name, vec)
 
     def vals(a):
         if vec:
@@ -593,41 +756,62 @@ def _write_field(path, name, cls, dims, cells, ghosts, patches, time_name):
         f.write("    defaultFaces\n    {\n        type            empty;\n    }\n}\n")
 
 
+def _write_field_binary(path, name, cls, dims, cells, ghosts, patches, time_name, vec):
+    """The field in OpenFOAM's binary form: the dictionary as text, each nonuniform list as its size
+    and raw 64-bit values (vectors with a zero z component, double precision, so no rounding)."""
+    kind = "vector" if vec else "scalar"
+
+    def block(a):
+        a = np.asarray(a, dtype=np.float64)
+        if vec:
+            a = np.c_[a, np.zeros(a.shape[0])]
+        return f"nonuniform List<{kind}> \n{a.shape[0]}\n".encode() + _binary_payload(a, "<f8")
+
+    with open(path, "wb") as f:
+        f.write(_header(cls, name, time_name, binary=True).encode())
+        f.write(f"dimensions      {dims};\n\ninternalField   ".encode() + block(cells) + b";\n\nboundaryField\n{\n")
+        off = 0
+        for pname, _, _, size in patches:
+            f.write(f"    {pname}\n    {{\n        type            calculated;\n        value           ".encode()
+                    + block(ghosts[off:off + size]) + b";\n    }\n")
+            off += size
+        f.write(b"    defaultFaces\n    {\n        type            empty;\n    }\n}\n")
+
+
 def time_name(t: float) -> str:
     """OpenFOAM's time directory name (general format, 6 significant digits)."""
     return f"{t:.6g}"
 
 
-def write_fields(out_dir: str, t: float, m: M.FoamMesh, FD: np.ndarray, flags: np.ndarray):
+def write_fields(out_dir: str, t: float, m: M.FoamMesh, FD: np.ndarray, flags: np.ndarray, binary: bool = False):
     """``<t>/p``, ``U``, ``T`` and ``shockIndicator`` like the reference's writeField
     (basicCUDAsolver.cpp:874-913): cell values and ghost values per patch; the indicator is the
-    final switch type of each cell (boundary values 0)."""
+    final switch type of each cell (boundary values 0).  ascii (9 significant digits) or binary
+    (the doubles themselves)."""
     tn = time_name(t)
     d = os.path.join(out_dir, tn)
     os.makedirs(d, exist_ok=True)
     nc = m.n_cells
     cells, ghosts = FD[:nc], FD[nc:]
     _write_field(os.path.join(d, "p"), "p", "volScalarField", "[1 -1 -2 0 0 0 0]", cells[:, 0], ghosts[:, 0],
-                 m.patches, tn)
+                 m.patches, tn, binary)
     _write_field(os.path.join(d, "U"), "U", "volVectorField", "[0 1 -1 0 0 0 0]", cells[:, 1:3], ghosts[:, 1:3],
-                 m.patches, tn)
+                 m.patches, tn, binary)
     _write_field(os.path.join(d, "T"), "T", "volScalarField", "[0 0 0 1 0 0 0]", cells[:, 3], ghosts[:, 3],
-                 m.patches, tn)
+                 m.patches, tn, binary)
     si = np.asarray(flags[1:2 * nc:2], dtype=np.float64)
     _write_field(os.path.join(d, "shockIndicator"), "shockIndicator", "volScalarField", "[0 0 0 0 0 0 0]", si,
-                 np.zeros(ghosts.shape[0]), m.patches, tn)
+                 np.zeros(ghosts.shape[0]), m.patches, tn, binary)
     return d
 
 
 def read_field(path: str) -> np.ndarray:
-    """The internal values of a field written by ``write_fields`` (nonuniform ascii lists)."""
-    txt = open(path).read()
-    m = re.search(r"internalField\s+nonuniform\s+List<(\w+)>\s*(\d+)\s*\((.*?)\)\s*;", txt, re.S)
-    kind, n, body = m.group(1), int(m.group(2)), m.group(3)
-    if kind == "vector":
-        vals = np.array([[float(x) for x in s.split()] for s in re.findall(r"\(([^()]*)\)", body)])
-        return vals[:n]
-    return np.array([float(x) for x in body.split()])[:n]
+    """The internal values of a field file with a nonuniform internalField, ascii or binary:
+    (N,) scalars or (N, 3) vectors."""
+    v = read_field_dict(path)["internalField"]
+    if isinstance(v, list) and len(v) == 2 and v[0] == "nonuniform":  # a short ascii list kept as tokens
+        v = np.asarray(v[1], dtype=np.float64)
+    return np.asarray(v, dtype=np.float64)
 
 
 # ----------------------------------------------------------------------------------- RBF basis files
@@ -646,13 +830,14 @@ def _basis_layout(hf):
     return lens, np.stack([base, base + maxS + 1])
 
 
-def write_basis_lists(system_dir: str, hf, precision: int = 17):
+def write_basis_lists(system_dir: str, hf, precision: int = 17, binary: bool = False):
     """``basisOwnList`` and ``basisNeiList``: the O3 RBF weights of every internal face as OpenFOAM
     ascii ``IOList<List<scalar>>`` files, one list per face with the owner's (neighbour's) stencil
     length, the cell itself first -- the files the reference writes beside its case dictionaries
     after computing the weights (basicCUDAsolver.cpp:538-651).  The values are the double weights
     when the bundle carries them (``RBFbasis64``), else its float weights; ``precision`` significant
-    digits (17 reads back bit-exact)."""
+    digits (17 reads back bit-exact).  In binary each face's list is its length and its raw doubles,
+    inside the outer list's text parentheses, as OpenFOAM writes a list of lists."""
     os.makedirs(system_dir, exist_ok=True)
     w = hf.a.get("RBFbasis64")
     if w is None or w.shape[0] != hf.a["RBFbasis"].shape[0]:
@@ -660,6 +845,14 @@ def write_basis_lists(system_dir: str, hf, precision: int = 17):
     lens, starts = _basis_layout(hf)
     fmt = f"{{:.{precision}g}}"
     for side, name in enumerate(BASIS_FILES):
+        if binary:
+            with open(os.path.join(system_dir, name), "wb") as f:
+                f.write(_header("scalarListList", name, "system", binary=True).encode())
+                f.write(f"\n{lens.shape[1]}\n(\n".encode())
+                for n, o in zip(lens[side].tolist(), starts[side].tolist()):
+                    f.write(f"\n{n}\n".encode() + _binary_payload(w[o:o + n], "<f8") + b"\n")
+                f.write(b")\n")
+            continue
         with open(os.path.join(system_dir, name), "w") as f:
             f.write(_header("scalarListList", name, "system"))
             f.write(f"{lens.shape[1]}\n(\n")
@@ -671,12 +864,12 @@ def write_basis_lists(system_dir: str, hf, precision: int = 17):
 def _read_list_list(path: str, lens: np.ndarray) -> np.ndarray:
     """The values of an ascii ``List<List<scalar>>`` whose inner lengths must equal ``lens``,
     concatenated.  Inner lists may be written on one line (``n(a b c)``) or one value per line,
-    as OpenFOAM writes lists longer than ten."""
-    txt = _strip_comments(open(path).read())
-    m = re.search(r"FoamFile\s*\{(.*?)\}", txt, re.S)
-    if m and re.search(r"format\s+binary", m.group(1)):
-        raise ValueError(f"{path}: binary lists are not supported; write the case in ascii")
-    body = txt[m.end():] if m else txt
+    as OpenFOAM writes lists longer than ten; in a binary file each inner list is its length and
+    raw doubles."""
+    raw, txt, fmt, hend = _load(path)
+    if fmt.binary:
+        return _read_binary_list_list(raw, txt, fmt, hend, lens, path)
+    body = _strip_comments(txt[hend:])
     if "{" in body:
         raise ValueError(f"{path}: uniform list notation n{{v}} is not supported")
     a = np.fromstring(body.replace("(", " ").replace(")", " "), dtype=np.float64, sep=" ")
@@ -691,6 +884,26 @@ def _read_list_list(path: str, lens: np.ndarray) -> np.ndarray:
                          f"{int(lens[min(face, n - 1)])}")
     idx = np.repeat(heads + 1, lens) + (np.arange(int(lens.sum())) - np.repeat(np.cumsum(lens) - lens, lens))
     return a[idx]
+
+
+def _read_binary_list_list(raw, txt, fmt, pos, lens, path):
+    m = _SIZE.match(txt, pos)
+    n = lens.shape[0]
+    if not m or int(m.group(1)) != n:
+        raise ValueError(f"{path}: {int(m.group(1)) if m else 0} lists, the mesh has {n} internal faces")
+    i = m.end()
+    while txt[i] in " \t\r\n":
+        i += 1
+    if txt[i] != "(":
+        raise ValueError(f"{path}: list of lists without its opening parenthesis")
+    i += 1
+    out = []
+    for face in range(n):
+        a, i = _binary_list(raw, txt, i, fmt.scalar, 1, path)
+        if a.shape[0] != lens[face]:
+            raise ValueError(f"{path}: the list of face {face} does not have the stencil's length {int(lens[face])}")
+        out.append(a)
+    return np.concatenate(out) if out else np.zeros(0)
 
 
 def read_basis_lists(system_dir: str, hf):
@@ -726,19 +939,20 @@ def run_case(case_dir: str, out_dir: str | None = None, policy: str = "mixed", d
     from .solver import CudaSolver, precompute
 
     case = load_case(case_dir)
+    binary = str(read_foam(os.path.join(case_dir, "system", "controlDict")).get("writeFormat", "ascii")) == "binary"
     m = case.mesh
     save_basis = case.recalc_basis and write and out_dir
     hf = precompute(m, case.config, case.W, case.Wb, want_rbf64=policy == "fp64" or bool(save_basis))
     if not case.recalc_basis:
         read_basis_lists(os.path.join(case_dir, "system"), hf)
     elif save_basis:
-        write_basis_lists(os.path.join(out_dir, "system"), hf)
+        write_basis_lists(os.path.join(out_dir, "system"), hf, binary=binary)
     s = CudaSolver(hf, case.config, policy=policy, device=device)
     try:
         if write and out_dir:
-            write_poly_mesh(out_dir, m)
+            write_poly_mesh(out_dir, m, binary=binary)
             FD, flags = s.write_field()
-            write_fields(out_dir, 0.0, m, FD, flags)
+            write_fields(out_dir, 0.0, m, FD, flags, binary=binary)
         wi = case.write_interval if case.write_interval > 0 else case.end_time
         s.set_write_interval(wi)
         dt_fixed = 0.0 if case.adjust_time_step else case.delta_t
@@ -754,7 +968,7 @@ def run_case(case_dir: str, out_dir: str | None = None, policy: str = "mixed", d
                 if not np.isfinite(FD[:m.n_cells]).all():
                     raise FloatingPointError(f"non-finite state before t = {target}")
             if write and out_dir:
-                write_fields(out_dir, target, m, FD, flags)
+                write_fields(out_dir, target, m, FD, flags, binary=binary)
             written.append(target)
             k += 1
         t, _, steps = s.time()

@@ -63,8 +63,8 @@ boundaryField
 """
 
 
-def write_case(root, n=4, end=0.02, wi=0.005, recalc_basis=None):
-    """Blocks of (3n x n), (3n x 4n), (12n x 4n) cells."""
+def write_case(root, n=4, end=0.02, wi=0.005, recalc_basis=None, write_format=None):
+    """Blocks of (3n x n), (3n x 4n), (12n x 4n) cells; write_format: the controlDict writeFormat."""
     for d in ("system", "0", "constant"):
         os.makedirs(os.path.join(root, d), exist_ok=True)
 
@@ -75,7 +75,8 @@ def write_case(root, n=4, end=0.02, wi=0.005, recalc_basis=None):
     put("system/blockMeshDict", "blockMeshDict", BLOCK_MESH % {"na": 3 * n, "nb": n, "nc": 4 * n, "nd": 12 * n})
     recalc = "" if recalc_basis is None else f"    recalcBasis {'true' if recalc_basis else 'false'};\n"
     put("system/fvSchemes", "fvSchemes", SCHEMES % {"recalc": recalc})
-    put("system/controlDict", "controlDict", CONTROL % {"end": end, "wi": wi})
+    put("system/controlDict", "controlDict",
+        CONTROL % {"end": end, "wi": wi} + (f"writeFormat {write_format};\n" if write_format else ""))
     put("0/p", "p", FIELD % {"dims": "[1 -1 -2 0 0 0 0]", "val": "1", "wall": "zeroGradient"})
     put("0/U", "U", FIELD % {"dims": "[0 1 -1 0 0 0 0]", "val": "(3 0 0)", "wall": "slip"})
     put("0/T", "T", FIELD % {"dims": "[0 0 0 1 0 0 0]", "val": "1", "wall": "zeroGradient"})

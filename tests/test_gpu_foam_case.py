@@ -82,3 +82,37 @@ def test_recalc_basis_false_reuses_the_written_weights(tmp_path):
             a = foam.read_field(os.path.join(first, t, f))
             b = foam.read_field(os.path.join(second, t, f))
             assert np.array_equal(a, b), (t, f)
+
+
+def test_run_case_in_binary_write_format(tmp_path):
+    """writeFormat binary (the reference case's setting): the fields, the polyMesh and the O3
+    weight files come out in OpenFOAM's binary form, hold the same values as the ascii run (to the
+    ascii files' 9 digits; the state is the same, bit for bit), and the binary weight files feed a
+    recalcBasis false run that reproduces the first."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import foam
+
+    res, outs = {}, {}
+    for fmt in ("ascii", "binary"):
+        case_dir = write_case(str(tmp_path / f"case_{fmt}"), n=4, end=0.01, wi=0.005, write_format=fmt)
+        outs[fmt] = str(tmp_path / f"out_{fmt}")
+        res[fmt] = foam.run_case(case_dir, outs[fmt], policy="fp64")
+    assert res["ascii"]["steps"] == res["binary"]["steps"]
+    for t in ("0.005", "0.01"):
+        for name in ("p", "U", "T"):
+            head = open(os.path.join(outs["binary"], t, name), "rb").read(200)
+            assert b"format      binary;" in head
+            a = foam.read_field(os.path.join(outs["ascii"], t, name))
+            b = foam.read_field(os.path.join(outs["binary"], t, name))
+            assert np.allclose(a, b, rtol=2e-9, atol=1e-12), (t, name)
+    m = foam.read_poly_mesh(outs["binary"], {0: 3, 1: 4, 2: 2})
+    assert m.n_cells == res["binary"]["cells"]
+    # rerun from the binary weight files (recalcBasis false): the same final fields, bit for bit
+    again = write_case(str(tmp_path / "again"), n=4, end=0.01, wi=0.005, recalc_basis=False, write_format="binary")
+    import shutil
+    for f in foam.BASIS_FILES:
+        shutil.copy(os.path.join(outs["binary"], "system", f), os.path.join(again, "system", f))
+    out2 = str(tmp_path / "out_again")
+    foam.run_case(again, out2, policy="fp64")
+    for name in ("p", "U", "T"):
+        assert np.array_equal(foam.read_field(os.path.join(out2, "0.01", name)),
+                              foam.read_field(os.path.join(outs["binary"], "0.01", name)))
