@@ -142,6 +142,9 @@ def lib():
             "afar_batch_size": (S, [_p, C.POINTER(C.c_int)]),
             "afar_batch_run": (S, [_p, C.c_int, C.POINTER(C.c_float)]),
             "afar_batch_destroy": (S, [_p]),
+            "afar_batch_get_schedule": (S, [_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+            "afar_batch_set_schedule": (S, [_p, C.c_int, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -174,6 +177,6 @@ EXPORTED = [
     "afar_download_ls_matrix", "afar_device_bytes", "afar_launches_per_step", "afar_run_timed",
     "afar_profile_step", "afar_state_snapshot", "afar_adjustTimeStep_noalloc", "afar_set_step_params",
     "afar_set_write_interval", "afar_set_periodic", "afar_set_tuning", "afar_get_tuning", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
-    "afar_batch_destroy", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
+    "afar_batch_destroy", "afar_batch_get_schedule", "afar_batch_set_schedule", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
     "afar_server_destroy", "afar_server_cancel", "afar_switch_counts", "afar_measure_fp64_peak",
 ]

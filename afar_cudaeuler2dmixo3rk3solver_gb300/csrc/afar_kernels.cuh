@@ -1643,15 +1643,23 @@ __global__ void __launch_bounds__(128, 4) kb_reconstruct_staged<PolicyFP64>(cons
   const int2 m = map[blockIdx.x];
   recon_staged_body<PolicyFP64>(tab[m.x], m.y);
 }
+// the register-pass reconstruct of the mixed policy over the members the autotuner gave it
 template <class P>
-// mixed: 32 registers, 16 blocks (the full 64 warps) per SM for this gather-bound kernel
-__global__ void __launch_bounds__(128, P::id == PolicyMixed::id ? 16 : 10) kb_bvd(
+__global__ void __launch_bounds__(128, 5) kb_reconstruct_reg(const StageArgs<P>* __restrict__ tab,
+                                                            const int2* __restrict__ map) {
+  const int2 m = map[blockIdx.x];
+  recon_reg_body<P>(tab[m.x], m.y);
+}
+// BVD and flux in blocks of B threads (the batch autotuner's choice; the map's blocks are B cells
+// or faces of one member).  mixed BVD: 32 registers, the full 64 warps per SM; fp64: 40 warps.
+template <class P, int B>
+__global__ void __launch_bounds__(B, (P::id == PolicyMixed::id ? 2048 : 1280) / B) kb_bvd(
     const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
   bvd_body<P>(tab[m.x], m.y);
 }
-template <class P, bool DT>
-__global__ void __launch_bounds__(256) kb_flux(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
+template <class P, bool DT, int B>
+__global__ void __launch_bounds__(B) kb_flux(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
   flux_body<P, DT>(tab[m.x], m.y);
 }

@@ -1463,6 +1463,15 @@ extern "C" afar_status afar_set_write_interval(afar_solver* s, double writeInter
   return AFAR_OK;
 }
 
+// The batch's launch schedule: which reconstruct each member runs (its own autotuned choice, so a
+// member's result never depends on its batch-mates) and the BVD and flux block sizes (timed on the
+// whole batch; the results do not depend on them, every reduction being an exact minimum).
+struct BatchSchedule {
+  int bvd_block = 128, flux_block = 256;
+  int tile_members = 0, reg_members = 0;
+  float ms[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // BVD at 64, 128, 256; flux at 128, 256 (0: from the cache)
+};
+
 struct afar_batch {
   int policy = AFAR_POLICY_MIXED;
   int device = 0;
@@ -1470,31 +1479,117 @@ struct afar_batch {
   std::vector<afar_solver*> members;
   void* tab = nullptr;  // StageArgs<P>[members]
   size_t tab_bytes = 0;
-  int2* cmap = nullptr;  // per cell block: (member, block within the member)
-  int2* fmap = nullptr;  // per face block
-  size_t cmap_n = 0, fmap_n = 0;
-  int ncb = 0, nfb = 0;
+  // block maps, (member, block within the member) per block, one after another in one buffer:
+  // 128-cell blocks of the tile-reconstruct members, of the register-reconstruct members, of every
+  // member (update; the fp64 reconstruct), BVD blocks, face blocks
+  int2* maps = nullptr;
+  size_t maps_n = 0;
+  int n_tile = 0, n_reg = 0, n_cell = 0, n_bvd = 0, n_face = 0;
   size_t smem = 0;  // dynamic shared memory of the staged reconstruct (largest member)
+  BatchSchedule sched;
+  int forced_bvd = 0, forced_flux = 0;  // afar_batch_set_schedule (0: autotune)
   cudaGraphExec_t graph = nullptr;
   bool dirty = true;
 };
 
 namespace {
 
+// Blocks of `block` cells (or faces when faces) of each member in `which` (empty: all members).
+void batch_map(const std::vector<afar_solver*>& members, int block, bool faces, const std::vector<int>* which,
+               std::vector<int2>& out) {
+  for (size_t i = 0; i < members.size(); ++i) {
+    if (which && !(*which)[i]) continue;
+    const afar_solver* s = members[i];
+    const long long n = faces ? (long long)s->Nf + s->Nb : (long long)s->Nc;
+    const int nb = grid_for(n, block);
+    for (int k = 0; k < nb; ++k) out.push_back(int2{(int)i, k});
+  }
+}
+
+template <class P>
+void launch_bvd(int block, int nblocks, const StageArgs<P>* t, const int2* map, cudaStream_t st) {
+  if (nblocks == 0) return;
+  if (block == 64)
+    kb_bvd<P, 64><<<nblocks, 64, 0, st>>>(t, map);
+  else if (block == 256)
+    kb_bvd<P, 256><<<nblocks, 256, 0, st>>>(t, map);
+  else
+    kb_bvd<P, 128><<<nblocks, 128, 0, st>>>(t, map);
+}
+template <class P, bool DT>
+void launch_flux(int block, int nblocks, const StageArgs<P>* t, const int2* map, cudaStream_t st) {
+  if (nblocks == 0) return;
+  if (block == 128)
+    kb_flux<P, DT, 128><<<nblocks, 128, 0, st>>>(t, map);
+  else
+    kb_flux<P, DT, 256><<<nblocks, 256, 0, st>>>(t, map);
+}
+
+// The batch autotuner's decisions, per device, policy and batch shape (cells and members, each to
+// a factor of two): BVD and flux block sizes.
+std::mutex g_batch_tune_mu;
+std::map<std::tuple<int, int, int, int>, std::pair<int, int>> g_batch_tune;
+
 template <class P>
 afar_status batch_build(afar_batch* b) {
   std::vector<StageArgs<P>> tab;
-  std::vector<int2> cm, fm;
   size_t smem = 0;
   afar_status st;
+  long long cells = 0;
+  std::vector<int> is_tile(b->members.size(), 1), is_reg(b->members.size(), 0);
   for (size_t i = 0; i < b->members.size(); ++i) {
     afar_solver* s = b->members[i];
     tab.push_back(make_args<P>(s));
-    const int nc = grid_for(s->Nc, kCellBlock), nf = grid_for((long long)s->Nf + s->Nb, kFaceBlock);
-    for (int k = 0; k < nc; ++k) cm.push_back(int2{(int)i, k});
-    for (int k = 0; k < nf; ++k) fm.push_back(int2{(int)i, k});
     smem = std::max(smem, recon_smem<P>(s));
+    cells += s->Nc;
+    if constexpr (P::id == PolicyMixed::id) {
+      is_reg[i] = s->recon_variant == 1;  // the member's own autotuned (or forced) reconstruct
+      is_tile[i] = !is_reg[i];
+    }
   }
+  int lc = 0, lm = 0;
+  while ((1ll << (lc + 1)) <= cells) ++lc;
+  while ((1ll << (lm + 1)) <= (long long)b->members.size()) ++lm;
+  const auto key = std::make_tuple(b->device, (int)P::id, lc, lm);
+  BatchSchedule sc;
+  for (size_t i = 0; i < b->members.size(); ++i) sc.tile_members += is_tile[i], sc.reg_members += is_reg[i];
+  bool timed = true;
+  if (b->forced_bvd || b->forced_flux) {
+    sc.bvd_block = b->forced_bvd ? b->forced_bvd : 128;
+    sc.flux_block = b->forced_flux ? b->forced_flux : 256;
+    timed = false;
+  } else {
+    std::lock_guard<std::mutex> lock(g_batch_tune_mu);
+    auto it = g_batch_tune.find(key);
+    if (it != g_batch_tune.end()) {
+      sc.bvd_block = it->second.first;
+      sc.flux_block = it->second.second;
+      timed = false;
+    }
+  }
+
+  std::vector<int2> mp_tile, mp_reg, mp_cell;
+  batch_map(b->members, kTile, false, &is_tile, mp_tile);
+  batch_map(b->members, kTile, false, &is_reg, mp_reg);
+  batch_map(b->members, kCellBlock, false, nullptr, mp_cell);
+  // candidate maps for the timing: BVD in 64/128/256-cell blocks, flux in 128/256-face blocks
+  const int bvd_sizes[3] = {64, 128, 256}, flux_sizes[2] = {128, 256};
+  std::vector<int2> mp_bvd[3], mp_face[2];
+  for (int k = 0; k < 3; ++k)
+    if (timed || bvd_sizes[k] == sc.bvd_block) batch_map(b->members, bvd_sizes[k], false, nullptr, mp_bvd[k]);
+  for (int k = 0; k < 2; ++k)
+    if (timed || flux_sizes[k] == sc.flux_block) batch_map(b->members, flux_sizes[k], true, nullptr, mp_face[k]);
+  std::vector<int2> all;
+  auto append = [&](const std::vector<int2>& v) {
+    const size_t o = all.size();
+    all.insert(all.end(), v.begin(), v.end());
+    return o;
+  };
+  const size_t o_tile = append(mp_tile), o_reg = append(mp_reg), o_cell = append(mp_cell);
+  size_t o_bvd[3], o_face[2];
+  for (int k = 0; k < 3; ++k) o_bvd[k] = append(mp_bvd[k]);
+  for (int k = 0; k < 2; ++k) o_face[k] = append(mp_face[k]);
+
   auto grow = [&](void** p, size_t* cap, size_t need) -> afar_status {
     if (need > *cap) {
       if (*p) cudaFree(*p);
@@ -1504,20 +1599,15 @@ afar_status batch_build(afar_batch* b) {
     }
     return AFAR_OK;
   };
-  size_t cap_c = b->cmap_n * sizeof(int2), cap_f = b->fmap_n * sizeof(int2);
+  size_t cap_m = b->maps_n * sizeof(int2);
   if ((st = grow(&b->tab, &b->tab_bytes, std::max<size_t>(1, tab.size()) * sizeof(StageArgs<P>)))) return st;
-  if ((st = grow(reinterpret_cast<void**>(&b->cmap), &cap_c, std::max<size_t>(1, cm.size()) * sizeof(int2)))) return st;
-  if ((st = grow(reinterpret_cast<void**>(&b->fmap), &cap_f, std::max<size_t>(1, fm.size()) * sizeof(int2)))) return st;
-  b->cmap_n = cap_c / sizeof(int2);
-  b->fmap_n = cap_f / sizeof(int2);
+  if ((st = grow(reinterpret_cast<void**>(&b->maps), &cap_m, std::max<size_t>(1, all.size()) * sizeof(int2)))) return st;
+  b->maps_n = cap_m / sizeof(int2);
   if (!tab.empty()) {
     AFAR_CUDA(cudaMemcpyAsync(b->tab, tab.data(), tab.size() * sizeof(StageArgs<P>), cudaMemcpyHostToDevice, b->stream));
-    AFAR_CUDA(cudaMemcpyAsync(b->cmap, cm.data(), cm.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
-    AFAR_CUDA(cudaMemcpyAsync(b->fmap, fm.data(), fm.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
+    AFAR_CUDA(cudaMemcpyAsync(b->maps, all.data(), all.size() * sizeof(int2), cudaMemcpyHostToDevice, b->stream));
   }
   AFAR_CUDA(cudaStreamSynchronize(b->stream));
-  b->ncb = (int)cm.size();
-  b->nfb = (int)fm.size();
   b->smem = smem;
   int nfmax = 3;
   for (afar_solver* s : b->members) nfmax = std::max(nfmax, s->maxM);
@@ -1527,32 +1617,88 @@ afar_status batch_build(afar_batch* b) {
     if ((st = raise_smem_limit(kb_reconstruct_tile<P, 3>, b->device, smem))) return st;
     if ((st = raise_smem_limit(kb_reconstruct_tile<P, 4>, b->device, smem))) return st;
   }
-  // capture one step of the whole batch
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
+  b->n_tile = (int)mp_tile.size();
+  b->n_reg = (int)mp_reg.size();
+  b->n_cell = (int)mp_cell.size();
   if (tab.empty()) {
+    b->sched = sc;
     b->dirty = false;
     return AFAR_OK;
   }
   const StageArgs<P>* t = static_cast<const StageArgs<P>*>(b->tab);
+  auto reconstruct = [&]() {
+    if constexpr (P::id == PolicyMixed::id) {
+      if (b->n_tile) {
+        if (nfmax <= 3)
+          kb_reconstruct_tile<P, 3><<<b->n_tile, kTile, b->smem, b->stream>>>(t, b->maps + o_tile);
+        else
+          kb_reconstruct_tile<P, 4><<<b->n_tile, kTile, b->smem, b->stream>>>(t, b->maps + o_tile);
+      }
+      if (b->n_reg) kb_reconstruct_reg<P><<<b->n_reg, kCellBlock, 0, b->stream>>>(t, b->maps + o_reg);
+    } else
+      kb_reconstruct_staged<P><<<b->n_cell, kCellBlock, b->smem, b->stream>>>(t, b->maps + o_cell);
+  };
+
+  if (timed) {
+    // reconstruct once so that the BVD and flux read this step's intermediates, then time each
+    // candidate: a warm-up and the best of three launches (both kernels are functions of the state
+    // and the stage's intermediates; they change neither the state nor the step control)
+    reconstruct();
+    cudaEvent_t e0, e1;
+    AFAR_CUDA(cudaEventCreate(&e0));
+    AFAR_CUDA(cudaEventCreate(&e1));
+    auto best_of = [&](auto&& launch) -> float {
+      launch();
+      float best = 1e30f;
+      for (int r = 0; r < 3; ++r) {
+        cudaEventRecord(e0, b->stream);
+        launch();
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        best = std::min(best, ms);
+      }
+      return best;
+    };
+    for (int k = 0; k < 3; ++k)
+      sc.ms[k] = best_of([&] { launch_bvd<P>(bvd_sizes[k], (int)mp_bvd[k].size(), t, b->maps + o_bvd[k], b->stream); });
+    for (int k = 0; k < 2; ++k)
+      sc.ms[3 + k] =
+          best_of([&] { launch_flux<P, false>(flux_sizes[k], (int)mp_face[k].size(), t, b->maps + o_face[k], b->stream); });
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    AFAR_CUDA(cudaGetLastError());
+    for (afar_solver* m : b->members)
+      if ((st = check_device_error(m))) return st;
+    sc.bvd_block = bvd_sizes[std::min_element(sc.ms, sc.ms + 3) - sc.ms];
+    sc.flux_block = flux_sizes[std::min_element(sc.ms + 3, sc.ms + 5) - (sc.ms + 3)];
+    std::lock_guard<std::mutex> lock(g_batch_tune_mu);
+    g_batch_tune[key] = {sc.bvd_block, sc.flux_block};
+  }
+  const int kb = sc.bvd_block == 64 ? 0 : sc.bvd_block == 128 ? 1 : 2;
+  const int kf = sc.flux_block == 128 ? 0 : 1;
+  const int2* bmap = b->maps + o_bvd[kb];
+  const int2* fmap = b->maps + o_face[kf];
+  b->n_bvd = (int)mp_bvd[kb].size();
+  b->n_face = (int)mp_face[kf].size();
+  b->sched = sc;
+
+  // capture one step of the whole batch
   cudaGraph_t g = nullptr;
   AFAR_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   for (int k = 0; k < 3; ++k) {
-    if constexpr (P::id == PolicyMixed::id) {
-      if (nfmax <= 3)
-        kb_reconstruct_tile<P, 3><<<b->ncb, kTile, b->smem, b->stream>>>(t, b->cmap);
-      else
-        kb_reconstruct_tile<P, 4><<<b->ncb, kTile, b->smem, b->stream>>>(t, b->cmap);
-    } else
-      kb_reconstruct_staged<P><<<b->ncb, kCellBlock, b->smem, b->stream>>>(t, b->cmap);
-    kb_bvd<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap);
+    reconstruct();
+    launch_bvd<P>(sc.bvd_block, b->n_bvd, t, bmap, b->stream);
     if (k == 0)
-      kb_flux<P, true><<<b->nfb, kFaceBlock, 0, b->stream>>>(t, b->fmap);
+      launch_flux<P, true>(sc.flux_block, b->n_face, t, fmap, b->stream);
     else
-      kb_flux<P, false><<<b->nfb, kFaceBlock, 0, b->stream>>>(t, b->fmap);
-    kb_update<P><<<b->ncb, kCellBlock, 0, b->stream>>>(t, b->cmap, stage_coef(k));
+      launch_flux<P, false>(sc.flux_block, b->n_face, t, fmap, b->stream);
+    kb_update<P><<<b->n_cell, kCellBlock, 0, b->stream>>>(t, b->maps + o_cell, stage_coef(k));
   }
   kb_finish_step<P><<<grid_for((long long)tab.size(), 128), 128, 0, b->stream>>>(t, (int)tab.size());
   AFAR_CUDA(cudaStreamEndCapture(b->stream, &g));
@@ -1660,9 +1806,36 @@ extern "C" afar_status afar_batch_destroy(afar_batch* b) {
   for (afar_solver* m : b->members) m->batch = nullptr;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   if (b->tab) cudaFree(b->tab);
-  if (b->cmap) cudaFree(b->cmap);
-  if (b->fmap) cudaFree(b->fmap);
+  if (b->maps) cudaFree(b->maps);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_batch_set_schedule(afar_batch* b, int bvdBlock, int fluxBlock) {
+  if (!b) return (set_error("null batch"), AFAR_ERR_ARGUMENT);
+  if ((bvdBlock != 0 && bvdBlock != 64 && bvdBlock != 128 && bvdBlock != 256) ||
+      (fluxBlock != 0 && fluxBlock != 128 && fluxBlock != 256))
+    return (set_error("afar_batch_set_schedule: BVD block 0/64/128/256, flux block 0/128/256"), AFAR_ERR_ARGUMENT);
+  b->forced_bvd = bvdBlock;
+  b->forced_flux = fluxBlock;
+  b->dirty = true;
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_batch_get_schedule(afar_batch* b, int* tileMembers, int* registerMembers, int* bvdBlock,
+                                               int* fluxBlock, float ms[5]) {
+  if (!b) return (set_error("null batch"), AFAR_ERR_ARGUMENT);
+  if (b->dirty) {
+    AFAR_CUDA(cudaSetDevice(b->device));
+    const afar_status st = b->policy == AFAR_POLICY_MIXED ? batch_build<PolicyMixed>(b) : batch_build<PolicyFP64>(b);
+    if (st) return st;
+  }
+  if (tileMembers) *tileMembers = b->sched.tile_members;
+  if (registerMembers) *registerMembers = b->sched.reg_members;
+  if (bvdBlock) *bvdBlock = b->sched.bvd_block;
+  if (fluxBlock) *fluxBlock = b->sched.flux_block;
+  if (ms)
+    for (int k = 0; k < 5; ++k) ms[k] = b->sched.ms[k];
   return AFAR_OK;
 }

@@ -469,6 +469,19 @@ class Batch:
         check(lib().afar_batch_run(self.h, n_steps, C.byref(ms)))
         return ms.value
 
+    def schedule(self) -> dict:
+        """The autotuner's launch schedule (afar_batch_get_schedule): members on the tile-staged and
+        register-pass reconstruct, BVD and flux block sizes, and the launch times it measured."""
+        t, r, bb, fb = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        ms = (C.c_float * 5)()
+        check(lib().afar_batch_get_schedule(self.h, C.byref(t), C.byref(r), C.byref(bb), C.byref(fb), ms))
+        return {"tile_members": t.value, "register_members": r.value, "bvd_block": bb.value, "flux_block": fb.value,
+                "ms_bvd": {64: ms[0], 128: ms[1], 256: ms[2]}, "ms_flux": {128: ms[3], 256: ms[4]}}
+
+    def set_schedule(self, bvd_block: int = 0, flux_block: int = 0):
+        """Forces the BVD and flux block sizes (0: autotune)."""
+        check(lib().afar_batch_set_schedule(self.h, bvd_block, flux_block))
+
     def close(self):
         if self.h:
             lib().afar_batch_destroy(self.h)

@@ -1125,6 +1125,7 @@ def run_batch(args, dist: Dist):
         s.restore()
     dist.barrier()
     ms = dist.max(batch.run(args.batch_steps))
+    schedule = batch.schedule()
     finite = all(bool(np.isfinite(s.state()["FD"]).all()) for s in solvers)
     batch.close()
     for s in solvers:
@@ -1138,6 +1139,7 @@ def run_batch(args, dist: Dist):
         "data": "synthetic (compression ramps 5k-200k quads, Mach 1.5-4, 5-20 deg, vortex 0-5, seeded)",
         "config": {"workload": "batch_wedges", "solves": args.batch_solves, "cells": int(cells.sum()),
                    "steps": args.batch_steps, "policy": "mixed", "launches_per_step": 13, "setup_s": round(setup_s, 1)},
+        "schedule": schedule,
         "one_after_another": {"value": float(cells.sum()) / (solo_ms * 1e-3), "ms_per_step": solo_ms,
                               "launches_per_step": 13 * args.batch_solves},
         "finite": finite,

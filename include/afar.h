@@ -335,8 +335,7 @@ afar_status afar_set_write_interval(afar_solver* solver, double writeInterval);
 
 /* Periods of a periodic mesh (as in its afar_polyMesh), before afar_setDeviceFieldDataStencil: the
  * device geometry (least-squares rows, face offsets, Courant distances) then takes differences
- * between cell and face centres to the nearest periodic image.  Policies fp64 and mixed (the ref
- * policy's flux recomputes geometry from the raw centres, as the reference's kernel does). */
+ * between cell and face centres to the nearest periodic image.  Policies fp64 and mixed. */
 afar_status afar_set_periodic(afar_solver* solver, double periodX, double periodY);
 
 /* ---- batches: many independent solves stepped by the same kernel launches ------------------- */
@@ -359,6 +358,20 @@ afar_status afar_batch_size(afar_batch* batch, int* members);
  * the batch stream).  Waits for completion. */
 afar_status afar_batch_run(afar_batch* batch, int nSteps, float* ms);
 afar_status afar_batch_destroy(afar_batch* batch);
+/* The batch's launch schedule, picked by the batch autotuner (no counterpart in the reference,
+ * whose kernels run in blocks of BLOCKDIM = 128, basicDataStructure.h:6) when the batch is built
+ * (its first run after members join or leave): each mixed-policy member reconstructs with the
+ * kernel its own solver's autotuner chose for its mesh class (tile-staged or register pass; so a
+ * member's result never depends on its batch-mates), and the BVD and flux kernels run in the block
+ * size that timed fastest on the whole batch (BVD 64, 128 or 256 cells, flux 128 or 256 faces;
+ * best of three launches each), cached per device, policy and batch shape (cells and members, each
+ * to a factor of two).  Block sizes do not change results.  afar_batch_get_schedule reports the
+ * members on each reconstruct, the block sizes and the launch times measured (ms: BVD at 64, 128,
+ * 256, flux at 128, 256; zeros when the decision came from the cache or was forced);
+ * afar_batch_set_schedule forces block sizes (0: autotune). */
+afar_status afar_batch_get_schedule(afar_batch* batch, int* tileMembers, int* registerMembers, int* bvdBlock,
+                                    int* fluxBlock, float ms[5]);
+afar_status afar_batch_set_schedule(afar_batch* batch, int bvdBlock, int fluxBlock);
 
 /* ---- serving: a queue of solve requests on one GPU under a device-memory budget --------------- */
 /* No counterpart in the reference (it runs one case per process).  A server owns a worker thread

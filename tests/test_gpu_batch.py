@@ -192,3 +192,82 @@ def test_batch_rejects_bad_members(cases):
     m.run(1)  # stepping alone again after leaving
     other.close()
     batch.close()
+
+
+@pytest.mark.parametrize("policy", ["mixed", "fp64"])
+def test_batch_schedule_block_sizes_do_not_change_results(cases, policy):
+    """The batch autotuner's choices: every forced BVD/flux block size gives bitwise the same member
+    results (the only reductions are exact minima); the autotuned schedule reports what it timed and
+    a second batch of the same shape takes the cached decision."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch
+
+    names = ["quad_riemann", "ffs_tri", "mixed_riemann"]
+    runs = []
+    for bvd, flux in ((64, 128), (128, 256), (256, 128), (0, 0)):
+        solvers = [_make(cases, n, policy) for n in names]
+        b = Batch(policy)
+        for s in solvers:
+            s.set_step_params()
+            b.add(s)
+        b.set_schedule(bvd, flux)
+        b.run(STEPS)
+        sch = b.schedule()
+        if bvd:
+            assert (sch["bvd_block"], sch["flux_block"]) == (bvd, flux)
+        else:
+            assert sch["bvd_block"] in (64, 128, 256) and sch["flux_block"] in (128, 256)
+        runs.append(([s.state() for s in solvers], [s.time() for s in solvers], sch))
+        b.close()
+        for s in solvers:
+            s.close()
+    for states, times, _ in runs[1:]:
+        for a, b_ in zip(runs[0][0], states):
+            for k in ("FD", "cFD", "shockIndicator"):
+                assert np.array_equal(a[k], b_[k]), k
+        assert times == runs[0][1]
+    # the same shape again: the decision comes from the cache (no launch times measured)
+    solvers = [_make(cases, n, policy) for n in names]
+    b = Batch(policy)
+    for s in solvers:
+        s.set_step_params()
+        b.add(s)
+    sch = b.schedule()
+    auto = runs[-1][2]
+    assert (sch["bvd_block"], sch["flux_block"]) == (auto["bvd_block"], auto["flux_block"])
+    if max(auto["ms_bvd"].values()) > 0:  # this process timed the shape first
+        assert max(sch["ms_bvd"].values()) == 0 and max(sch["ms_flux"].values()) == 0
+    b.close()
+    for s in solvers:
+        s.close()
+
+
+def test_batch_member_keeps_its_own_reconstruct_choice(cases):
+    """A mixed-policy member reconstructs with the kernel its own solver chose (here forced to the
+    register pass): the schedule counts it, and its result is bitwise the same in a batch with
+    other members as in a batch of its own."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch
+
+    def run(with_others):
+        s = _make(cases, "ffs_tri", "mixed")
+        s.set_tuning(1)
+        others = [_make(cases, n, "mixed") for n in (["quad_riemann", "mixed_riemann"] if with_others else [])]
+        for o in others:
+            o.set_tuning(0)
+        b = Batch("mixed")
+        for x in [s] + others:
+            x.set_step_params()
+            b.add(x)
+        b.run(STEPS)
+        sch = b.schedule()
+        st = s.state()
+        b.close()
+        for x in [s] + others:
+            x.close()
+        return st, sch
+
+    alone, sch1 = run(False)
+    mixed, sch3 = run(True)
+    assert sch1["register_members"] == 1 and sch1["tile_members"] == 0
+    assert sch3["register_members"] == 1 and sch3["tile_members"] == 2
+    for k in ("FD", "cFD", "shockIndicator"):
+        assert np.array_equal(alone[k], mixed[k]), k
