@@ -875,15 +875,16 @@ def fp64_perturbation_floor(hf, cfg, device, n_steps=0, t_end=0.0, every=10, ini
     return out
 
 
-def fp64_reorder_floor(m, make_fields, cfg, device, n_steps=0, t_end=0.0, every=10):
+def fp64_reorder_floor(make_mesh, make_fields, cfg, device, n_steps=0, t_end=0.0, every=10):
     """The FP64 policy against itself on the same mesh with its cells in another order (reverse
     Cuthill-McKee as generated, and along a Hilbert curve): the face and stencil lists, and so every
     summation, follow the numbering, and the O3 weights are solved with the stencil rows permuted.
     Both solves take the first one's step sizes; the states are compared cell for cell (matched by
-    centroid).  make_fields(mesh) -> (W, Wb, U or None)."""
-    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver, mesh, precompute
+    centroid).  make_mesh(order) builds the mesh in "rcm" or "hilbert" order; make_fields(mesh) ->
+    (W, Wb, U or None)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver, precompute
 
-    m2 = mesh.renumber_mesh(m, "hilbert")
+    m, m2 = make_mesh("rcm"), make_mesh("hilbert")
     c1, c2 = m.cell_centres(), m2.cell_centres()
     o1, o2 = np.lexsort((c1[:, 1], c1[:, 0])), np.lexsort((c2[:, 1], c2[:, 0]))
     to2 = np.empty(m.n_cells, dtype=np.int64)
@@ -962,6 +963,7 @@ def run_accuracy(args, dist: Dist):
                 return mesh.primitive_from_conserved(U), None, U
 
             run, init = {"t_end": 2.0, "every": 25}, (W0, U0)
+            make_mesh = lambda o: mesh.periodic_quad_grid(256, 256, 0.0, 10.0, 0.0, 10.0, renumber=o)
         elif name == "step":
             m = mesh.forward_step_triangles(args.points, seed=args.seed)
             W, Wb = mesh.uniform_fields(m, 1.0, 3.0, 0.0, 1.0)
@@ -973,6 +975,7 @@ def run_accuracy(args, dist: Dist):
                 return (*mesh.uniform_fields(mm, 1.0, 3.0, 0.0, 1.0), None)
 
             run, init = {"n_steps": args.acc_steps, "every": 10}, None
+            make_mesh = lambda o: mesh.forward_step_triangles(args.points, seed=args.seed, renumber=o)
         elif name == "riemann_mixed":
             m = mesh.riemann_mixed(args.mixed_n, seed=args.seed)
             W, Wb = mesh.riemann_fields(m)
@@ -984,6 +987,7 @@ def run_accuracy(args, dist: Dist):
                 return (*mesh.riemann_fields(mm), None)
 
             run, init = {"t_end": 0.3, "every": 100}, None
+            make_mesh = lambda o: mesh.riemann_mixed(args.mixed_n, seed=args.seed, renumber=o)
         elif name == "batch":
             rng = np.random.default_rng(args.seed)
             params = [batch_member_params(rng) for _ in range(args.batch_solves)]
@@ -997,7 +1001,8 @@ def run_accuracy(args, dist: Dist):
                 if args.floor:
                     brun = {"n_steps": args.batch_steps, "every": 50}
                     rk["fp64_floor_reorder"] = fp64_reorder_floor(
-                        mm, lambda m_, p_=params[k]: (*batch_member_fields(m_, p_), None), cfg, dev, **brun)
+                        lambda o, p_=params[k]: batch_member_mesh(p_, renumber=o),
+                        lambda m_, p_=params[k]: (*batch_member_fields(m_, p_), None), cfg, dev, **brun)
                     rk["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, dev, **brun)
                 members.append(rk)
             r = {"members": members, "L1_rho_max": max(x["L1_rho"] for x in members),
@@ -1009,7 +1014,7 @@ def run_accuracy(args, dist: Dist):
         if hf is not None:
             line["cells"] = hf.nc
             if args.floor:
-                r["fp64_floor_reorder"] = fp64_reorder_floor(m, fields, cfg, dev, **run)
+                r["fp64_floor_reorder"] = fp64_reorder_floor(make_mesh, fields, cfg, dev, **run)
                 r["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, dev, init=init, **run)
         line.update(r)
         line["wall_s"] = round(time.time() - t0, 1)
@@ -1070,11 +1075,18 @@ def batch_member(params):
     isentropic vortex carried in the stream; face-neighbour stencils, CFL 0.3."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import CaseConfig, mesh
 
-    nc, angle, u0, strength = params
-    ny = max(8, int(round(np.sqrt(nc / 2.0))))
-    m = mesh.wedge_quads(2 * ny, ny, angle)
+    m = batch_member_mesh(params)
     W, Wb = batch_member_fields(m, params)
     return m, W, Wb, CaseConfig(stencilType="faceNeighbour", CFL=0.3)
+
+
+def batch_member_mesh(params, renumber="rcm"):
+    """The compression-ramp mesh of a batched solve (quads in a 2:1 channel)."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import mesh
+
+    nc, angle, _, _ = params
+    ny = max(8, int(round(np.sqrt(nc / 2.0))))
+    return mesh.wedge_quads(2 * ny, ny, angle, renumber=renumber)
 
 
 def batch_member_fields(m, params):
