@@ -122,6 +122,7 @@ def lib():
             "afar_download_ls_matrix": (S, [_p, _p]),
             "afar_device_bytes": (S, [_p, C.POINTER(C.c_size_t)]),
             "afar_measure_fp64_peak": (S, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float)]),
+            "afar_debug_wait_injection": (S, [C.c_int, C.c_uint, C.c_longlong]),
             "afar_launches_per_step": (C.c_int, [_p]),
             "afar_set_step_params": (S, [_p, C.c_double, C.c_double, C.c_double]),
             "afar_set_write_interval": (S, [_p, C.c_double]),
@@ -179,4 +180,5 @@ EXPORTED = [
     "afar_set_write_interval", "afar_set_periodic", "afar_set_tuning", "afar_get_tuning", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
     "afar_batch_destroy", "afar_batch_get_schedule", "afar_batch_set_schedule", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
     "afar_server_destroy", "afar_server_cancel", "afar_switch_counts", "afar_measure_fp64_peak",
+    "afar_debug_wait_injection",
 ]

@@ -321,6 +321,12 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
 // one mbarrier) instead of per-thread loads: ~50 KB per tile in flight from a handful of lanes,
 // while registers stay free for the stencil gathers, which hit L2.
 constexpr int kTile = 128;
+// Test hooks of the tile's bounded waits (afar_debug_wait_injection): the wait limit in SM clocks,
+// and bytes added to the transaction count the first barrier of every tile expects (never issued,
+// so that barrier cannot complete and its wait runs out).  2^31 clocks and no extra bytes in normal
+// operation.
+static __device__ long long g_tile_wait_limit = 1ll << 31;
+static __device__ unsigned g_tile_extra_tx = 0;
 struct ReconTile {
   unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_bar, bytes;
 };
@@ -364,7 +370,7 @@ __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const in
   const int rows = 4 * M + S + M * S + 1;  // weight rows 1..S of each face slot (row 0, the cell's own
                                            // weight, drops out of the difference-form sums)
   if (lane == 0) {
-    mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16);
+    mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16 + g_tile_extra_tx);
     mbar_arrive_expect_tx(bar + 1, ne * (M * (8 + 8 + 8) + M * S * 4));
   }
   __syncwarp();
@@ -437,15 +443,16 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   if (t < 32) recon_tile_fetch(a, blk, L, sm, bar);
   const int c = blk * kTile + t;
   const int nS = c < a.Nc ? a.nS[c] : 0, nM = c < a.Nc ? a.nM[c] : 0;
+  const long long limit = g_tile_wait_limit;
   // leaving: every copy into this block's shared memory must have landed first
   auto give_up = [&]() {
     if (t == 0) atomicOr(&a.ctl->err, 1u);
-    mbar_wait_bounded(bar, 0);
-    mbar_wait_bounded(bar + 1, 0);
+    mbar_wait_bounded(bar, 0, limit);
+    mbar_wait_bounded(bar + 1, 0, limit);
   };
-  if (!mbar_wait_bounded(bar, 0)) return give_up();
+  if (!mbar_wait_bounded(bar, 0, limit)) return give_up();
   if (c >= a.Nc) {
-    if (!mbar_wait_bounded(bar + 1, 0)) give_up();
+    if (!mbar_wait_bounded(bar + 1, 0, limit)) give_up();
     return;
   }
   const int* s_cf = reinterpret_cast<const int*>(sm + L.off_cf);
@@ -471,7 +478,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
 #pragma unroll
   for (int u = 0; u < U; ++u)
     if (u < nS) wj[u] = a.W[s_sten[u * kTile + t]];
-  if (!mbar_wait_bounded(bar + 1, 0)) return give_up();
+  if (!mbar_wait_bounded(bar + 1, 0, limit)) return give_up();
   // O3 weights of boundary-face and missing slots are zero in the operator rows (setup), so only
   // slots past this mesh's largest cell (a batch may stage fewer rows than NF) are skipped
   const int nfm = a.maxM;

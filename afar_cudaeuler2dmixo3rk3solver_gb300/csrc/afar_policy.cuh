@@ -114,11 +114,13 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
       : "memory");
   return ok != 0;
 }
-// Waits for phase `parity` of the barrier for at most ~1 s of SM clocks; false if it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+// Waits for phase `parity` of the barrier for at most `limit` SM clocks (by default 2^31, about
+// 1 s); false if it gave up.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  const long long limit = 1ll << 31) {
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity))
-    if (clock64() - t0 > (1ll << 31)) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 

@@ -1839,3 +1839,12 @@ extern "C" afar_status afar_batch_get_schedule(afar_batch* b, int* tileMembers, 
     for (int k = 0; k < 5; ++k) ms[k] = b->sched.ms[k];
   return AFAR_OK;
 }
+
+extern "C" afar_status afar_debug_wait_injection(int device, unsigned extraBytes, long long limitClocks) {
+  AFAR_CUDA(cudaSetDevice(device));
+  const long long lim = limitClocks > 0 ? limitClocks : (1ll << 31);
+  AFAR_CUDA(cudaMemcpyToSymbol(g_tile_extra_tx, &extraBytes, sizeof(extraBytes)));
+  AFAR_CUDA(cudaMemcpyToSymbol(g_tile_wait_limit, &lim, sizeof(lim)));
+  AFAR_CUDA(cudaDeviceSynchronize());
+  return AFAR_OK;
+}

@@ -476,6 +476,16 @@ afar_status afar_get_tuning(afar_solver* solver, int* reconVariant, float* msTil
  * fp64 policy, whose flux and update are bound by the FP64 pipe rather than by memory. */
 afar_status afar_measure_fp64_peak(int device, double* gflops, float* ms);
 
+/* Test hook for the bounded device waits (no counterpart in the reference).  The mixed policy's
+ * tile-staged reconstruct waits on mbarriers for its bulk copies; each wait gives up after a limit
+ * of SM clocks (2^31, about a second), marks the solver's error word and lets the kernel return, so
+ * that the call which waits next returns AFAR_ERR_CUDA ("... the state is not valid") and the CUDA
+ * context stays usable.  extraBytes > 0 adds that many bytes to the transaction count the first
+ * barrier of every tile expects (bytes never issued, so those waits run out); limitClocks > 0
+ * replaces the limit (<= 0: the default).  afar_debug_wait_injection(device, 0, 0) restores normal
+ * operation.  Affects every solver and batch on the device until then. */
+afar_status afar_debug_wait_injection(int device, unsigned extraBytes, long long limitClocks);
+
 /* Number of kernel launches one afar_run step issues on this solver (for accounting). */
 int afar_launches_per_step(afar_solver* solver);
 

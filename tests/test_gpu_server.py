@@ -157,3 +157,37 @@ def test_non_finite_request_fails_alone(cases):
     st = srv.stats()
     assert st["failed"] == 1 and st["completed"] == 1
     srv.close()
+
+
+def test_late_arrivals_join_the_running_batch(cases):
+    """Continuous batching: requests submitted after the batch has started stepping are admitted
+    at the next chunk boundary while the first solve is still running, finish before it, and every
+    result -- the late ones and the long one -- is bitwise its result in a batch of its own."""
+    import time
+
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Server
+
+    long_steps = 20000  # the smooth vortex box: stays finite, keeps the batch busy for a while
+    srv = Server("mixed", chunk_steps=5)
+    first = srv.submit(*cases["vortex_box"], n_steps=long_steps)
+    t0 = time.time()
+    while srv.stats()["batchSteps"] == 0 and time.time() - t0 < 60:
+        time.sleep(0.001)
+    assert srv.stats()["batchSteps"] > 0, "the batch never started stepping"
+    late = [("quad_riemann", 0.02, 0), ("ffs_tri", 0.0, 7), ("mixed_riemann", 0.0, 12)]
+    ids = [srv.submit(*cases[n], t_end=t, n_steps=k) for n, t, k in late]
+    overlap = 0
+    for rid, (n, t, k) in zip(ids, late):
+        FD, si, _ = srv.wait(rid, timeout=120.0)
+        overlap = max(overlap, srv.stats()["peakRunning"])
+        ref = _alone(*cases[n], "mixed", t, k)
+        assert np.array_equal(FD, ref["FD"]), n
+        assert np.array_equal(si, ref["shockIndicator"]), n
+    st = srv.stats()
+    assert st["completed"] == len(late) and st["running"] == 1, st  # the long solve is still stepping
+    assert overlap >= 2
+    FD, si, _, steps = srv.wait(first, timeout=300.0, with_steps=True)
+    assert steps == long_steps
+    ref = _alone(*cases["vortex_box"], "mixed", 0.0, long_steps)
+    assert np.array_equal(FD, ref["FD"]) and np.array_equal(si, ref["shockIndicator"])
+    srv.close()
