@@ -93,6 +93,9 @@ def lib():
             "afar_free_host_fields": (None, [C.POINTER(FieldPointer)]),
             "afar_precompute_fields_device": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), _p, _p, C.c_int,
                                                   C.POINTER(FieldPointer), C.POINTER(FieldSizes), C.POINTER(_p)]),
+            "afar_precompute_fields_gauss": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), _p, _p, C.c_int,
+                                                 C.POINTER(FieldPointer), C.POINTER(FieldSizes), C.POINTER(_p),
+                                                 C.POINTER(_p), C.POINTER(C.c_int)]),
             "afar_gauss_quadrature": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), _p, _p, _p, C.POINTER(C.c_int)]),
             "afar_face_gauss_quadrature": (S, [C.POINTER(PolyMesh), C.POINTER(CaseConfig), C.POINTER(C.c_int), _p, _p]),
             "afar_solver_create": (S, [C.POINTER(_p), C.c_int, C.c_int]),
@@ -123,6 +126,7 @@ def lib():
             "afar_device_bytes": (S, [_p, C.POINTER(C.c_size_t)]),
             "afar_measure_fp64_peak": (S, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_float)]),
             "afar_debug_wait_injection": (S, [C.c_int, C.c_uint, C.c_longlong]),
+            "afar_set_face_gauss_flux": (S, [_p, C.c_int, _p, _p, _p]),
             "afar_launches_per_step": (C.c_int, [_p]),
             "afar_set_step_params": (S, [_p, C.c_double, C.c_double, C.c_double]),
             "afar_set_write_interval": (S, [_p, C.c_double]),
@@ -171,7 +175,7 @@ def ptr(a):
 EXPORTED = [
     "afar_last_error", "afar_default_case_config", "afar_precompute_fields", "afar_free_host_fields",
     "afar_precompute_fields_device",
-    "afar_gauss_quadrature", "afar_face_gauss_quadrature", "afar_solver_create", "afar_setDeviceFieldData", "afar_setDeviceFieldDataStencil",
+    "afar_gauss_quadrature", "afar_face_gauss_quadrature", "afar_precompute_fields_gauss", "afar_solver_create", "afar_setDeviceFieldData", "afar_setDeviceFieldDataStencil",
     "afar_adjustTimeStep", "afar_GPUevolve", "afar_copyFieldDataDeviceToHost", "afar_freeFieldData", "afar_set_gas",
     "afar_set_rbf_basis64", "afar_run", "afar_run_async", "afar_synchronize", "afar_get_stream", "afar_get_time",
     "afar_set_time", "afar_stage_debug", "afar_debug_limiter64", "afar_upload_state", "afar_download_state",
@@ -180,5 +184,5 @@ EXPORTED = [
     "afar_set_write_interval", "afar_set_periodic", "afar_set_tuning", "afar_get_tuning", "afar_batch_create", "afar_batch_add", "afar_batch_remove", "afar_batch_size", "afar_batch_run",
     "afar_batch_destroy", "afar_batch_get_schedule", "afar_batch_set_schedule", "afar_server_create", "afar_server_submit", "afar_server_wait", "afar_server_get_stats",
     "afar_server_destroy", "afar_server_cancel", "afar_switch_counts", "afar_measure_fp64_peak",
-    "afar_debug_wait_injection",
+    "afar_debug_wait_injection", "afar_set_face_gauss_flux",
 ]

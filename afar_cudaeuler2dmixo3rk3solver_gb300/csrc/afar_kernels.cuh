@@ -101,6 +101,13 @@ struct StageArgs {
   float Rf, Cvf, gRf;  // R, Cv and gamma*R as floats (mixed)
   double px, py;       // periods of a periodic mesh (0: none); setup kernels only
   const V2<float>* dtgf;  // Nf (delta r, fraction) as floats (mixed Courant estimate)
+  // the optional multi-point face flux (ng > 0 points per face; 0: the face-centre flux)
+  int ng;
+  const S* wg;       // [(maxM*ng)*(maxS+1)][ldc] O3 weights at the face Gauss points, per cell slot
+  const V2<G>* sgk;  // [maxM*ng][ldc] point minus cell centre, per cell slot
+  const V2<G>* fgk;  // [Nf*ng] point minus face centre
+  V4<G>* fvg;        // [2Nf*ng] face values at the points ((2f + side)*ng + k)
+  G gw[4];           // the points' weights, normalised to sum to one
 };
 
 // limiterProcess (reference cudaLimiter.h:35-50)
@@ -1626,6 +1633,187 @@ __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const StageCoef 
   update_body<P>(a, blockIdx.x, k);
 }
 
+// ---------------------------------------------------------------- the multi-point face flux
+// An option of the fp64 and mixed policies (no counterpart in the reference, whose flux uses the
+// face centre): the face flux as the weighted sum of the fluxes at the face's Gauss points.  The
+// switch decisions (troubled cells, BVD) stay those of the face-centre values; at each point the
+// state is the O3 value there, or the TVD state extrapolated there with the cell's limited
+// gradient, as the cell's switch asks.
+
+// The face values of a cell's side of each internal face at the Gauss points, with the selection
+// rules of the face-centre values (recon_*_body): the O3 value where the variable varies over the
+// compact stencil by at least 1e-5, else its unlimited linear value; every variable linear in a
+// cell of flat temperature.  Runs after the reconstruct, whose gradient it reads.
+template <class P>
+__global__ void __launch_bounds__(128) k_reconstruct_gauss(StageArgs<P> a) {
+  using S = typename P::S;
+  using G = typename P::G;
+  using WT = typename P::W;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int ldc = a.ldc, nS = a.nS[c], nM = a.nM[c], ng = a.ng, wrow = a.maxS + 1;
+  const V4<WT> wc = a.W[c];
+  const S pc = (S)wc.x, uxc = (S)wc.y, uyc = (S)wc.z, tc = (S)wc.w;
+  S pMax = pc, pMin = pc, uxMax = uxc, uxMin = uxc, uyMax = uyc, uyMin = uyc, tMax = tc, tMin = tc;
+  for (int i = 0; i < nM; ++i) {
+    const V4<WT> v = a.W[a.sten[i * ldc + c]];
+    pMax = fmx((S)v.x, pMax);
+    pMin = fmn((S)v.x, pMin);
+    uxMax = fmx((S)v.y, uxMax);
+    uxMin = fmn((S)v.y, uxMin);
+    uyMax = fmx((S)v.z, uyMax);
+    uyMin = fmn((S)v.z, uyMin);
+    tMax = fmx((S)v.w, tMax);
+    tMin = fmn((S)v.w, tMin);
+  }
+  const V4<G> g0 = a.grad[2 * c], g1 = a.grad[2 * c + 1];  // (px py uxx uxy), (uyx uyy tx ty)
+  const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
+  const bool flat = fab(tMax - tMin) < VSMALL;
+  const bool o3p = !flat && fab(pMax - pMin) >= SMALL, o3ux = !flat && fab(uxMax - uxMin) >= SMALL;
+  const bool o3uy = !flat && fab(uyMax - uyMin) >= SMALL, o3t = !flat && fab(tMax - tMin) >= SMALL;
+  for (int fi = 0; fi < nM; ++fi) {
+    const int fid = a.cf[fi * ldc + c];
+    const int f = abs(fid) - 1;
+    if (f >= a.Nf) continue;
+    const int side = fid < 0;
+    for (int k = 0; k < ng; ++k) {
+      const V2<G> d = a.sgk[(fi * ng + k) * ldc + c];
+      V4<G> o;
+      o.x = (G)pc + g0.x * d.x + g0.y * d.y;
+      o.y = (G)uxc + g0.z * d.x + g1.x * d.y;
+      o.z = (G)uyc + g0.w * d.x + g1.y * d.y;
+      o.w = (G)tc + g1.z * d.x + g1.w * d.y;
+      if (o3p || o3ux || o3uy || o3t) {
+        const S* w = a.wg + (size_t)((fi * ng + k) * wrow) * ldc + c;
+        G sp, sux, suy, st;
+        if constexpr (std::is_same<G, float>::value) {  // mixed: the difference form of recon_tile_body
+          sp = sux = suy = st = G(0);
+          for (int j = 0; j < nS; ++j) {
+            const S wj = w[(size_t)(j + 1) * ldc];
+            const V4<WT> v = a.W[a.sten[j * ldc + c]];
+            sp += wj * ((S)v.x - pc);
+            sux += wj * ((S)v.y - uxc);
+            suy += wj * ((S)v.z - uyc);
+            st += wj * ((S)v.w - tc);
+          }
+          sp += (G)pc;
+          sux += (G)uxc;
+          suy += (G)uyc;
+          st += (G)tc;
+        } else {  // fp64: the plain sum, the cell itself first
+          const S w0 = w[0];
+          sp = w0 * pc;
+          sux = w0 * uxc;
+          suy = w0 * uyc;
+          st = w0 * tc;
+          for (int j = 0; j < nS; ++j) {
+            const S wj = w[(size_t)(j + 1) * ldc];
+            const V4<WT> v = a.W[a.sten[j * ldc + c]];
+            sp += wj * (S)v.x;
+            sux += wj * (S)v.y;
+            suy += wj * (S)v.z;
+            st += wj * (S)v.w;
+          }
+        }
+        if (o3p) o.x = sp;
+        if (o3ux) o.y = sux;
+        if (o3uy) o.z = suy;
+        if (o3t) o.w = st;
+      }
+      a.fvg[(2 * f + side) * ng + k] = o;
+    }
+  }
+}
+
+// The multi-point face flux: for each internal face, the flux at every Gauss point (state
+// selection, minimised jumps, central flux and Roe/KFVS dissipation as in flux_body) times the
+// point's weight, summed; boundary faces as flux_body (the ghost state is constant along the face,
+// so its flux is the same at every point).  The Courant step of the first stage runs as k_delta_t.
+template <class P>
+__global__ void __launch_bounds__(256) k_flux_gauss(StageArgs<P> a) {
+  using S = typename P::S;
+  using G = typename P::G;
+  const int id = blockIdx.x * blockDim.x + threadIdx.x;
+  G R, Cv, iR;
+  if constexpr (std::is_same<G, float>::value) {
+    R = a.Rf;
+    Cv = a.Cvf;
+    iR = a.invRf;
+  } else {
+    R = (G)a.R;
+    Cv = (G)a.Cv;
+    iR = (G)a.invR;
+  }
+  if (id < a.Nf) {
+    const int2 on = a.on[id];
+    const int cell[2] = {on.x, on.y};
+    const V4<G> fd = a.fd[id];
+    const int8_t sw[2] = {a.si[2 * on.x + 1], a.si[2 * on.y + 1]};
+    const bool isShock = sw[0] < 0 || sw[1] < 0;
+    const V4<G> fs = a.fs[id];
+    const G Sfx = fs.x, Sfy = fs.y, magSf = fs.z, nfx = Sfx * fs.w, nfy = Sfy * fs.w;
+    const G gam = std::is_same<G, float>::value ? (G)(a.gm1f + 1.f) : (G)a.gamma;
+    const G K = G(2) * Cv * iR - G(2);
+    G acc[4] = {G(0), G(0), G(0), G(0)};
+    for (int k = 0; k < a.ng; ++k) {
+      const V2<G> off = a.fgk[id * a.ng + k];
+      G st[2][4], T[2][4], rho[2], rhoT[2];
+#pragma unroll
+      for (int sd = 0; sd < 2; ++sd) {
+        const int c = cell[sd];
+        const G dx = (sd ? fd.z : fd.x) + off.x, dy = (sd ? fd.w : fd.y) + off.y;
+        const V4<typename P::W> w = a.W[c];
+        const V4<G> g0 = a.grad[2 * c], g1 = a.grad[2 * c + 1];
+        const V4<S> l = a.lim[c];
+        T[sd][0] = (G)w.x + l.x * (g0.x * dx + g0.y * dy);
+        T[sd][1] = (G)w.y + l.y * (g0.z * dx + g1.x * dy);
+        T[sd][2] = (G)w.z + l.z * (g0.w * dx + g1.y * dy);
+        T[sd][3] = (G)w.w + l.w * (g1.z * dx + g1.w * dy);
+        const V4<G> o3 = a.fvg[(2 * id + sd) * a.ng + k];
+        const bool tvd = sw[sd] != 0;
+        st[sd][0] = tvd ? T[sd][0] : o3.x;
+        st[sd][1] = tvd ? T[sd][1] : o3.y;
+        st[sd][2] = tvd ? T[sd][2] : o3.z;
+        st[sd][3] = tvd ? T[sd][3] : o3.w;
+        rho[sd] = fdiv(st[sd][0] * iR, st[sd][3]);
+        rhoT[sd] = fdiv(T[sd][0] * iR, T[sd][3]);
+      }
+      const G dP = min_delta<G, G>(st[0][0], st[1][0], T[0][0], T[1][0]);
+      const G dRho = min_delta<G, G>(rho[0], rho[1], rhoT[0], rhoT[1]);
+      const G h = G(0.5);
+      G F0 = h * rho[0] * (st[0][1] * Sfx + st[0][2] * Sfy) + h * rho[1] * (st[1][1] * Sfx + st[1][2] * Sfy);
+      G F1 = h * (F0 * st[0][1] + st[0][0] * Sfx) + h * (F0 * st[1][1] + st[1][0] * Sfx);
+      G F2 = h * (F0 * st[0][2] + st[0][0] * Sfy) + h * (F0 * st[1][2] + st[1][0] * Sfy);
+      G F3 = h * F0 * (Cv * st[0][3] + h * (st[0][1] * st[0][1] + st[0][2] * st[0][2]) + R * st[0][3]) +
+             h * F0 * (Cv * st[1][3] + h * (st[1][1] * st[1][1] + st[1][2] * st[1][2]) + R * st[1][3]);
+      if (isShock)
+        kfvs_flux_fast<G>(F0, F1, F2, F3, rho[0], rho[1], st[0][0], st[1][0], st[0][1], st[1][1], st[0][2], st[1][2],
+                          st[0][3], st[1][3], R, Cv, K, magSf, nfx, nfy);
+      else
+        roe_flux_fast<G>(F0, F1, F2, F3, rho[0], rho[1], st[0][1], st[1][1], st[0][2], st[1][2], st[0][3], st[1][3],
+                         dP, dRho, R, Cv, gam, magSf, nfx, nfy);
+      const G wk = a.gw[k];
+      acc[0] += wk * F0;
+      acc[1] += wk * F1;
+      acc[2] += wk * F2;
+      acc[3] += wk * F3;
+    }
+    a.flux[id] = V4<typename P::F>{(typename P::F)acc[0], (typename P::F)acc[1], (typename P::F)acc[2],
+                                   (typename P::F)acc[3]};
+  } else if (id < a.Nf + a.Nb) {  // boundary faces: the Euler flux of the ghost state
+    const int b = id - a.Nf;
+    const V4<typename P::W> wb = a.W[a.Nc + b];
+    const V4<G> fs = a.fs[id];
+    const G Sfx = fs.x, Sfy = fs.y;
+    const G bp = wb.x, bUx = wb.y, bUy = wb.z, bT = wb.w;
+    const G rho = bp / (R * bT);
+    const G rhoFlux = rho * (bUx * Sfx + bUy * Sfy);
+    a.flux[id] = V4<typename P::F>{(typename P::F)rhoFlux, (typename P::F)(rhoFlux * bUx + bp * Sfx),
+                                   (typename P::F)(rhoFlux * bUy + bp * Sfy),
+                                   (typename P::F)(rhoFlux * (Cv * bT + G(0.5) * (bUx * bUx + bUy * bUy) + bp / rho))};
+  }
+}
+
 // ------------------------------------------------------------------------- batch kernels
 // Many independent solves in one launch: block b works on solve map[b].x (its arguments are
 // tab[map[b].x]), as that solve's block map[b].y.  A block never spans two solves, so block-level
@@ -1864,6 +2052,42 @@ __global__ void k_setup_face_geom(StageArgs<P> a, const V4<double>* faceXY, cons
     const int b = f - a.Nf;
     const_cast<V2<double>*>(a.bn)[b] = V2<double>{s.x / s.z, s.y / s.z};
   }
+}
+
+// The multi-point face flux's per-cell arrays from the face-ordered inputs: each cell slot's O3
+// weights at the points (its side's row of rbfg [face][side][point][maxS+1]; zeros past the stencil
+// and for boundary faces) and the points minus the cell centre (nearest periodic image).
+template <class P>
+__global__ void k_setup_gauss(StageArgs<P> a, const double* rbfg, const double* pts) {
+  using S = typename P::S;
+  using G = typename P::G;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.Nc) return;
+  const int ng = a.ng, nmax = a.maxS + 1, ldc = a.ldc;
+  S* wg = const_cast<S*>(a.wg);
+  V2<G>* sgk = const_cast<V2<G>*>(a.sgk);
+  const double x0 = a.cellC[c].x, y0 = a.cellC[c].y;
+  for (int fi = 0; fi < a.nM[c]; ++fi) {
+    const int fid = a.cf[fi * ldc + c];
+    const int f = abs(fid) - 1;
+    if (f >= a.Nf) continue;
+    const int side = fid < 0;
+    for (int k = 0; k < ng; ++k) {
+      const double px = pts[2 * ((size_t)f * ng + k)], py = pts[2 * ((size_t)f * ng + k) + 1];
+      sgk[(fi * ng + k) * ldc + c] = V2<G>{(G)wrapd(px - x0, a.px), (G)wrapd(py - y0, a.py)};
+      const double* src = rbfg + (((size_t)f * 2 + side) * ng + k) * nmax;
+      for (int j = 0; j <= a.nS[c]; ++j) wg[(size_t)((fi * ng + k) * nmax + j) * ldc + c] = (S)src[j];
+    }
+  }
+}
+template <class P>
+__global__ void k_setup_gauss_faces(StageArgs<P> a, const double* pts, const V4<double>* faceXY) {
+  using G = typename P::G;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.Nf * a.ng) return;
+  const int f = i / a.ng;
+  const V4<double> xy = faceXY[f];
+  const_cast<V2<G>*>(a.fgk)[i] = V2<G>{(G)wrapd(pts[2 * (size_t)i] - xy.x, a.px), (G)wrapd(pts[2 * (size_t)i + 1] - xy.y, a.py)};
 }
 
 }  // namespace afar

@@ -527,8 +527,10 @@ static T* xalloc(size_t n) {
 
 // The whole precompute; the RBF stage runs on CUDA device `device` when it is >= 0, else on the host.
 static afar_status precompute(const afar_polyMesh* m, const afar_caseConfig* cfg, const double* Wc, const double* Wb,
-                              int device, afar_fieldPointer* h, afar_fieldSizes* sz, double** rbf64_out) {
+                              int device, afar_fieldPointer* h, afar_fieldSizes* sz, double** rbf64_out,
+                              double** gauss_out = nullptr, int* gauss_n = nullptr) {
   if (rbf64_out) *rbf64_out = nullptr;
+  if (gauss_out) *gauss_out = nullptr;
   if (!check_mesh(m)) return AFAR_ERR_ARGUMENT;
   if (!cfg || !Wc || !h || !sz) {
     set_error("afar_precompute_fields: null argument");
@@ -772,13 +774,18 @@ static afar_status precompute(const afar_polyMesh* m, const afar_caseConfig* cfg
       std::free(rbf64);
       return st;
     }
-  } else {
-  // ---- RBF P matrices, pseudo-inverses, trouble flags (basicCUDAsolver.cpp:461-533)
-  std::vector<double> refd(nc, 0.0);
-  std::vector<double> Gall((size_t)nc * nmax * nmax, 0.0);
-  std::vector<char> trouble(nc, 0);
+  }
+  // ---- RBF P matrices, pseudo-inverses, trouble flags (basicCUDAsolver.cpp:461-533): on the host
+  // for the host stage, and for the face Gauss-point weights when they are asked for
+  std::vector<double> refd;
+  std::vector<double> Gall;
+  std::vector<char> trouble;
   const double shape = cfg->shapeFactor;
   const afar_meshCellData* CELL = h->CELL;
+  auto build_inverses = [&]() {
+  refd.assign(nc, 0.0);
+  Gall.assign((size_t)nc * nmax * nmax, 0.0);
+  trouble.assign(nc, 0);
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
 #endif
@@ -815,6 +822,37 @@ static afar_status precompute(const afar_polyMesh* m, const afar_caseConfig* cfg
         break;
       }
   }
+  };
+  // The O3 weights of cell c at point (x, y): (G^T b) corrected to sum to one, b the multiquadric
+  // basis of the stencil at the point (basicCUDAsolver.cpp:585-619); a troubled cell's weights
+  // select the cell itself.  n = stencil size + 1 values into out.
+  auto o3_weights = [&](const int c, const double x, const double y, double* out) {
+    const int n = h->stencilSize[c] + 1;
+    if (trouble[c]) {
+      out[0] = 1.0;
+      for (int i = 1; i < n; ++i) out[i] = 0.0;
+      return;
+    }
+    const int* st = &gsten[(size_t)maxS * c];
+    const double rd = refd[c];
+    double bvec[AFAR_MAX_VALID_STENCIL_SIZE + 1];
+    for (int i = 0; i < n; ++i) {
+      const int si = i == 0 ? c : st[i - 1];
+      const double ex = wrapd(x - CELL[si].x, px) / rd, ey = wrapd(y - CELL[si].y, py) / rd;
+      bvec[i] = std::sqrt(shape + (ex * ex + ey * ey));
+    }
+    const double* G = &Gall[(size_t)c * nmax * nmax];
+    double sum = 0.0;
+    for (int i = 0; i < n; ++i) {  // (G^T b)_i = sum_j G(j,i) b_j
+      double acc = 0.0;
+      for (int j = 0; j < n; ++j) acc += G[j * n + i] * bvec[j];
+      out[i] = acc;
+      sum += acc;
+    }
+    for (int i = 0; i < n; ++i) out[i] = out[i] - sum / double(n) + 1.0 / double(n);
+  };
+  if (device < 0) {
+  build_inverses();
 
   // ---- O3 face weights (basicCUDAsolver.cpp:538-619), stored as float
 #ifdef _OPENMP
@@ -859,8 +897,40 @@ static afar_status precompute(const afar_polyMesh* m, const afar_caseConfig* cfg
       }
     }
   }
-  std::vector<double>().swap(Gall);
   }
+  if (gauss_out) {
+    // ---- O3 weights at the face Gauss points (the optional multi-point face flux): the fOrder
+    // bar rule on each internal face (d2GaussQuadrature.C:153-214), the weights of both sides'
+    // stencils at every point, [face][side][point][maxS+1]
+    if (Gall.empty()) build_inverses();
+    std::vector<double> bp, bw;
+    bar_rule(cfg->fOrder, bp, bw);
+    const int ng = (int)bp.size();
+    double* gw = xalloc<double>((size_t)nf * 2 * ng * nmax);
+    if (!gw) {
+      set_error("out of host memory for the face Gauss-point weights");
+      afar_free_host_fields(h);
+      std::free(rbf64);
+      return AFAR_ERR_LIMIT;
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1024) num_threads(nthreads)
+#endif
+    for (int f = 0; f < nf; ++f) {
+      const int a = m->facePoints[2 * f], b = m->facePoints[2 * f + 1];
+      const double xa = m->points[2 * a], ya = m->points[2 * a + 1];
+      const double xb = m->points[2 * b], yb = m->points[2 * b + 1];
+      for (int side = 0; side < 2; ++side)
+        for (int k = 0; k < ng; ++k) {
+          const double xi = bp[k];
+          const double x = 0.5 * xa * (1 - xi) + 0.5 * xb * (1 + xi), y = 0.5 * ya * (1 - xi) + 0.5 * yb * (1 + xi);
+          o3_weights(h->neighbour[2 * f + side], x, y, &gw[(((size_t)f * 2 + side) * ng + k) * nmax]);
+        }
+    }
+    *gauss_out = gw;
+    if (gauss_n) *gauss_n = ng;
+  }
+  std::vector<double>().swap(Gall);
 
   // ---- 128-cell block halo remap (basicCUDAsolver.cpp:697-850)
   const int BD = AFAR_BLOCKDIM;
@@ -977,4 +1047,15 @@ extern "C" afar_status afar_precompute_fields_device(const afar_polyMesh* m, con
     return AFAR_ERR_ARGUMENT;
   }
   return precompute(m, cfg, Wc, Wb, device, h, sz, rbf64_out);
+}
+
+extern "C" afar_status afar_precompute_fields_gauss(const afar_polyMesh* m, const afar_caseConfig* cfg,
+                                                   const double* Wc, const double* Wb, int device,
+                                                   afar_fieldPointer* h, afar_fieldSizes* sz, double** rbf64_out,
+                                                   double** gaussWeights, int* pointsPerFace) {
+  if (!gaussWeights || !pointsPerFace) {
+    set_error("afar_precompute_fields_gauss: null output");
+    return AFAR_ERR_ARGUMENT;
+  }
+  return precompute(m, cfg, Wc, Wb, device, h, sz, rbf64_out, gaussWeights, pointsPerFace);
 }

@@ -237,6 +237,13 @@ struct afar_solver {
   void* fv = nullptr;
   void* flux = nullptr;
   void* snap = nullptr;       // device snapshot of W, U, U0, step control
+  // the optional multi-point face flux (afar_set_face_gauss_flux): points per face (0: off)
+  int ng = 0;
+  void* wg = nullptr;
+  void* sgk = nullptr;
+  void* fgk = nullptr;
+  void* fvg = nullptr;
+  double gw[4] = {0.0, 0.0, 0.0, 0.0};
   std::vector<double> rbf64;  // optional FP64 weights awaiting the stencil upload
   cudaGraphExec_t graph = nullptr;
   size_t bytes = 0;
@@ -310,6 +317,12 @@ StageArgs<P> make_args(afar_solver* s) {
   a.dtgf = s->dtgf;
   a.px = s->px;
   a.py = s->py;
+  a.ng = s->ng;
+  a.wg = static_cast<const S*>(s->wg);
+  a.sgk = static_cast<const V2<G>*>(s->sgk);
+  a.fgk = static_cast<const V2<G>*>(s->fgk);
+  a.fvg = static_cast<V4<G>*>(s->fvg);
+  for (int k = 0; k < 4; ++k) a.gw[k] = (G)s->gw[k];
   return a;
 }
 
@@ -355,6 +368,9 @@ struct Stage {
         k_reconstruct_tile<P, 4><<<gc(), kTile, recon_smem<P>(s), s->stream>>>(a);
     } else
       k_reconstruct_staged<P><<<gc(), kCellBlock, recon_smem<P>(s), s->stream>>>(a);
+    if constexpr (P::id != PolicyRef::id) {
+      if (s->ng > 0) k_reconstruct_gauss<P><<<gc(), kCellBlock, 0, s->stream>>>(a);
+    }
   }
   void bvd() const { k_bvd<P><<<gc(), kCellBlock, 0, s->stream>>>(a); }
   // The face flux.  The ref policy computes the CFL step as a kernel of its own before the first
@@ -365,6 +381,10 @@ struct Stage {
       if (dt_stage && s->Nf > 0)
         k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
       k_flux<P, false><<<gf, kFaceBlock, 0, s->stream>>>(a);
+    } else if (s->ng > 0) {  // the multi-point face flux; the Courant step as a kernel of its own
+      if (dt_stage && s->Nf > 0)
+        k_delta_t<P><<<grid_for(s->Nf, kFaceBlock), kFaceBlock, 0, s->stream>>>(a, 0.0, &s->ctl->dt_bits, s->ctl);
+      k_flux_gauss<P><<<gf, kFaceBlock, 0, s->stream>>>(a);
     } else {
       if (dt_stage)
         k_flux<P, true><<<gf, kFaceBlock, 0, s->stream>>>(a);
@@ -1413,7 +1433,11 @@ extern "C" afar_status afar_device_bytes(afar_solver* s, size_t* bytes) {
   return AFAR_OK;
 }
 
-extern "C" int afar_launches_per_step(afar_solver* s) { return s && s->policy == AFAR_POLICY_REF ? 14 : 13; }
+extern "C" int afar_launches_per_step(afar_solver* s) {
+  if (!s) return 13;  // the face-centre step of the fp64 and mixed policies
+  if (s->policy == AFAR_POLICY_REF) return 14;
+  return s->ng > 0 ? 17 : 13;  // the multi-point flux: a Gauss-point reconstruct per stage, the Courant kernel
+}
 
 extern "C" afar_status afar_freeFieldData(afar_solver* s) {
   if (!s) return AFAR_OK;
@@ -1744,6 +1768,9 @@ extern "C" afar_status afar_batch_add(afar_batch* b, afar_solver* s) {
   if (!s->have_stencil)
     return (set_error("afar_batch_add: upload the stencil (afar_setDeviceFieldDataStencil) first"), AFAR_ERR_STATE);
   if (s->batch) return (set_error("afar_batch_add: the solver already belongs to a batch"), AFAR_ERR_STATE);
+  if (s->ng > 0)
+    return (set_error("afar_batch_add: batches run the face-centre flux; the solver has the multi-point face flux"),
+            AFAR_ERR_ARGUMENT);
   AFAR_CUDA(cudaStreamSynchronize(s->stream));  // no pending work of the member on its own stream
   b->members.push_back(s);
   s->batch = b;
@@ -1846,5 +1873,83 @@ extern "C" afar_status afar_debug_wait_injection(int device, unsigned extraBytes
   AFAR_CUDA(cudaMemcpyToSymbol(g_tile_extra_tx, &extraBytes, sizeof(extraBytes)));
   AFAR_CUDA(cudaMemcpyToSymbol(g_tile_wait_limit, &lim, sizeof(lim)));
   AFAR_CUDA(cudaDeviceSynchronize());
+  return AFAR_OK;
+}
+
+extern "C" afar_status afar_set_face_gauss_flux(afar_solver* s, int nPoints, const double* points,
+                                                const double* pointWeights, const double* rbfGauss) {
+  afar_status st = check_ready(s);
+  if (st || (st = check_not_batched(s))) return st;
+  if (nPoints == 0) {
+    s->ng = 0;
+    destroy_graphs(s);
+    return AFAR_OK;
+  }
+  if (s->policy == AFAR_POLICY_REF)
+    return (set_error("afar_set_face_gauss_flux: the ref policy keeps the reference's face-centre flux"),
+            AFAR_ERR_ARGUMENT);
+  if (nPoints < 1 || nPoints > 4 || !points || !pointWeights || !rbfGauss)
+    return (set_error("afar_set_face_gauss_flux: 1 to 4 points per face and non-null arrays"), AFAR_ERR_ARGUMENT);
+  double wsum = 0.0;
+  for (int k = 0; k < nPoints; ++k) {
+    if (!(pointWeights[k] > 0.0)) return (set_error("afar_set_face_gauss_flux: non-positive point weight"), AFAR_ERR_ARGUMENT);
+    wsum += pointWeights[k];
+  }
+  const int Nf = s->Nf, ng = nPoints, nmax = s->maxS + 1;
+  const bool mixed = s->policy == AFAR_POLICY_MIXED;
+  const size_t wS = mixed ? sizeof(float) : sizeof(double), wG = mixed ? sizeof(float) : sizeof(double);
+  if ((st = dalloc(s, &s->wg, wS * (size_t)s->maxM * ng * nmax * s->ldc))) return st;
+  AFAR_CUDA(cudaMemsetAsync(s->wg, 0, wS * (size_t)s->maxM * ng * nmax * s->ldc, s->stream));
+  if ((st = dalloc(s, &s->sgk, 2 * wG * (size_t)s->maxM * ng * s->ldc))) return st;
+  AFAR_CUDA(cudaMemsetAsync(s->sgk, 0, 2 * wG * (size_t)s->maxM * ng * s->ldc, s->stream));
+  if ((st = dalloc(s, &s->fgk, 2 * wG * (size_t)Nf * ng))) return st;
+  if ((st = dalloc(s, &s->fvg, 4 * wG * 2 * (size_t)Nf * ng))) return st;
+  double *d_w = nullptr, *d_p = nullptr;
+  V4<double>* fxy = nullptr;
+  auto cleanup = [&]() {
+    if (d_w) cudaFree(d_w);
+    if (d_p) cudaFree(d_p);
+    if (fxy) cudaFree(fxy);
+  };
+  const size_t nw = (size_t)Nf * 2 * ng * nmax, np = (size_t)Nf * ng * 2;
+  if (cudaMalloc(&d_w, sizeof(double) * (nw ? nw : 1)) != cudaSuccess ||
+      cudaMalloc(&d_p, sizeof(double) * (np ? np : 1)) != cudaSuccess ||
+      cudaMalloc(&fxy, sizeof(V4<double>) * (size_t)(Nf + s->Nb + 1)) != cudaSuccess) {
+    cleanup();
+    set_error("afar_set_face_gauss_flux: out of device memory for the set-up");
+    return AFAR_ERR_CUDA;
+  }
+  cudaMemcpyAsync(d_w, rbfGauss, sizeof(double) * nw, cudaMemcpyHostToDevice, s->stream);
+  cudaMemcpyAsync(d_p, points, sizeof(double) * np, cudaMemcpyHostToDevice, s->stream);
+  V4<double>* fsr = nullptr;
+  if (cudaMalloc(&fsr, sizeof(V4<double>) * (size_t)(Nf + s->Nb + 1)) != cudaSuccess) {
+    cleanup();
+    set_error("afar_set_face_gauss_flux: out of device memory for the set-up");
+    return AFAR_ERR_CUDA;
+  }
+  const int gF = grid_for((long long)Nf + s->Nb, kFaceBlock);
+  k_split_faces<<<gF, kFaceBlock, 0, s->stream>>>(Nf + s->Nb, s->faceRaw, fxy, fsr);
+  s->ng = ng;
+  for (int k = 0; k < 4; ++k) s->gw[k] = k < ng ? pointWeights[k] / wsum : 0.0;
+  auto setup = [&](auto tag) {
+    using P = decltype(tag);
+    StageArgs<P> a = make_args<P>(s);
+    k_setup_gauss<P><<<grid_for(s->Nc, kCellBlock), kCellBlock, 0, s->stream>>>(a, d_w, d_p);
+    if (Nf > 0) k_setup_gauss_faces<P><<<grid_for((long long)Nf * ng, 256), 256, 0, s->stream>>>(a, d_p, fxy);
+  };
+  if (mixed)
+    setup(PolicyMixed{});
+  else
+    setup(PolicyFP64{});
+  const cudaError_t e = cudaGetLastError();
+  const cudaError_t e2 = cudaStreamSynchronize(s->stream);
+  cleanup();
+  cudaFree(fsr);
+  if (e != cudaSuccess || e2 != cudaSuccess) {
+    s->ng = 0;
+    set_error("afar_set_face_gauss_flux: set-up failed: %s", cudaGetErrorString(e != cudaSuccess ? e : e2));
+    return AFAR_ERR_CUDA;
+  }
+  destroy_graphs(s);  // the next run captures the step with the multi-point flux
   return AFAR_OK;
 }

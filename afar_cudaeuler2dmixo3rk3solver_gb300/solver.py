@@ -178,7 +178,7 @@ def _cache_key(mesh: FoamMesh, cfg: CaseConfig, Wc, Wb, want_rbf64) -> str:
 
 
 def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_rbf64=False, cache_dir=None,
-               device=None):
+               device=None, gauss_flux=False):
     """Mesh + initial fields -> the reference's host field bundle (native precompute).
 
     With ``device`` (a CUDA device index) the RBF stage -- P matrices, inverses, O3 weights -- runs on
@@ -187,7 +187,13 @@ def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_r
     With ``cache_dir`` the bundle is kept on disk under a hash of every input and read back on the
     next call with the same inputs, instead of recomputing the RBF pseudo-inverses and weights (the
     role of the reference's basisOwnList/basisNeiList files and its ``recalcBasis`` switch,
-    basicCUDAsolver.cpp:626-694)."""
+    basicCUDAsolver.cpp:626-694).
+
+    With ``gauss_flux`` the bundle also carries what the optional multi-point face flux needs
+    (``afar_precompute_fields_gauss``): ``faceGaussPoints`` (Nf, n, 2), ``faceGaussWeights`` (Nf, n)
+    and ``RBFbasisGauss64``, the O3 weights at every point, [face][side][point][maxS+1]."""
+    if gauss_flux and cache_dir is not None:
+        raise ValueError("precompute: gauss_flux bundles are not cached")
     if cache_dir is not None:
         path = os.path.join(cache_dir, f"afar_bundle_{_cache_key(mesh, cfg, W_cells, W_boundary, want_rbf64)}.npz")
         if os.path.exists(path):
@@ -208,7 +214,12 @@ def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_r
     sz = _ffi.FieldSizes()
     c = cfg.to_c()
     r64 = C.c_void_p()
-    if device is None:
+    gw, ng = C.c_void_p(), C.c_int()
+    if gauss_flux:
+        st = lib().afar_precompute_fields_gauss(C.byref(m), C.byref(c), ptr(Wc), ptr(Wb),
+                                                -1 if device is None else int(device), C.byref(fp), C.byref(sz),
+                                                C.byref(r64) if want_rbf64 else None, C.byref(gw), C.byref(ng))
+    elif device is None:
         st = lib().afar_precompute_fields(C.byref(m), C.byref(c), ptr(Wc), ptr(Wb), C.byref(fp), C.byref(sz),
                                           C.byref(r64) if want_rbf64 else None)
     else:
@@ -222,10 +233,20 @@ def precompute(mesh: FoamMesh, cfg: CaseConfig, W_cells, W_boundary=None, want_r
             n = hf.a["RBFbasis"].shape[0]
             buf = (C.c_double * n).from_address(r64.value) if n else None
             hf.a["RBFbasis64"] = np.frombuffer(buf, dtype=np.float64).copy() if n else np.zeros(0)
+        if gauss_flux:
+            nf, nmax = hf.nf, hf.sizes["maxStencilSize"] + 1
+            cnt = nf * 2 * ng.value * nmax
+            buf = (C.c_double * cnt).from_address(gw.value) if cnt else None
+            hf.a["RBFbasisGauss64"] = np.frombuffer(buf, dtype=np.float64).copy() if cnt else np.zeros(0)
+            pts, w = face_gauss_quadrature(mesh, cfg)
+            hf.a["faceGaussPoints"] = np.ascontiguousarray(pts[:nf])
+            hf.a["faceGaussWeights"] = np.ascontiguousarray(w[:nf])
     finally:
         lib().afar_free_host_fields(C.byref(fp))
         if want_rbf64 and r64.value:
             C.CDLL(None).free(r64)
+        if gw.value:
+            C.CDLL(None).free(gw)
     del keep
     return hf
 
@@ -263,7 +284,7 @@ def face_gauss_quadrature(mesh: FoamMesh, cfg: CaseConfig):
 class CudaSolver:
     """The reference's basicCUDAsolver on libafar (one mesh, one GPU)."""
 
-    def __init__(self, fields: HostFields, cfg: CaseConfig, policy="ref", device=0, period=None):
+    def __init__(self, fields: HostFields, cfg: CaseConfig, policy="ref", device=0, period=None, gauss_flux=False):
         self.cfg = cfg
         self.fields = fields
         self.policy = policy
@@ -284,6 +305,19 @@ class CudaSolver:
             s["maxStencilSize"], s["maxCompactStencilSize"], s["maxLocalBlockStencilSize"],
             s["maxCompactLocalBlockStencilSize"]))
         check(lib().afar_set_gas(self.h, cfg.R, cfg.Cv))
+        if gauss_flux:
+            self.set_face_gauss_flux(fields)
+
+    def set_face_gauss_flux(self, fields: HostFields | None = None):
+        """The multi-point face flux (afar_set_face_gauss_flux) from a bundle precomputed with
+        ``gauss_flux=True``; ``fields=None`` turns it off (the face-centre flux)."""
+        if fields is None:
+            check(lib().afar_set_face_gauss_flux(self.h, 0, None, None, None))
+            return
+        pts = np.ascontiguousarray(fields.a["faceGaussPoints"], dtype=np.float64)
+        w = np.ascontiguousarray(fields.a["faceGaussWeights"][0] if fields.nf else np.ones(pts.shape[1]))
+        rg = np.ascontiguousarray(fields.a["RBFbasisGauss64"], dtype=np.float64)
+        check(lib().afar_set_face_gauss_flux(self.h, pts.shape[1], ptr(pts), ptr(w), ptr(rg)))
 
     # -- reference-shaped calls (basicCUDAsolver.cpp:854-913)
     def set_delta_t(self) -> float:

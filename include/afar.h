@@ -198,6 +198,19 @@ afar_status afar_precompute_fields_device(const afar_polyMesh* mesh, const afar_
                                           afar_fieldPointer* host, afar_fieldSizes* sizes,
                                           double** RBFbasis64);
 
+/* afar_precompute_fields (device >= 0: afar_precompute_fields_device) plus the O3 weights at the
+ * face Gauss points, for the optional multi-point face flux (afar_set_face_gauss_flux; no
+ * counterpart in the reference, whose flux uses the face centre).  For every internal face, each
+ * side and each point of the fOrder bar rule (the points of afar_face_gauss_quadrature), the
+ * weights of that side's stencil (the cell itself first) formed like the face-centre weights
+ * (basicCUDAsolver.cpp:585-619: the multiquadric basis at the point times the cell's RBF inverse,
+ * corrected to sum to one; a troubled cell's select the cell).  *gaussWeights is malloc'd (free()
+ * it): [face][side][point][maxStencilSize+1] doubles; *pointsPerFace receives the rule's size. */
+afar_status afar_precompute_fields_gauss(const afar_polyMesh* mesh, const afar_caseConfig* cfg,
+                                         const double* W_cells, const double* W_boundary, int device,
+                                         afar_fieldPointer* host, afar_fieldSizes* sizes, double** RBFbasis64,
+                                         double** gaussWeights, int* pointsPerFace);
+
 /* The face Gauss points and weights of every face, internal then boundary in face order (the
  * d2GaussQuadrature faceGaussPoints/faceGaussWeights layout, d2GaussQuadrature.C:153-277 and the
  * getters of d2GaussQuadrature.H:75-83): the fOrder bar rule (1, 2, 3 or 4 points) on each edge from
@@ -485,6 +498,20 @@ afar_status afar_measure_fp64_peak(int device, double* gflops, float* ms);
  * replaces the limit (<= 0: the default).  afar_debug_wait_injection(device, 0, 0) restores normal
  * operation.  Affects every solver and batch on the device until then. */
 afar_status afar_debug_wait_injection(int device, unsigned extraBytes, long long limitClocks);
+
+/* The multi-point face flux (no counterpart in the reference, whose flux uses the face centre; off
+ * by default since it changes results).  After afar_setDeviceFieldDataStencil, policies fp64 and
+ * mixed: the flux of every internal face becomes the weighted sum of the fluxes at its nPoints (1-4)
+ * Gauss points -- at each point the O3 value there (weights rbfGauss) or the TVD state
+ * extrapolated there with the cell's limited gradient, as the cells' switches ask, then the same
+ * Roe/KFVS choice and dissipation as at the face centre.  The troubled-cell and BVD decisions
+ * stay those of the face-centre values; the Courant step is evaluated in FP64 by a kernel of its
+ * own.  points: [2*nPoints*facesNum] the points of each internal face (afar_face_gauss_quadrature);
+ * pointWeights: [nPoints] positive (normalised here to sum to one); rbfGauss:
+ * [facesNum][2][nPoints][maxStencilSize+1] (afar_precompute_fields_gauss).  nPoints = 0 restores
+ * the face-centre flux.  A solver with it cannot join a batch. */
+afar_status afar_set_face_gauss_flux(afar_solver* solver, int nPoints, const double* points,
+                                     const double* pointWeights, const double* rbfGauss);
 
 /* Number of kernel launches one afar_run step issues on this solver (for accounting). */
 int afar_launches_per_step(afar_solver* solver);

@@ -217,3 +217,117 @@ double oracle_delta_t(const oracle_mesh* m, const double* FD, double R, double C
 #undef RBF
 #undef MAT
 #undef PI_
+
+/* ---- the multi-point face flux (fp64 policy of the library; see afar_oracle.h) ------------------ */
+void oracle_reconstruct_gauss_fp64(const oracle_mesh* m, const double* FD, const double* grad, int ng,
+                                   const double* rbfg, const double* gpts, double* faceFDg) {
+  const int Nc = m->Nc, Nf = m->Nf, maxS = m->maxS, maxM = m->maxM;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < Nc; ++c) {
+    const int S = m->S[c], Mc = m->M[c];
+    const int* st = m->gsten + (size_t)maxS * c;
+    const double* W = FD + 4 * (size_t)c;
+    const double* g = grad + 8 * (size_t)c;
+    /* the gradient of each variable (x, y): p (0, 1), Ux (2, 4), Uy (3, 5), T (6, 7) */
+    const int gx[4] = {0, 2, 3, 6}, gy[4] = {1, 4, 5, 7};
+    double vmax[4], vmin[4];
+    for (int v = 0; v < 4; ++v) vmax[v] = vmin[v] = W[v];
+    for (int i = 0; i < Mc; ++i)
+      for (int v = 0; v < 4; ++v) {
+        const double q = FD[4 * (size_t)st[i] + v];
+        vmax[v] = fmax(q, vmax[v]);
+        vmin[v] = fmin(q, vmin[v]);
+      }
+    const int flatT = fabs(vmax[3] - vmin[3]) < 1e-10;
+    for (int fi = 0; fi < Mc; ++fi) {
+      int f = m->cellFaces[(size_t)maxM * c + fi];
+      const int isNei = f < 0;
+      f = abs(f) - 1;
+      if (f >= Nf) continue;
+      for (int k = 0; k < ng; ++k) {
+        const double dx = gpts[2 * ((size_t)f * ng + k)] - m->CELL[c].x;
+        const double dy = gpts[2 * ((size_t)f * ng + k) + 1] - m->CELL[c].y;
+        const double* w = rbfg + (((size_t)f * 2 + isNei) * ng + k) * (maxS + 1);
+        double o3[4];
+        for (int v = 0; v < 4; ++v) o3[v] = w[0] * W[v];
+        for (int ci = 0; ci < S; ++ci)
+          for (int v = 0; v < 4; ++v) o3[v] += w[ci + 1] * FD[4 * (size_t)st[ci] + v];
+        double* o = faceFDg + ((2 * (size_t)f + isNei) * ng + k) * 4;
+        for (int v = 0; v < 4; ++v) {
+          const double lin = W[v] + g[gx[v]] * dx + g[gy[v]] * dy;
+          o[v] = (!flatT && fabs(vmax[v] - vmin[v]) >= 1e-5) ? o3[v] : lin;
+        }
+      }
+    }
+  }
+}
+
+void oracle_flux_gauss_fp64(const oracle_mesh* m, const double* FD, const double* grad, const double* lim,
+                            const double* faceFDg, const int8_t* si, int ng, const double* gpts, const double* gw,
+                            double R, double Cv, double* Flux) {
+  const int Nf = m->Nf;
+  oracle_flux_fp64(m, FD, grad, lim, faceFDg, si, R, Cv, Flux); /* the boundary faces (internal ones rewritten) */
+#pragma omp parallel for schedule(static)
+  for (int f = 0; f < Nf; ++f) {
+    const int cell[2] = {m->neighbour[2 * f], m->neighbour[2 * f + 1]};
+    const int tvd[2] = {si[2 * (size_t)cell[0] + 1] != 0, si[2 * (size_t)cell[1] + 1] != 0};
+    const int shock = si[2 * (size_t)cell[0] + 1] < 0 || si[2 * (size_t)cell[1] + 1] < 0;
+    const double magSf = m->FACE[f].magSf, Sfx = m->FACE[f].Sfx, Sfy = m->FACE[f].Sfy;
+    const int gx[4] = {0, 2, 3, 6}, gy[4] = {1, 4, 5, 7};
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int k = 0; k < ng; ++k) {
+      double st[2][4], T[2][4], rho[2], rhoT[2];
+      for (int s = 0; s < 2; ++s) {
+        const int c = cell[s];
+        const double dx = gpts[2 * ((size_t)f * ng + k)] - m->CELL[c].x;
+        const double dy = gpts[2 * ((size_t)f * ng + k) + 1] - m->CELL[c].y;
+        const double* W = FD + 4 * (size_t)c;
+        const double* g = grad + 8 * (size_t)c;
+        const double* L = lim + 4 * (size_t)c;
+        const double* o3 = faceFDg + ((2 * (size_t)f + s) * ng + k) * 4;
+        for (int v = 0; v < 4; ++v) {
+          T[s][v] = W[v] + L[v] * (g[gx[v]] * dx + g[gy[v]] * dy);
+          st[s][v] = tvd[s] ? T[s][v] : o3[v];
+        }
+        rho[s] = st[s][0] / (R * st[s][3]);
+        rhoT[s] = T[s][0] / (R * T[s][3]);
+      }
+      const double dP = min_deltafp64(st[0][0], st[1][0], T[0][0], T[1][0]);
+      const double dRho = min_deltafp64(rho[0], rho[1], rhoT[0], rhoT[1]);
+      double F[4];
+      F[0] = 0.5 * rho[0] * (st[0][1] * Sfx + st[0][2] * Sfy) + 0.5 * rho[1] * (st[1][1] * Sfx + st[1][2] * Sfy);
+      F[1] = 0.5 * (F[0] * st[0][1] + st[0][0] * Sfx) + 0.5 * (F[0] * st[1][1] + st[1][0] * Sfx);
+      F[2] = 0.5 * (F[0] * st[0][2] + st[0][0] * Sfy) + 0.5 * (F[0] * st[1][2] + st[1][0] * Sfy);
+      F[3] = 0.5 * F[0] * (Cv * st[0][3] + 0.5 * (st[0][1] * st[0][1] + st[0][2] * st[0][2]) + st[0][0] / rho[0]) +
+             0.5 * F[0] * (Cv * st[1][3] + 0.5 * (st[1][1] * st[1][1] + st[1][2] * st[1][2]) + st[1][0] / rho[1]);
+      if (shock)
+        kfvsfp64(F, rho[0], rho[1], st[0][0], st[1][0], st[0][1], st[1][1], st[0][2], st[1][2], st[0][3], st[1][3], R,
+                 Cv, magSf, Sfx, Sfy);
+      else
+        roefp64(F, rho[0], rho[1], st[0][0], st[1][0], st[0][1], st[1][1], st[0][2], st[1][2], st[0][3], st[1][3], dP,
+                dRho, R, Cv, magSf, Sfx, Sfy);
+      for (int v = 0; v < 4; ++v) acc[v] += gw[k] * F[v];
+    }
+    for (int v = 0; v < 4; ++v) Flux[4 * (size_t)f + v] = acc[v];
+  }
+}
+
+void oracle_evolve_gauss_fp64(const oracle_mesh* m, double* FD, double* cFD, double* cFDold, int8_t* si,
+                              oracle_work* w, double R, double Cv, double dt, int ng, const double* rbfg,
+                              const double* gpts, const double* gw, double* faceFDg) {
+  const double gamma = R / Cv + 1.0;
+  const double b1[3] = {1.0, 0.75, 0.333333};
+  const double b2[3] = {0.0, 0.25, 0.666667};
+  const double b3[3] = {1.0, 0.25, 0.666667};
+  double* lim = (double*)w->lim;
+  for (int k = 0; k < 3; ++k) {
+    oracle_reconstruct_fp64(m, FD, w->grad, lim, w->faceFD, si);
+    oracle_reconstruct_gauss_fp64(m, FD, w->grad, ng, rbfg, gpts, faceFDg);
+    oracle_bvd_fp64(m, FD, w->grad, lim, w->faceFD, si);
+    oracle_flux_gauss_fp64(m, FD, w->grad, lim, faceFDg, si, ng, gpts, gw, R, Cv, w->Flux);
+    oracle_residual(m, w->Flux, w->Res);
+    oracle_update(m, FD, cFD, cFDold, w->Res, R, gamma, dt, b1[k], b2[k], b3[k]);
+    oracle_boundary(m, FD, R, Cv);
+  }
+  memcpy(cFDold, cFD, sizeof(double) * 4 * (size_t)m->Nc);
+}

@@ -91,6 +91,25 @@ void oracle_evolve_ref(const oracle_mesh* m, double* FD, double* cFD, double* cF
 void oracle_evolve_fp64(const oracle_mesh* m, double* FD, double* cFD, double* cFDold, int8_t* si, oracle_work* w,
                         double R, double Cv, double dt, int exactRK);
 
+/* The optional multi-point face flux of the library (fp64 policy; no counterpart in the reference,
+ * whose flux uses the face centre).  ng points per internal face: gpts [Nf][ng][2] their
+ * coordinates, gw [ng] their weights normalised to sum to one, rbfg [Nf][2][ng][maxS+1] the O3
+ * weights of each side's stencil at each point.  oracle_reconstruct_gauss_fp64 writes the face
+ * values at the points, faceFDg [2Nf][ng][4], with the selection rules of the face-centre values
+ * (O3 where a variable varies over the compact stencil, else its unlimited linear value; every
+ * variable linear in a cell of flat temperature); oracle_flux_gauss_fp64 sums the flux of every
+ * point times its weight, each with the switch of its cells (TVD states extrapolated to the point
+ * with the cell's limited gradient); boundary faces as oracle_flux_fp64. */
+void oracle_reconstruct_gauss_fp64(const oracle_mesh* m, const double* FD, const double* grad, int ng,
+                                   const double* rbfg, const double* gpts, double* faceFDg);
+void oracle_flux_gauss_fp64(const oracle_mesh* m, const double* FD, const double* grad, const double* lim,
+                            const double* faceFDg, const int8_t* si, int ng, const double* gpts, const double* gw,
+                            double R, double Cv, double* Flux);
+/* oracle_evolve_fp64 with the multi-point face flux; faceFDg: scratch of 8*ng*Nf doubles. */
+void oracle_evolve_gauss_fp64(const oracle_mesh* m, double* FD, double* cFD, double* cFDold, int8_t* si,
+                              oracle_work* w, double R, double Cv, double dt, int ng, const double* rbfg,
+                              const double* gpts, const double* gw, double* faceFDg);
+
 int oracle_max_threads(void);
 void oracle_set_threads(int n);
 

@@ -45,6 +45,11 @@ def lib():
             getattr(L, f"oracle_evolve_{pol}").argtypes = [C.POINTER(OracleMesh), _p, _p, _p, _p,
                                                            C.POINTER(OracleWork), C.c_double, C.c_double, C.c_double,
                                                            C.c_int]
+        L.oracle_reconstruct_gauss_fp64.argtypes = [C.POINTER(OracleMesh), _p, _p, C.c_int, _p, _p, _p]
+        L.oracle_flux_gauss_fp64.argtypes = [C.POINTER(OracleMesh), _p, _p, _p, _p, _p, C.c_int, _p, _p, C.c_double,
+                                             C.c_double, _p]
+        L.oracle_evolve_gauss_fp64.argtypes = [C.POINTER(OracleMesh), _p, _p, _p, _p, C.POINTER(OracleWork),
+                                               C.c_double, C.c_double, C.c_double, C.c_int, _p, _p, _p, _p]
         L.oracle_residual.argtypes = [C.POINTER(OracleMesh), _p, _p]
         L.oracle_update.argtypes = [C.POINTER(OracleMesh), _p, _p, _p, _p] + [C.c_double] * 6
         L.oracle_boundary.argtypes = [C.POINTER(OracleMesh), _p, C.c_double, C.c_double]
@@ -65,8 +70,19 @@ class Oracle:
 
     BETA = ((1.0, 0.0, 1.0), (0.75, 0.25, 0.25), (0.333333, 0.666667, 0.666667))
 
-    def __init__(self, hf, R, Cv, policy="ref", matrix32=None):
+    def __init__(self, hf, R, Cv, policy="ref", matrix32=None, gauss_flux=False):
+        """gauss_flux: the library's optional multi-point face flux (fp64 policy only), with the
+        bundle's faceGaussPoints / faceGaussWeights / RBFbasisGauss64."""
         s = hf.sizes
+        self.gauss = None
+        if gauss_flux:
+            if policy != "fp64":
+                raise ValueError("the multi-point face flux oracle is FP64")
+            pts = np.ascontiguousarray(hf.a["faceGaussPoints"], dtype=np.float64)
+            w = np.asarray(hf.a["faceGaussWeights"][0], dtype=np.float64) if hf.a["faceGaussWeights"].size else \
+                np.ones(pts.shape[1])
+            self.gauss = (pts.shape[1], np.ascontiguousarray(hf.a["RBFbasisGauss64"]), pts,
+                          np.ascontiguousarray(w / w.sum()))
         self.hf = hf
         self.R, self.Cv = float(R), float(Cv)
         self.policy = policy
@@ -124,9 +140,18 @@ class Oracle:
         FD, cFD, cFDold, si = st["FD"], st["cFD"], st["cFDold"], st["si"]
         getattr(L, f"oracle_reconstruct_{pol}")(C.byref(self.m), _ptr(FD), _ptr(grad), _ptr(lim), _ptr(fv), _ptr(si))
         raw_lim = lim.copy()
+        if self.gauss:
+            ng, rbfg, gpts, gw = self.gauss
+            fvg = np.zeros((2 * self.Nf, ng, 4))
+            L.oracle_reconstruct_gauss_fp64(C.byref(self.m), _ptr(FD), _ptr(grad), ng, _ptr(rbfg), _ptr(gpts),
+                                            _ptr(fvg))
         getattr(L, f"oracle_bvd_{pol}")(C.byref(self.m), _ptr(FD), _ptr(grad), _ptr(lim), _ptr(fv), _ptr(si))
-        getattr(L, f"oracle_flux_{pol}")(C.byref(self.m), _ptr(FD), _ptr(grad), _ptr(lim), _ptr(fv), _ptr(si),
-                                         self.R, self.Cv, _ptr(flux))
+        if self.gauss:
+            L.oracle_flux_gauss_fp64(C.byref(self.m), _ptr(FD), _ptr(grad), _ptr(lim), _ptr(fvg), _ptr(si), ng,
+                                     _ptr(gpts), _ptr(gw), self.R, self.Cv, _ptr(flux))
+        else:
+            getattr(L, f"oracle_flux_{pol}")(C.byref(self.m), _ptr(FD), _ptr(grad), _ptr(lim), _ptr(fv), _ptr(si),
+                                             self.R, self.Cv, _ptr(flux))
         L.oracle_residual(C.byref(self.m), _ptr(flux), _ptr(res))
         res_out = res.copy()
         b1, b2, b3 = self.BETA[k]
@@ -146,6 +171,13 @@ class Oracle:
         bufs = [np.zeros((self.Nc, 8)), np.zeros((self.Nc, 4), dtype=self.lim_dtype()), np.zeros((2 * self.Nf, 4)),
                 np.zeros((self.Nf + self.Nb, 4)), np.zeros((self.Nc, 4))]
         work.grad, work.lim, work.faceFD, work.Flux, work.Res = [_ptr(b) for b in bufs]
+        if self.gauss:
+            ng, rbfg, gpts, gw = self.gauss
+            fvg = np.zeros((2 * self.Nf, ng, 4))
+            lib().oracle_evolve_gauss_fp64(C.byref(self.m), _ptr(st["FD"]), _ptr(st["cFD"]), _ptr(st["cFDold"]),
+                                           _ptr(st["si"]), C.byref(work), self.R, self.Cv, dt, ng, _ptr(rbfg),
+                                           _ptr(gpts), _ptr(gw), _ptr(fvg))
+            return
         getattr(lib(), f"oracle_evolve_{self.policy}")(C.byref(self.m), _ptr(st["FD"]), _ptr(st["cFD"]),
                                                       _ptr(st["cFDold"]), _ptr(st["si"]), C.byref(work), self.R,
                                                       self.Cv, dt, int(exact_rk))
