@@ -94,8 +94,6 @@ struct StageArgs {
   int8_t* si;                 // 2(Nc+Nb): [2c] troubled-cell flag, [2c+1] final switch type
   V4<G>* fv;                  // 2Nf
   V4<typename P::F>* flux;    // Nf+Nb
-  float* fvT;                 // 2Nf (mixed) the T component of fv, for the BVD
-  V2<float>* gT;              // Nc (mixed) the T gradient, for the BVD
   StepCtl* ctl;
   V4<double>* res_dbg;        // optional residual dump (parity hook)
   double R, Cv, invR, gamma;
@@ -261,7 +259,6 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
   }
   a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
   a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
-  if constexpr (P::id == PolicyMixed::id) a.gT[c] = V2<float>{gTx, gTy};  // for the BVD
 
   const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
   V4<S> L;
@@ -281,7 +278,6 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
       o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
       o.w = (G)(tc) + gTx * dx + gTy * dy;
       a.fv[2 * f + isNei] = o;
-      if constexpr (P::id == PolicyMixed::id) a.fvT[2 * f + isNei] = o.w;
     }
     flag0 = 0;
   } else {  // reference :235-314
@@ -313,7 +309,6 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
       o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
       notTrouble = phif > S(0);
       a.fv[2 * f + isNei] = o;
-      if constexpr (P::id == PolicyMixed::id) a.fvT[2 * f + isNei] = o.w;
     }
     L.x = fmx(lp, S(0)) * notTrouble;
     L.y = fmx(lux, S(0)) * notTrouble;
@@ -550,7 +545,6 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   }
   a.grad[2 * c] = V4<G>{gPx, gPy, gUxx, gUxy};
   a.grad[2 * c + 1] = V4<G>{gUyx, gUyy, gTx, gTy};
-  if constexpr (P::id == PolicyMixed::id) a.gT[c] = V2<float>{gTx, gTy};  // for the BVD
 
   const S SMALL = AFAR_LIT(S, 1e-5), VSMALL = AFAR_LIT(S, 1e-10);
   V4<S> Lm;
@@ -570,7 +564,6 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
       o.z = (G)(uyc) + gUxy * dx + gUyy * dy;
       o.w = (G)(tc) + gTx * dx + gTy * dy;
       a.fv[2 * f + isNei] = o;
-      if constexpr (P::id == PolicyMixed::id) a.fvT[2 * f + isNei] = o.w;
     }
     flag0 = 0;
   } else {  // reference :235-314
@@ -602,7 +595,6 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
       o.w = pick<P>(fab(tMax - tMin) >= SMALL, fab(tMax - tMin) < SMALL, tf, phif);
       notTrouble = phif > S(0);
       a.fv[2 * f + isNei] = o;
-      if constexpr (P::id == PolicyMixed::id) a.fvT[2 * f + isNei] = o.w;
     }
     Lm.x = fmx(lp, S(0)) * notTrouble;
     Lm.y = fmx(lux, S(0)) * notTrouble;
@@ -853,16 +845,8 @@ __device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
   }
 
   const S tc = (S)a.W[c].w;
-  G gTx, gTy;
-  if constexpr (P::id == PolicyMixed::id) {  // the compact copies the reconstruct wrote (8 bytes, not 16)
-    const V2<float> g = a.gT[c];
-    gTx = g.x;
-    gTy = g.y;
-  } else {
-    const V4<G> g1 = a.grad[2 * c + 1];
-    gTx = g1.z;
-    gTy = g1.w;
-  }
+  const V4<G> g1 = a.grad[2 * c + 1];
+  const G gTx = g1.z, gTy = g1.w;
   V4<S> L = a.lim[c];
   int bvdType = 0, bfaces = 0;
   for (int fi = 0; fi < nM; ++fi) {
@@ -878,15 +862,8 @@ __device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
       continue;
     }
     const V2<G> d = a.sg[fi * ldc + c];
-    G tfOwn, tfNei;
-    if constexpr (P::id == PolicyMixed::id) {  // both sides' T from one 8-byte pair instead of two 16-byte values
-      const float2 t2 = reinterpret_cast<const float2*>(a.fvT)[f];
-      tfOwn = t2.x;
-      tfNei = t2.y;
-    } else {
-      tfOwn = a.fv[2 * f].w;
-      tfNei = a.fv[2 * f + 1].w;
-    }
+    const G tfOwn = a.fv[2 * f].w;
+    const G tfNei = a.fv[2 * f + 1].w;
     const G tfCur = pick<P>(isNei, !isNei, tfNei, tfOwn);
     const G tfOther = pick<P>(!isNei, isNei, tfNei, tfOwn);
     const G lim = to_bj(L.w);

@@ -236,8 +236,6 @@ struct afar_solver {
   void* lim = nullptr;
   void* fv = nullptr;
   void* flux = nullptr;
-  float* fvT = nullptr;       // mixed: T of the face values, for the BVD
-  V2<float>* gT = nullptr;    // mixed: T gradient, for the BVD
   void* snap = nullptr;       // device snapshot of W, U, U0, step control
   // the optional multi-point face flux (afar_set_face_gauss_flux): points per face (0: off)
   int ng = 0;
@@ -303,8 +301,6 @@ StageArgs<P> make_args(afar_solver* s) {
   a.si = s->si;
   a.fv = static_cast<V4<G>*>(s->fv);
   a.flux = static_cast<V4<typename P::F>*>(s->flux);
-  a.fvT = s->fvT;
-  a.gT = s->gT;
   a.vinv = s->vinv;
   a.ctl = s->ctl;
   a.res_dbg = nullptr;
@@ -807,11 +803,6 @@ extern "C" afar_status afar_setDeviceFieldData(afar_solver* s, const afar_fieldP
   if ((st = dalloc_t(s, &s->dtg, Nf))) return st;
   if ((st = dalloc_t(s, &s->bn, Nb))) return st;
   AFAR_CUDA(cudaMemsetAsync(s->fv, 0, g * 2 * Nf, s->stream));
-  if (s->policy == AFAR_POLICY_MIXED) {  // compact T copies for the BVD
-    if ((st = dalloc_t(s, &s->fvT, 2 * (size_t)Nf))) return st;
-    if ((st = dalloc_t(s, &s->gT, (size_t)Nc))) return st;
-    AFAR_CUDA(cudaMemsetAsync(s->fvT, 0, sizeof(float) * 2 * Nf, s->stream));
-  }
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
   AFAR_CUDA(cudaGetLastError());
   s->have_fields = true;
