@@ -374,7 +374,7 @@ afar_status afar_batch_destroy(afar_batch* batch);
 /* The batch's launch schedule, picked by the batch autotuner (no counterpart in the reference,
  * whose kernels run in blocks of BLOCKDIM = 128, basicDataStructure.h:6) when the batch is built
  * (its first run after members join or leave): each mixed-policy member reconstructs with the
- * kernel its own solver's autotuner chose for its mesh class (tile-staged or register pass; so a
+ * tile-staged kernel, or with the register pass where its solver forces it (afar_set_tuning; so a
  * member's result never depends on its batch-mates), and the BVD and flux kernels run in the block
  * size that timed fastest on the whole batch (BVD 64, 128 or 256 cells, flux 128 or 256 faces;
  * best of three launches each), cached per device, policy and batch shape (cells and members, each

@@ -242,9 +242,9 @@ def test_batch_schedule_block_sizes_do_not_change_results(cases, policy):
 
 
 def test_batch_member_keeps_its_own_reconstruct_choice(cases):
-    """A mixed-policy member reconstructs with the kernel its own solver chose (here forced to the
-    register pass): the schedule counts it, and its result is bitwise the same in a batch with
-    other members as in a batch of its own."""
+    """A mixed-policy member whose solver forces the register-pass reconstruct keeps it in a batch
+    (the others run the tile-staged one): the schedule counts it, and its result is bitwise the same
+    in a batch with other members as in a batch of its own."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch
 
     def run(with_others):
@@ -252,7 +252,7 @@ def test_batch_member_keeps_its_own_reconstruct_choice(cases):
         s.set_tuning(1)
         others = [_make(cases, n, "mixed") for n in (["quad_riemann", "mixed_riemann"] if with_others else [])]
         for o in others:
-            o.set_tuning(0)
+            o.set_tuning(-1)  # autotuned solo; in the batch the tile-staged kernel
         b = Batch("mixed")
         for x in [s] + others:
             x.set_step_params()
