@@ -94,7 +94,8 @@ def parse():
     ap.add_argument("--acc-sample", type=int, default=8, help="--accuracy batch: solves of the batch re-run")
     ap.add_argument("--floor", action="store_true",
                     help="--accuracy: also the FP64 policy against itself, on the same mesh in another cell order "
-                         "(Hilbert curve instead of RCM: another summation order) and from a 1-ulp perturbed start")
+                         "(Hilbert curve instead of RCM: another summation order), from a 1-ulp perturbed start, and "
+                         "from the start rounded to float")
     ap.add_argument("--cache-mesh", default="", help=argparse.SUPPRESS)  # helper: build the workload, save it
     ap.add_argument("--cpu-sample", default="", help=argparse.SUPPRESS)  # helper: time the oracle on a saved mesh
     ap.add_argument("--cpu-policy", default="ref", help=argparse.SUPPRESS)
@@ -835,11 +836,14 @@ def accuracy_pair(hf, cfg, device, t_end=0.0, n_steps=0, every=10, init=None):
     return out, a, b
 
 
-def fp64_perturbation_floor(hf, cfg, device, n_steps=0, t_end=0.0, every=10, init=None, seed=1):
-    """The FP64 policy against itself from a start perturbed by one unit in the last place (each
-    stored double moved up or down one ulp at random), with the same step sizes: how far rounding
+def fp64_perturbation_floor(hf, cfg, device, n_steps=0, t_end=0.0, every=10, init=None, seed=1, kind="ulp"):
+    """The FP64 policy against itself from a perturbed start, with the same step sizes.  kind "ulp":
+    each stored double moved up or down one unit in the last place at random -- how far rounding
     alone carries two FP64 solves apart on this configuration (the floor under any mixed-precision
-    form's difference from FP64)."""
+    form's difference from FP64).  kind "float": every stored value rounded to the nearest float --
+    a one-time perturbation of the size FP32 storage makes (2^-24 relative), showing how much of a
+    mixed-precision form's difference the configuration's sensitivity to a perturbation of that
+    size explains, however precisely its switches are then evaluated."""
     from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver
 
     a = CudaSolver(hf, cfg, policy="fp64", device=device)
@@ -849,6 +853,8 @@ def fp64_perturbation_floor(hf, cfg, device, n_steps=0, t_end=0.0, every=10, ini
 
     def ulp_nudge(x):
         x = np.ascontiguousarray(x, dtype=np.float64)
+        if kind == "float":
+            return x.astype(np.float32).astype(np.float64)
         return np.where(rng.integers(0, 2, x.shape) == 1, np.nextafter(x, np.inf), np.nextafter(x, -np.inf))
 
     a.upload_state(FD=FD0, cFD=U0, cFDold=U0)
@@ -869,7 +875,9 @@ def fp64_perturbation_floor(hf, cfg, device, n_steps=0, t_end=0.0, every=10, ini
             worst = max(worst, compare_policies(hf, a.state(), b.state())["L1_rho"])
     out = compare_policies(hf, a.state(), b.state())
     out.update({"steps": k, "max_L1_rho_over_run": max(worst, out["L1_rho"]),
-                "what": "FP64 policy vs itself from a start perturbed by 1 ulp per stored value, same step sizes"})
+                "what": ("FP64 policy vs itself from a start perturbed by 1 ulp per stored value, same step sizes"
+                         if kind == "ulp" else
+                         "FP64 policy vs itself from the start rounded to float (2^-24 relative), same step sizes")})
     a.close()
     b.close()
     return out
@@ -1004,6 +1012,7 @@ def run_accuracy(args, dist: Dist):
                         lambda o, p_=params[k]: batch_member_mesh(p_, renumber=o),
                         lambda m_, p_=params[k]: (*batch_member_fields(m_, p_), None), cfg, dev, **brun)
                     rk["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, dev, **brun)
+                    rk["fp64_float_start"] = fp64_perturbation_floor(hf, cfg, dev, kind="float", **brun)
                 members.append(rk)
             r = {"members": members, "L1_rho_max": max(x["L1_rho"] for x in members),
                  "Linf_rho_max": max(x["Linf_rho"] for x in members),
@@ -1016,6 +1025,7 @@ def run_accuracy(args, dist: Dist):
             if args.floor:
                 r["fp64_floor_reorder"] = fp64_reorder_floor(make_mesh, fields, cfg, dev, **run)
                 r["fp64_floor_perturbed_start"] = fp64_perturbation_floor(hf, cfg, dev, init=init, **run)
+                r["fp64_float_start"] = fp64_perturbation_floor(hf, cfg, dev, init=init, kind="float", **run)
         line.update(r)
         line["wall_s"] = round(time.time() - t0, 1)
         if dist.rank == 0:
