@@ -85,6 +85,7 @@ struct StageArgs {
   const V2<G>* sg;            // [maxM][ldc]
   const V2<S>* sr;            // [maxM][ldc]
   const S* wts;               // [maxM*(maxS+1)][ldc]
+  const struct TileMaps* tmaps;  // mixed: TMA tensor maps of the operator rows (tile-staged reconstruct)
   // state and stage intermediates
   V4<typename P::W>* W;       // Nc+Nb
   V4<double>* U;              // Nc conserved state (mixed: DF4 float pairs, same 32 bytes)
@@ -334,6 +335,33 @@ constexpr int kTile = 128;
 // operation.
 static __device__ long long g_tile_wait_limit = 1ll << 31;
 static __device__ unsigned g_tile_extra_tx = 0;
+// Tensor maps of the mixed policy's slot-major operator rows, one tiled TMA load per array and
+// tile: face ids [maxM][ldc] and the LS / face-geometry rows (float pairs, as 2 ldc floats), boxes
+// of 128 cells x maxM rows; stencil ids, a box of 128 cells x S rows for each stencil size S; O3
+// weights [maxM][maxS+1][ldc], a box of 128 cells x rows 1..S x maxM slots for each S (row 0, the
+// cell's own weight, drops out of the difference-form sums).  A tile loads the boxes of its own
+// largest stencil, so no row past it is fetched.
+struct TileMaps {
+  CUtensorMap cf, lsm, sg, sr;
+  CUtensorMap sten[AFAR_MAX_VALID_STENCIL_SIZE];
+  CUtensorMap wts[AFAR_MAX_VALID_STENCIL_SIZE];
+};
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+          "r"(smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];\n" ::"r"(smem_addr(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+
 struct ReconTile {
   unsigned off_cf, off_lsm, off_sg, off_sr, off_sten, off_wts, off_w, off_bar, bytes;
 };
@@ -359,72 +387,36 @@ __host__ __device__ inline ReconTile recon_tile_layout(const int maxM, const int
   return L;
 }
 
-// Issues the bulk copies of tile `blk` (called by warp 0).  Rows of the slot-major arrays hold
-// ldc elements (a multiple of 32), so every slice is a multiple of 128 bytes and 16-byte aligned;
-// the own-state slice holds the tile's cells (16 bytes each).  Only the stencil and weight rows up
-// to the tile's own largest stencil are fetched: the rows past it hold zeros for every cell of the
-// tile and are never read.  Two barriers: bar[0] covers what the stencil gathers need (face ids,
-// stencil ids, own states, 12 of the ~47 KB), bar[1] the LS rows, face geometry and O3 weights, so
-// the first gathers are in flight while the weights still stream in.
+// Issues the loads of tile `blk` (lanes 0-6 of warp 0): six tiled TMA loads of its operator rows
+// (TileMaps) and one bulk copy of its own states.  The x coordinate of every box is the tile's
+// first cell (a multiple of 128 elements: 512 or 1024 bytes, so 16-byte aligned); boxes reaching
+// past the row ends of the last tile read zeros and count their full size.  Two barriers: bar[0]
+// covers what the stencil gathers need (face ids, stencil ids, own states), bar[1] the LS rows,
+// face geometry and O3 weights, so the first gathers are in flight while the weights still stream
+// in.  Smem rows hold 128 cells: face ids [maxM][128], stencil ids [S][128], LS and geometry
+// [maxM][128] pairs, weights [maxM][S][128] (S = the tile's largest stencil).
 template <class P>
 __device__ __forceinline__ void recon_tile_fetch(const StageArgs<P>& a, const int blk, const ReconTile& L,
                                                  unsigned char* sm, unsigned long long* bar) {
   const int lane = threadIdx.x;
   const int c0 = blk * kTile;
-  const unsigned ne = (unsigned)min(kTile, a.ldc - c0);  // elements of a row slice
-  const unsigned nw = (unsigned)min(kTile, a.Nc - c0);   // cells of the tile
   const int M = a.maxM, S = a.tileS[blk];
-  const int rows = 4 * M + S + M * S + 1;  // weight rows 1..S of each face slot (row 0, the cell's own
-                                           // weight, drops out of the difference-form sums)
+  const TileMaps* tm = a.tmaps;
   if (lane == 0) {
-    mbar_arrive_expect_tx(bar, ne * (M * 4 + S * 4) + nw * 16 + g_tile_extra_tx);
-    mbar_arrive_expect_tx(bar + 1, ne * (M * (8 + 8 + 8) + M * S * 4));
+    const unsigned nw = (unsigned)min(kTile, a.Nc - c0);  // cells of the tile
+    mbar_arrive_expect_tx(bar, kTile * 4 * (M + S) + nw * 16 + g_tile_extra_tx);
+    mbar_arrive_expect_tx(bar + 1, kTile * 8 * 3 * M + kTile * 4 * S * M);
   }
   __syncwarp();
-  for (int r = lane; r < rows; r += 32) {
-    void* dst;
-    const void* src;
-    unsigned bytes;
-    unsigned long long* b = bar + 1;
-    if (r < M) {
-      dst = sm + L.off_cf + r * kTile * 4;
-      src = a.cf + (size_t)r * a.ldc + c0;
-      bytes = ne * 4;
-      b = bar;
-    } else if (r < 2 * M) {
-      const int k = r - M;
-      dst = sm + L.off_lsm + k * kTile * 8;
-      src = a.lsm + (size_t)k * a.ldc + c0;
-      bytes = ne * 8;
-    } else if (r < 3 * M) {
-      const int k = r - 2 * M;
-      dst = sm + L.off_sg + k * kTile * 8;
-      src = a.sg + (size_t)k * a.ldc + c0;
-      bytes = ne * 8;
-    } else if (r < 4 * M) {
-      const int k = r - 3 * M;
-      dst = sm + L.off_sr + k * kTile * 8;
-      src = a.sr + (size_t)k * a.ldc + c0;
-      bytes = ne * 8;
-    } else if (r < 4 * M + S) {
-      const int k = r - 4 * M;
-      dst = sm + L.off_sten + k * kTile * 4;
-      src = a.sten + (size_t)k * a.ldc + c0;
-      bytes = ne * 4;
-      b = bar;
-    } else if (r < rows - 1) {
-      const int q = r - 4 * M - S, fi = q / S;
-      const int k = fi * (a.maxS + 1) + 1 + (q - fi * S);  // row j = 1 + q - fi S of face slot fi
-      dst = sm + L.off_wts + k * kTile * 4;
-      src = a.wts + (size_t)k * a.ldc + c0;
-      bytes = ne * 4;
-    } else {
-      dst = sm + L.off_w;
-      src = a.W + c0;
-      bytes = nw * 16;
-      b = bar;
-    }
-    bulk_to_smem(dst, src, bytes, b);
+  switch (lane) {
+    case 0: tma_load_2d(sm + L.off_cf, &tm->cf, c0, 0, bar); break;
+    case 1: tma_load_2d(sm + L.off_sten, &tm->sten[S - 1], c0, 0, bar); break;
+    case 2: bulk_to_smem(sm + L.off_w, a.W + c0, (unsigned)min(kTile, a.Nc - c0) * 16u, bar); break;
+    case 3: tma_load_2d(sm + L.off_lsm, &tm->lsm, 2 * c0, 0, bar + 1); break;
+    case 4: tma_load_2d(sm + L.off_sg, &tm->sg, 2 * c0, 0, bar + 1); break;
+    case 5: tma_load_2d(sm + L.off_sr, &tm->sr, 2 * c0, 0, bar + 1); break;
+    case 6: tma_load_3d(sm + L.off_wts, &tm->wts[S - 1], c0, 1, 0, bar + 1); break;
+    default: break;
   }
 }
 
@@ -469,7 +461,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
   const int* s_sten = reinterpret_cast<const int*>(sm + L.off_sten);
   const S* s_wts = reinterpret_cast<const S*>(sm + L.off_wts);
   const V4<WT>* s_w = reinterpret_cast<const V4<WT>*>(sm + L.off_w);
-  const int wrow = a.maxS + 1;
+  const int wrow = a.tileS[blk];  // weight rows of a face slot in shared memory (members 1..S)
 
   int fid[NF];
   bool inner[NF];
@@ -534,7 +526,7 @@ __device__ __forceinline__ void recon_tile_body(const StageArgs<P>& a, const int
         }
 #pragma unroll
         for (int fi = 0; fi < NF; ++fi) {
-          const S wv = fi < nfm ? s_wts[(fi * wrow + ci + 1) * kTile + t] : S(0);
+          const S wv = fi < nfm ? s_wts[(fi * wrow + ci) * kTile + t] : S(0);
           acc[fi][0] += wv * dp;
           acc[fi][1] += wv * dux;
           acc[fi][2] += wv * duy;

@@ -16,6 +16,7 @@
 // FMA-contraction decisions; that is what makes the 1e-12 / identical-switch parity possible.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the type only: the library does not link the driver API)
 #include <cuda_runtime.h>
 #include <stdint.h>
 

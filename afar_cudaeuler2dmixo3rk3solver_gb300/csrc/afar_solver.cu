@@ -14,6 +14,7 @@
 #include <tuple>
 #include <vector>
 
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 #include <nvtx3/nvToolsExt.h>
 
 #include "afar_internal.h"
@@ -213,6 +214,7 @@ struct afar_solver {
   uint8_t* nS = nullptr;
   uint8_t* nM = nullptr;
   uint8_t* tileS = nullptr;  // per 128-cell tile: its largest stencil size
+  TileMaps* tmaps = nullptr;  // mixed: tensor maps of the operator rows (device memory)
   int* sten = nullptr;
   int* cf = nullptr;
   V4<double>* U = nullptr;
@@ -293,6 +295,7 @@ StageArgs<P> make_args(afar_solver* s) {
   a.sg = static_cast<const V2<G>*>(s->sg);
   a.sr = static_cast<const V2<S>*>(s->sr);
   a.wts = static_cast<const S*>(s->wts);
+  a.tmaps = s->tmaps;
   a.W = static_cast<V4<typename P::W>*>(s->W);
   a.U = s->U;
   a.U0 = s->U0;
@@ -681,6 +684,68 @@ static afar_status get_state(afar_solver* s, afar_basicFieldData* FD, afar_conse
 // launches, CUDA events on its stream; the launches only write the stage's intermediates) and the
 // faster kept.  Decisions are cached per device and mesh class (faces per cell, stencil size, cell
 // count to a factor of two), so later solvers of the same class skip the timing.
+// cuTensorMapEncodeTiled, looked up once through the runtime (the library links no driver API).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// The tensor maps of the mixed tile-staged reconstruct (TileMaps): built on the host after the
+// operator rows are in place and copied to the solver's device memory.  Each map describes one
+// slot-major array as rows of ldc elements (ldc a multiple of 32, so every row stride is a multiple
+// of 128 bytes), with boxes of 128 cells.
+static afar_status build_tile_maps(afar_solver* s) {
+  const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return (set_error("cuTensorMapEncodeTiled is not available from the driver"), AFAR_ERR_CUDA);
+  TileMaps h;
+  std::memset(&h, 0, sizeof(h));
+  const cuuint64_t ldc = (cuuint64_t)s->ldc, M = (cuuint64_t)s->maxM, S = (cuuint64_t)s->maxS;
+  const cuuint32_t one[3] = {1, 1, 1};
+  auto encode = [&](CUtensorMap* m, CUtensorMapDataType dt, cuuint32_t rank, void* base, const cuuint64_t* dims,
+                    const cuuint64_t* strides, const cuuint32_t* box) -> afar_status {
+    const CUresult r = enc(m, dt, rank, base, dims, strides, box, one, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return (set_error("cuTensorMapEncodeTiled failed (%d)", (int)r), AFAR_ERR_CUDA);
+    return AFAR_OK;
+  };
+  afar_status st;
+  {
+    const cuuint64_t dims[2] = {ldc, M}, strides[1] = {ldc * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kTile, (cuuint32_t)M};
+    if ((st = encode(&h.cf, CU_TENSOR_MAP_DATA_TYPE_INT32, 2, s->cf, dims, strides, box))) return st;
+  }
+  {
+    const cuuint64_t dims[2] = {2 * ldc, M}, strides[1] = {ldc * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)(2 * kTile), (cuuint32_t)M};
+    if ((st = encode(&h.lsm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->lsm, dims, strides, box))) return st;
+    if ((st = encode(&h.sg, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->sg, dims, strides, box))) return st;
+    if ((st = encode(&h.sr, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, s->sr, dims, strides, box))) return st;
+  }
+  for (cuuint32_t k = 1; k <= (cuuint32_t)S; ++k) {
+    const cuuint64_t dims[2] = {ldc, S}, strides[1] = {ldc * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kTile, k};
+    if ((st = encode(&h.sten[k - 1], CU_TENSOR_MAP_DATA_TYPE_INT32, 2, s->sten, dims, strides, box))) return st;
+    const cuuint64_t wdims[3] = {ldc, S + 1, M}, wstrides[2] = {ldc * 4, ldc * 4 * (S + 1)};
+    const cuuint32_t wbox[3] = {(cuuint32_t)kTile, k, (cuuint32_t)M};
+    if ((st = encode(&h.wts[k - 1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, s->wts, wdims, wstrides, wbox))) return st;
+  }
+  if (!s->tmaps) {
+    void* p = nullptr;
+    if ((st = dalloc(s, &p, sizeof(TileMaps)))) return st;
+    s->tmaps = static_cast<TileMaps*>(p);
+  }
+  AFAR_CUDA(cudaMemcpy(s->tmaps, &h, sizeof(TileMaps), cudaMemcpyHostToDevice));
+  return AFAR_OK;
+}
+
 static afar_status tune_reconstruct(afar_solver* s) {
   static std::mutex mu;
   static std::map<std::tuple<int, int, int, int>, int> cache;
@@ -931,6 +996,7 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
     const int ntile = (Nc + kTile - 1) / kTile;
     std::vector<uint8_t> ts(ntile, 0);
     for (int c = 0; c < Nc; ++c) ts[c / kTile] = std::max(ts[c / kTile], h->stencilSize[c]);
+    for (auto& v : ts) v = std::max<uint8_t>(v, 1);  // the tile kernel loads the boxes of stencil size v
     if ((st = dalloc_t(s, &s->tileS, (size_t)ntile))) return st;
     AFAR_CUDA(cudaMemcpy(s->tileS, ts.data(), ntile, cudaMemcpyHostToDevice));
   }
@@ -963,6 +1029,7 @@ extern "C" afar_status afar_setDeviceFieldDataStencil(afar_solver* s, const afar
   if (st) return st;
   if ((st = dalloc_t(s, &s->res_dbg, (size_t)Nc))) return st;
   AFAR_CUDA(cudaStreamSynchronize(s->stream));
+  if (s->policy == AFAR_POLICY_MIXED && (st = build_tile_maps(s))) return st;
   if (s->policy == AFAR_POLICY_MIXED && (st = tune_reconstruct(s))) return st;
   s->have_stencil = true;
   return AFAR_OK;
