@@ -247,7 +247,9 @@ afar_status afar_setDeviceFieldData(afar_solver* solver, const afar_fieldPointer
                                     int cellsNum, int facesNum, int totalBoundaryFacesNum);
 
 /* Replaces the 10-argument setDeviceFieldData (GPUevolve.h:16-27, GPUevolve.cu:67-148):
- * uploads the stencil/operator arrays and builds the least-squares matrix on the device. */
+ * uploads the stencil/operator arrays and builds the least-squares matrix on the device.  Mixed
+ * policy: also encodes the TMA tensor maps of the operator rows (cuTensorMapEncodeTiled through
+ * the runtime's driver entry point; AFAR_ERR_CUDA if the driver lacks it). */
 afar_status afar_setDeviceFieldDataStencil(afar_solver* solver, const afar_fieldPointer* host,
                                            int cellsNum, int facesNum, int patchesNum,
                                            int totalBoundaryFacesNum, int maxStencilSize,
