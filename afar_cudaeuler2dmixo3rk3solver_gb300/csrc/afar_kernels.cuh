@@ -887,6 +887,24 @@ __device__ __forceinline__ void bvd_body(const StageArgs<P>& a, const int blk) {
   a.lim[c] = L;
 }
 
+// The mixed policy's FP32 Courant estimate of one internal face (setDeltaT, reference
+// cudaFieldOperation.h:140-157): dt = CFL deltaR |Sf| / ((1-w)|U_o.Sf| + w|U_n.Sf| + c |Sf|),
+// c = sqrt(gamma R ((1-w) T_o + w T_n)).  Every rounding is written out, so the fused stage-1 flux
+// and the separate pass (afar_adjustTimeStep) give the same bits wherever the compiler places them.
+__device__ __forceinline__ float courant_den_f32(const float fraction, const float magSf, const float Sfx,
+                                                 const float Sfy, const V4<float>& Wo, const V4<float>& Wn,
+                                                 const float gRf) {
+  const float w0 = __fadd_rn(1.f, -fraction);
+  const float unL = fabsf(__fmaf_rn(Wo.y, Sfx, __fmul_rn(Wo.z, Sfy)));
+  const float unR = fabsf(__fmaf_rn(Wn.y, Sfx, __fmul_rn(Wn.z, Sfy)));
+  const float c = __fsqrt_rn(__fmul_rn(gRf, __fmaf_rn(w0, Wo.w, __fmul_rn(fraction, Wn.w))));
+  return __fmaf_rn(c, magSf, __fmaf_rn(w0, unL, __fmul_rn(fraction, unR)));
+}
+__device__ __forceinline__ float courant_dt_f32(const float cfl, const float deltaR, const float magSf,
+                                                const float den) {
+  return __fdiv_rn(__fmul_rn(__fmul_rn(cfl, deltaR), magSf), den);
+}
+
 // minimizeDeltaValue (reference cudaRiemannSolver.h:7-14)
 template <class D, class G>
 __device__ __forceinline__ D min_delta(const G l, const G r, const G lT, const G rT) {
@@ -1315,10 +1333,7 @@ __device__ __forceinline__ void flux_body(const StageArgs<P>& a, const int blk) 
       if constexpr (DT && kF32) {
         if (s_cfl_step) {  // setDeltaT, cudaFieldOperation.h:140-157, as an FP32 estimate
           const V2<float> g = a.dtgf[id];
-          const float deltaR = g.x, fraction = g.y;
-          dtf32 = s_cfl * deltaR * magSf /
-                  ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
-                   sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+          dtf32 = courant_dt_f32(s_cfl, g.x, magSf, courant_den_f32(g.y, magSf, Sfx, Sfy, Wo, Wn, a.gRf));
         }
       } else if (DT) {
         const StepCtl* ctl = a.ctl;
@@ -1616,8 +1631,9 @@ template <class P>
 __global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
   bvd_body<P>(a, blockIdx.x);
 }
+// mixed: 48 registers, 5 blocks an SM (the stage-1 form needs 52 unbounded, and 4 blocks)
 template <class P, bool DT>
-__global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
+__global__ void __launch_bounds__(256, P::id == PolicyMixed::id ? 5 : 1) k_flux(StageArgs<P> a) {
   flux_body<P, DT>(a, blockIdx.x);
 }
 template <class P>
@@ -1927,10 +1943,7 @@ __global__ void __launch_bounds__(256) k_delta_t_mixed(StageArgs<PolicyMixed> a,
     const V4<float> fs = a.fs[id];
     const float Sfx = fs.x, Sfy = fs.y, magSf = fs.z;
     const V2<float> g = a.dtgf[id];
-    const float deltaR = g.x, fraction = g.y;
-    dtf = cfl * deltaR * magSf /
-          ((1.f - fraction) * fabsf(Wo.y * Sfx + Wo.z * Sfy) + fraction * fabsf(Wn.y * Sfx + Wn.z * Sfy) +
-           sqrtf(a.gRf * ((1.f - fraction) * Wo.w + fraction * Wn.w)) * magSf);
+    dtf = courant_dt_f32(cfl, g.x, magSf, courant_den_f32(g.y, magSf, Sfx, Sfy, Wo, Wn, a.gRf));
   }
   unsigned v = (unsigned)__float_as_int(dtf);
   if (!(dtf >= 0.f)) v = 0x7F800000u;

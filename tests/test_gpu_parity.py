@@ -296,6 +296,26 @@ def test_tile_reconstruct_bitwise_equals_register_pass(cases, name):
     assert ta == tb
 
 
+def test_mixed_courant_step_same_bits_fused_and_separate(cases):
+    """The mixed policy's FP32 Courant estimate: the head of a step (the estimate fused into the
+    stage-1 flux, block minima) and the separate pass afar_adjustTimeStep runs for a batch member
+    (warp minima) give the same bits: both evaluate one estimate with every rounding written out."""
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import Batch
+
+    for name in ("quad_riemann", "ffs_tri", "mixed_riemann", "corner_flow"):
+        hf, cfg = cases[name]
+        s = _solver(hf, cfg, "mixed")
+        s.run(3)
+        fused = s.set_delta_t()  # the head of the coming step; the state does not change
+        b = Batch("mixed")
+        s.set_step_params()
+        b.add(s)
+        separate = s.set_delta_t()  # a batch member: the separate Courant pass
+        assert separate == fused and 0.0 < fused < 1.0, name
+        b.close()
+        s.close()
+
+
 @pytest.mark.parametrize("policy", ["ref", "mixed"])
 def test_switch_counts_match_the_flags(cases, policy):
     """afar_switch_counts against counts taken on the host from the downloaded flags."""
