@@ -325,9 +325,11 @@ __device__ __forceinline__ void recon_reg_body(const StageArgs<P>& a, const int 
 // ---------------------------------------------------------------- mixed reconstruct, tile-staged
 // One CTA per 128-cell tile.  The tile's slice of every per-cell operator row (face ids, LS rows,
 // face offsets, (dr, fraction), stencil ids, O3 weights) and the cells' own states are contiguous
-// 128-element runs of the slot-major arrays, so the CTA fetches them with bulk copies (TMA unit,
-// one mbarrier) instead of per-thread loads: ~50 KB per tile in flight from a handful of lanes,
-// while registers stay free for the stencil gathers, which hit L2.
+// 128-element runs of the slot-major arrays, so the CTA fetches them with the TMA unit (one tiled
+// load per array from its tensor map, one bulk copy of the states, two mbarriers) instead of
+// per-thread loads: ~50 KB per tile in flight from seven lanes, while registers stay free for the
+// stencil gathers, which hit L2.  One load per array rather than one per row: the fetch was bound
+// by the number of copies issued, not by their bytes.
 constexpr int kTile = 128;
 // Test hooks of the tile's bounded waits (afar_debug_wait_injection): the wait limit in SM clocks,
 // and bytes added to the transaction count the first barrier of every tile expects (never issued,

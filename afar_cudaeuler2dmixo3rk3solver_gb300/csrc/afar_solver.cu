@@ -678,7 +678,7 @@ static afar_status get_state(afar_solver* s, afar_basicFieldData* FD, afar_conse
 }
 
 // The project autotuner: the mixed reconstruct has two implementations whose speed depends on the
-// mesh (stencil size, faces per cell, size): the tile-staged kernel (bulk copies of each 128-cell
+// mesh (stencil size, faces per cell, size): the tile-staged kernel (TMA loads of each 128-cell
 // tile's operator rows into shared memory) and the register pass (no shared memory, more tiles per
 // SM).  At the stencil upload each is timed on the solver's own data (one warm-up, best of three
 // launches, CUDA events on its stream; the launches only write the stage's intermediates) and the

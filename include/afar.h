@@ -492,7 +492,7 @@ afar_status afar_get_tuning(afar_solver* solver, int* reconVariant, float* msTil
 afar_status afar_measure_fp64_peak(int device, double* gflops, float* ms);
 
 /* Test hook for the bounded device waits (no counterpart in the reference).  The mixed policy's
- * tile-staged reconstruct waits on mbarriers for its bulk copies; each wait gives up after a limit
+ * tile-staged reconstruct waits on mbarriers for its TMA loads; each wait gives up after a limit
  * of SM clocks (2^31, about a second), marks the solver's error word and lets the kernel return, so
  * that the call which waits next returns AFAR_ERR_CUDA ("... the state is not valid") and the CUDA
  * context stays usable.  extraBytes > 0 adds that many bytes to the transaction count the first
