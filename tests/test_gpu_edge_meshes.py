@@ -3,7 +3,9 @@ with no internal face (every stencil member a ghost), 130 cells (one full 128-ce
 ragged second one), and a one-cell-high strip of 257 cells (every cell on the boundary, two full
 tiles and one cell).  A fixed step size, since a mesh without internal faces has no CFL step.
 Policies: fp64 within 1e-10 of the FP64 oracle, ref within 1e-12 of the oracle in the face values
-and gradients with identical flags, mixed within 1e-5 of the fp64 policy after whole steps."""
+and gradients with identical flags, mixed within 1e-5 of the fp64 policy after whole steps, and its
+tile-staged reconstruct (TMA boxes of 128 cells reaching past the rows' ends, which read zeros)
+bitwise equal to its register pass."""
 import numpy as np
 import pytest
 
@@ -110,3 +112,19 @@ def test_mixed_policy_close_to_fp64(cases, name):
     a, b = res["mixed"]["FD"][:hf.nc], res["fp64"]["FD"][:hf.nc]
     assert np.isfinite(a).all()
     assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_mixed_tile_reconstruct_equals_register_pass(cases, name):
+    from afar_cudaeuler2dmixo3rk3solver_gb300 import CudaSolver
+
+    hf, cfg = cases[name]
+    res = []
+    for variant in (0, 1):  # tile-staged, register pass
+        s = CudaSolver(hf, cfg, policy="mixed")
+        s.set_tuning(variant)
+        s.run(5, dt=DT)
+        res.append(s.state())
+        s.close()
+    for k in ("FD", "cFD", "shockIndicator"):
+        assert np.array_equal(res[0][k], res[1][k]), k
