@@ -1633,10 +1633,20 @@ template <class P>
 __global__ void __launch_bounds__(128) k_bvd(StageArgs<P> a) {
   bvd_body<P>(a, blockIdx.x);
 }
-// mixed: 48 registers, 5 blocks an SM (the stage-1 form needs 52 unbounded, and 4 blocks)
 template <class P, bool DT>
-__global__ void __launch_bounds__(256, P::id == PolicyMixed::id ? 5 : 1) k_flux(StageArgs<P> a) {
+__global__ void __launch_bounds__(256) k_flux(StageArgs<P> a) {
   flux_body<P, DT>(a, blockIdx.x);
+}
+// mixed: 48 registers, 5 blocks an SM (the stage-1 form takes 54 unbounded, and 4 blocks).  The
+// bound is for this policy only: a minimum-blocks bound of 1 on the FP64 policies lets ptxas take
+// up to 162 registers (one block an SM) where the plain bound keeps 80-120.
+template <>
+__global__ void __launch_bounds__(256, 5) k_flux<PolicyMixed, false>(StageArgs<PolicyMixed> a) {
+  flux_body<PolicyMixed, false>(a, blockIdx.x);
+}
+template <>
+__global__ void __launch_bounds__(256, 5) k_flux<PolicyMixed, true>(StageArgs<PolicyMixed> a) {
+  flux_body<PolicyMixed, true>(a, blockIdx.x);
 }
 template <class P>
 __global__ void __launch_bounds__(128) k_update(StageArgs<P> a, const StageCoef k) {
