@@ -1839,31 +1839,45 @@ __global__ void __launch_bounds__(256) k_flux_gauss(StageArgs<P> a) {
 // tab[map[b].x]), as that solve's block map[b].y.  A block never spans two solves, so block-level
 // reductions (the CFL minimum, the step size) stay within one solve, and a solve's result does not
 // depend on which other solves share the batch.
+//
+// A block first copies its member's arguments from the table into shared memory (one coalesced
+// read of the entry), so the body reads every pointer and constant at shared-memory latency instead
+// of one dependent load through L1 per field (the single-solve kernels have them in the parameter
+// bank).  Every thread of the block takes part: call it before any thread can leave.
+template <class P>
+__device__ __forceinline__ const StageArgs<P>& member_args(const StageArgs<P>* __restrict__ tab, const int i) {
+  static_assert(sizeof(StageArgs<P>) % 4 == 0, "the argument block is copied as 32-bit words");
+  __shared__ __align__(16) unsigned raw[sizeof(StageArgs<P>) / 4];
+  const unsigned* src = reinterpret_cast<const unsigned*>(tab + i);
+  for (int w = threadIdx.x; w < (int)(sizeof(StageArgs<P>) / 4); w += blockDim.x) raw[w] = __ldg(src + w);
+  __syncthreads();
+  return *reinterpret_cast<const StageArgs<P>*>(raw);
+}
 template <class P, int NF>
 __global__ void __launch_bounds__(kTile, 4) kb_reconstruct_tile(const StageArgs<P>* __restrict__ tab,
                                                                 const int2* __restrict__ map) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int2 m = map[blockIdx.x];
-  recon_tile_body<P, NF>(tab[m.x], m.y, sm);
+  recon_tile_body<P, NF>(member_args(tab, m.x), m.y, sm);
 }
 template <class P>
 __global__ void __launch_bounds__(128) kb_reconstruct_staged(const StageArgs<P>* __restrict__ tab,
                                                              const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
-  recon_staged_body<P>(tab[m.x], m.y);
+  recon_staged_body<P>(member_args(tab, m.x), m.y);
 }
 template <>
 __global__ void __launch_bounds__(128, 4) kb_reconstruct_staged<PolicyFP64>(const StageArgs<PolicyFP64>* __restrict__ tab,
                                                                             const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
-  recon_staged_body<PolicyFP64>(tab[m.x], m.y);
+  recon_staged_body<PolicyFP64>(member_args(tab, m.x), m.y);
 }
 // the register-pass reconstruct of the mixed policy over the members the autotuner gave it
 template <class P>
 __global__ void __launch_bounds__(128, 5) kb_reconstruct_reg(const StageArgs<P>* __restrict__ tab,
                                                             const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
-  recon_reg_body<P>(tab[m.x], m.y);
+  recon_reg_body<P>(member_args(tab, m.x), m.y);
 }
 // BVD and flux in blocks of B threads (the batch autotuner's choice; the map's blocks are B cells
 // or faces of one member).  mixed BVD: 32 registers, the full 64 warps per SM; fp64: 40 warps.
@@ -1871,18 +1885,18 @@ template <class P, int B>
 __global__ void __launch_bounds__(B, (P::id == PolicyMixed::id ? 2048 : 1280) / B) kb_bvd(
     const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
-  bvd_body<P>(tab[m.x], m.y);
+  bvd_body<P>(tab[m.x], m.y);  // staging its arguments cost more than it saved (32 registers)
 }
 template <class P, bool DT, int B>
 __global__ void __launch_bounds__(B) kb_flux(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map) {
   const int2 m = map[blockIdx.x];
-  flux_body<P, DT>(tab[m.x], m.y);
+  flux_body<P, DT>(member_args(tab, m.x), m.y);
 }
 template <class P>
 __global__ void __launch_bounds__(128) kb_update(const StageArgs<P>* __restrict__ tab, const int2* __restrict__ map,
                                                  const StageCoef k) {
   const int2 m = map[blockIdx.x];
-  update_body<P>(tab[m.x], m.y, k);
+  update_body<P>(member_args(tab, m.x), m.y, k);
 }
 
 // Closes a step: advance time, record the step, re-arm the CFL minimum for the next step.
