@@ -41,8 +41,8 @@ PROFILE_STEPS = 10
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one mixed-policy reconstruct launch
 # (tile-staged) per cell, by cell order, from ncu captures of the 500,094-cell version of this
 # workload (traffic grows with the cells of the tile stream); None when no capture matches the
-# current kernels.
-RECON_TRAFFIC_BYTES_PER_CELL = {"rcm": 399.1, "hilbert": 398.5}
+# current kernels (the tensor-map fetch; Hilbert order not captured with it).
+RECON_TRAFFIC_BYTES_PER_CELL = {"rcm": 398.2, "hilbert": None}
 # FP64 work per internal face of the fp64 policy's flux, averaged over a step's three launches (the
 # first also reduces the Courant step), from the ncu instruction counts
 # smsp__sass_thread_inst_executed_op_{dfma,dadd,dmul}_pred_on.sum of the three launches on the
