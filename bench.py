@@ -85,6 +85,8 @@ def parse():
                     help="the batched workload instead: many independent solves stepped by one graph")
     ap.add_argument("--batch-solves", type=int, default=256)
     ap.add_argument("--batch-steps", type=int, default=500)
+    ap.add_argument("--batch-no-solo", action="store_true",
+                    help="--batch: skip timing the solves one after another (e.g. for a launch list of the batch kernels)")
     ap.add_argument("--setup", action="store_true",
                     help="time the precompute of the workload's mesh on the host and with its RBF stage on the GPU")
     ap.add_argument("--accuracy", default="",
@@ -1134,6 +1136,8 @@ def run_batch(args, dist: Dist):
     solo_ms = 0.0
     for s in solvers:
         s.save()
+        if args.batch_no_solo:
+            continue
         s.run_timed(3)
         s.restore()
         solo_ms += s.run_timed(40) / 40.0
@@ -1162,8 +1166,9 @@ def run_batch(args, dist: Dist):
         "config": {"workload": "batch_wedges", "solves": args.batch_solves, "cells": int(cells.sum()),
                    "steps": args.batch_steps, "policy": "mixed", "launches_per_step": 13, "setup_s": round(setup_s, 1)},
         "schedule": schedule,
-        "one_after_another": {"value": float(cells.sum()) / (solo_ms * 1e-3), "ms_per_step": solo_ms,
-                              "launches_per_step": 13 * args.batch_solves},
+        "one_after_another": None if args.batch_no_solo else {
+            "value": float(cells.sum()) / (solo_ms * 1e-3), "ms_per_step": solo_ms,
+            "launches_per_step": 13 * args.batch_solves},
         "finite": finite,
     }), flush=True)
 
